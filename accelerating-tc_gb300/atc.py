@@ -1,0 +1,334 @@
+"""Python binding of libatc's C ABI (include/atc.h), used by the tests and bench.py.
+
+The binding is a thin ctypes layer: it loads the in-tree libatc.so and raises
+ATCError when the library is missing or a call fails — there is no Python or CPU
+fallback for any entry point.  Host arrays are numpy int32 arrays of shape (m, 2).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libatc.so")
+ROOT = os.path.dirname(HERE)
+HEADER = os.path.join(ROOT, "include", "atc.h")
+
+
+class ATCError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (Status(status).name if status in Status._value2member_map_ else "?", status, msg))
+        self.status = status
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    ERR_INVALID = 1
+    ERR_OOM = 2
+    ERR_CUDA = 3
+    ERR_TIMEOUT = 4
+    ERR_UNSUPPORTED = 5
+
+
+class Dir(enum.IntEnum):
+    ID = 0
+    DEGREE = 1
+    DEGREE_LOWID = 2
+    ADIRECTION = 3
+
+
+class Order(enum.IntEnum):
+    NONE = 0
+    AORDER = 1
+
+
+class Kernel(enum.IntEnum):
+    AUTO = 0
+    HU = 1
+    BISSON = 2
+    FOX = 3
+    TRICORE = 4
+
+
+class Tuning(C.Structure):
+    _fields_ = [
+        ("prune_deg1", C.c_int32),
+        ("hu_blocks", C.c_int32),
+        ("hu_stage_ints", C.c_int32),
+        ("bisson_cutover", C.c_int32),
+        ("fox_rearrange", C.c_int32),
+        ("fox_work_per_thread", C.c_int32),
+        ("tricore_blocks", C.c_int32),
+        ("reserved", C.c_int32 * 9),
+    ]
+
+
+class CSRStruct(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("m", C.c_int64),
+        ("offsets", C.c_void_p),
+        ("cols", C.c_void_p),
+        ("n_input", C.c_int64),
+        ("wedges", C.c_int64),
+        ("dir", C.c_int32),
+        ("order", C.c_int32),
+        ("pruned", C.c_int32),
+        ("max_outdeg", C.c_int32),
+        ("priv", C.c_void_p),
+    ]
+
+
+class StatsStruct(C.Structure):
+    _fields_ = [
+        ("kernel_ms", C.c_float),
+        ("total_ms", C.c_float),
+        ("alg_bytes", C.c_uint64),
+        ("wedges", C.c_uint64),
+        ("kernel_used", C.c_int32),
+        ("launches", C.c_int32),
+    ]
+
+
+@dataclass
+class Stats:
+    kernel_ms: float
+    total_ms: float
+    alg_bytes: int
+    wedges: int
+    kernel_used: int
+    launches: int
+
+
+_lib = None
+
+_P = C.c_void_p
+_I32P = C.POINTER(C.c_int32)
+_SIGS = {
+    "atc_version": (C.c_char_p, []),
+    "atc_status_string": (C.c_char_p, [C.c_int]),
+    "atc_last_error": (C.c_char_p, []),
+    "atc_init": (C.c_int, [C.c_int]),
+    "atc_gen_rmat_host": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, C.c_int]),
+    "atc_gen_rmat_device": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P]),
+    "atc_simplify_host": (C.c_int, [_P, C.c_uint64, C.c_int, _P, C.POINTER(C.c_uint64)]),
+    "atc_pretc": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
+    "atc_pretc_device": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
+    "atc_csr_to_host": (C.c_int, [C.POINTER(CSRStruct), _P, _P, _P]),
+    "atc_csr_free": (C.c_int, [C.POINTER(CSRStruct)]),
+    "atc_adirection": (C.c_int, [_P, C.c_uint64, _P, C.POINTER(C.c_uint64), _P, _P]),
+    "atc_aorder": (C.c_int, [_P, C.c_uint64, _P, _P, _P, _P]),
+    "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
+    "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
+    "atc_costfunc": (C.c_int, [_P, C.c_uint64, C.c_int32, _P, _P]),
+    "atc_verification": (C.c_int, [_P, C.c_uint64, _P, _P]),
+}
+
+
+def lib():
+    """Loads libatc.so (built by build.py); raises ATCError when it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ATCError(Status.ERR_UNSUPPORTED, "libatc.so not built: run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != 0:
+        raise ATCError(status, lib().atc_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _pairs(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    if a.ndim == 1:
+        a = a.reshape(-1, 2)
+    assert a.ndim == 2 and a.shape[1] == 2
+    return a
+
+
+def version():
+    return lib().atc_version().decode()
+
+
+def init(device=0):
+    _check(lib().atc_init(device))
+
+
+GRAPH500 = (570000, 190000, 190000)
+
+
+def gen_rmat(scale, edge_factor=16, seed=1, abc=GRAPH500, nthreads=None):
+    """Raw R-MAT samples (edge_factor * 2^scale pairs) generated on the host."""
+    n = edge_factor << scale
+    out = np.empty((n, 2), dtype=np.int32)
+    _check(lib().atc_gen_rmat_host(scale, edge_factor, abc[0], abc[1], abc[2], seed, _ptr(out),
+                                    nthreads or os.cpu_count() or 1))
+    return out
+
+
+def simplify(pairs, symmetric=True):
+    """Loop-free, duplicate-free edges: (min,max) once, or both directions sorted."""
+    p = _pairs(pairs)
+    out = np.empty((p.shape[0] * (2 if symmetric else 1), 2), dtype=np.int32)
+    n = C.c_uint64(0)
+    _check(lib().atc_simplify_host(_ptr(p), p.shape[0], 1 if symmetric else 0, _ptr(out), C.byref(n)))
+    return out[: n.value].copy()
+
+
+def rmat_graph(scale, edge_factor=16, seed=1, symmetric=True):
+    """The benchmarks' input: seeded R-MAT, symmetrised, loops and repeats removed."""
+    return simplify(gen_rmat(scale, edge_factor, seed), symmetric=symmetric)
+
+
+class CSR:
+    """Device-resident oriented CSR owned by libatc; freed with free() or on GC."""
+
+    def __init__(self, st: CSRStruct, perm=None):
+        self._st = st
+        self.perm = perm
+
+    @property
+    def n(self):
+        return self._st.n
+
+    @property
+    def m(self):
+        return self._st.m
+
+    @property
+    def wedges(self):
+        return self._st.wedges
+
+    @property
+    def max_outdeg(self):
+        return self._st.max_outdeg
+
+    @property
+    def struct(self):
+        return self._st
+
+    def to_host(self, stream=None):
+        off = np.empty(self.n + 1, dtype=np.int64)
+        cols = np.empty(self.m, dtype=np.int32)
+        _check(lib().atc_csr_to_host(C.byref(self._st), _ptr(off), _ptr(cols), stream))
+        return off, cols
+
+    def free(self):
+        if self._st is not None and self._st.offsets is not None:
+            lib().atc_csr_free(C.byref(self._st))
+        self._st = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _tuning(t):
+    if t is None:
+        return None
+    if isinstance(t, Tuning):
+        return C.byref(t)
+    tt = Tuning()
+    for k, v in t.items():
+        setattr(tt, k, v)
+    return C.byref(tt)
+
+
+def pretc(pairs, dir=Dir.DEGREE, order=Order.NONE, tuning=None, want_perm=False, stream=None):
+    p = _pairs(pairs)
+    st = CSRStruct()
+    perm = None
+    if want_perm:
+        nin = int(p.max()) + 1 if p.size else 0
+        perm = np.empty(max(nin, 1), dtype=np.int32)
+    _check(lib().atc_pretc(_ptr(p), p.shape[0], int(dir), int(order), _tuning(tuning), C.byref(st),
+                           _ptr(perm), stream))
+    return CSR(st, perm)
+
+
+def pretc_device(pairs_dev_ptr, n_pairs, dir=Dir.DEGREE, order=Order.NONE, tuning=None, stream=None):
+    st = CSRStruct()
+    _check(lib().atc_pretc_device(C.c_void_p(pairs_dev_ptr), n_pairs, int(dir), int(order), _tuning(tuning),
+                                  C.byref(st), None, stream))
+    return CSR(st)
+
+
+def _stats(s: StatsStruct):
+    return Stats(s.kernel_ms, s.total_ms, s.alg_bytes, s.wedges, s.kernel_used, s.launches)
+
+
+def tc(csr: CSR, kernel=Kernel.AUTO, tuning=None, stream=None):
+    cnt = C.c_uint64(0)
+    st = StatsStruct()
+    _check(lib().atc_tc(C.byref(csr.struct), int(kernel), _tuning(tuning), C.byref(cnt), C.byref(st), stream))
+    return cnt.value, _stats(st)
+
+
+def kcl(csr: CSR, k, stream=None):
+    cnt = C.c_uint64(0)
+    st = StatsStruct()
+    _check(lib().atc_kcl(C.byref(csr.struct), k, C.byref(cnt), C.byref(st), stream))
+    return cnt.value, _stats(st)
+
+
+def adirection(pairs, want_prio=False, stream=None):
+    p = _pairs(pairs)
+    out = np.empty((max(p.shape[0], 1), 2), dtype=np.int32)
+    n = C.c_uint64(0)
+    prio = None
+    if want_prio:
+        prio = np.empty(int(p.max()) + 1 if p.size else 1, dtype=np.int32)
+    _check(lib().atc_adirection(_ptr(p), p.shape[0], _ptr(out), C.byref(n), _ptr(prio), stream))
+    res = out[: n.value].copy()
+    return (res, prio) if want_prio else res
+
+
+def aorder(pairs, stream=None):
+    """Returns (lookup, normal, reordered) exactly as the A-order program computes them."""
+    p = _pairs(pairs)
+    nin = int(p.max()) + 1 if p.size else 1
+    lookup = np.empty(nin, dtype=np.int32)
+    normal = np.empty_like(p)
+    reordered = np.empty_like(p)
+    _check(lib().atc_aorder(_ptr(p), p.shape[0], _ptr(lookup), _ptr(normal), _ptr(reordered), stream))
+    return lookup, normal, reordered
+
+
+def costfunc(pairs, k, stream=None):
+    p = _pairs(pairs)
+    out = np.zeros(3, dtype=np.float32)
+    _check(lib().atc_costfunc(_ptr(p), p.shape[0], k, _ptr(out), stream))
+    return out
+
+
+def verification(pairs, stream=None):
+    p = _pairs(pairs)
+    out = np.zeros(2, dtype=np.float32)
+    _check(lib().atc_verification(_ptr(p), p.shape[0], _ptr(out), stream))
+    return out
+
+
+def header_symbols():
+    """Names of every function declared in include/atc.h."""
+    import re
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(atc_[a-z0-9_]+)\s*\(", txt)))

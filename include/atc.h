@@ -1,0 +1,182 @@
+/*
+ * atc.h — C ABI of libatc, the GB300 (sm_103a) triangle-counting library.
+ *
+ * The reference (pkumod/accelerating-TC) ships stand-alone programs whose in-process
+ * interfaces are process globals filled by `preProcess` and `__constant__` pointer
+ * symbols read by the kernels.  This header replaces them with reentrant calls on
+ * plain pointers and sizes; each declaration names the reference interface it stands
+ * for.  All entry points return an atc_status and never abort the process.
+ *
+ * Ownership: the library owns every device buffer reachable from an atc_csr and frees
+ * it in atc_csr_free.  Callers own their input arrays.  Host pointers are plain
+ * pageable or pinned memory; "_device" variants take device pointers.  Streams are
+ * cudaStream_t values passed as void* (NULL = the legacy default stream); every call
+ * that returns a host result synchronises its stream before returning.
+ *
+ * Vertex ids are int32 >= 0; an input pair is two consecutive int32 {src, dst}, the
+ * little-endian layout of the reference's binary edge files (Hu/preTC.cu:29-32,84).
+ */
+#ifndef ATC_H_
+#define ATC_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* atc_stream; /* a cudaStream_t */
+
+typedef enum atc_status {
+  ATC_OK = 0,
+  ATC_ERR_INVALID = 1,     /* bad argument: negative id, NULL pointer, bad enum, ... */
+  ATC_ERR_OOM = 2,         /* device or host allocation failed */
+  ATC_ERR_CUDA = 3,        /* a CUDA runtime call failed (message: atc_last_error) */
+  ATC_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
+  ATC_ERR_UNSUPPORTED = 5  /* input outside what the algorithm defines (see the call) */
+} atc_status;
+
+/* Edge orientation.  Every rule is acyclic, so the count is the same for all. */
+typedef enum atc_dir {
+  /* u -> v iff u > v: N+(u) holds the smaller ids (Bisson/preTC.cu:135-144, chooseIndex 0;
+     Fox/preTC.cu:92-101). */
+  ATC_DIR_ID = 0,
+  /* lower degree -> higher degree; equal degrees: the larger id is the source
+     (Hu/preTC.cu:125-133; A-order.cpp:88-99). */
+  ATC_DIR_DEGREE = 1,
+  /* lower degree -> higher degree; equal degrees: the smaller id is the source
+     (tricore/src/tricount_gpu.cu:69-80). */
+  ATC_DIR_DEGREE_LOWID = 2,
+  /* A-direction: peel priorities, u -> v iff prio[v] > prio[u] or (equal and u < v)
+     (edge_directing/A-direction-seri.cpp:35-153, 254-273). */
+  ATC_DIR_ADIRECTION = 3
+} atc_dir;
+
+typedef enum atc_order {
+  ATC_ORDER_NONE = 0,
+  /* A-order relabelling (vertex_ordering/A-order/A-order.cpp:62-247). */
+  ATC_ORDER_AORDER = 1
+} atc_order;
+
+typedef enum atc_kernel {
+  ATC_KERNEL_AUTO = 0,    /* library default for the graph */
+  ATC_KERNEL_HU = 1,      /* vertex-range wedge walk, staged N+(u) (Hu/tc.cu:69-201) */
+  ATC_KERNEL_BISSON = 2,  /* bitmap for large N+(u), search otherwise (Bisson/tc.cu:18-104) */
+  ATC_KERNEL_FOX = 3,     /* edge bins with 1..32 threads per edge (Fox/tc.cu:64-125,316-384) */
+  ATC_KERNEL_TRICORE = 4  /* warp per edge, 32 pivots + binary search (tricount_gpu.cu:215-290) */
+} atc_kernel;
+
+/* Tuning knobs; zero means "library default".  The reference hard-codes these as
+   #defines (Hu/tc.cu:6-8, Bisson/tc.cu:5-6, Fox/tc.cu:318-319, tricount_gpu.cu:24-25). */
+typedef struct atc_tuning {
+  int32_t prune_deg1;        /* drop degree<=1 vertices, compact ids (Hu/preTC.cu:135-169) */
+  int32_t hu_blocks;         /* CTAs of the Hu-style kernel (0: 8 per SM) */
+  int32_t hu_stage_ints;     /* ints of N+(u) staged in shared memory per CTA */
+  int32_t bisson_cutover;    /* out-degree above which the bitmap path is taken (32) */
+  int32_t fox_rearrange;     /* interleave each bin's edges (Fox/tc.cu:127-183) */
+  int32_t fox_work_per_thread; /* bin base of the threads-per-edge bins (8) */
+  int32_t tricore_blocks;    /* CTAs of the TriCore-style kernel (0: auto) */
+  int32_t reserved[9];
+} atc_tuning;
+
+/* Oriented CSR on the device (the reference's edgeOffset/edgeRow/adjLength globals,
+   Hu/preTC.cu:59-62).  Lists are sorted ascending and duplicate-free. */
+typedef struct atc_csr {
+  int64_t n;            /* vertices of the counted graph */
+  int64_t m;            /* oriented edges */
+  int64_t* offsets;     /* device, n+1 */
+  int32_t* cols;        /* device, m */
+  int64_t n_input;      /* max input id + 1 */
+  int64_t wedges;       /* W = sum_v indeg(v) * outdeg(v) */
+  int32_t dir;          /* atc_dir used */
+  int32_t order;        /* atc_order used */
+  int32_t pruned;       /* 1 when degree<=1 vertices were removed */
+  int32_t max_outdeg;
+  void* priv;           /* library-internal */
+} atc_csr;
+
+typedef struct atc_stats {
+  float kernel_ms;       /* device time of the counting kernels (events on the stream) */
+  float total_ms;        /* device time of the whole call */
+  uint64_t alg_bytes;    /* 4(n+1) + 4m + 4W + 8: the bytes every kernel family must read */
+  uint64_t wedges;       /* W of the counted CSR */
+  int32_t kernel_used;   /* atc_kernel actually run */
+  int32_t launches;      /* kernel launches made by the call */
+} atc_stats;
+
+/* ---- library ---------------------------------------------------------------- */
+const char* atc_version(void);
+const char* atc_status_string(atc_status s);
+/* Text of the last error on the calling thread (CUDA message or argument check). */
+const char* atc_last_error(void);
+/* Makes `device` current on the calling thread and initialises its context. */
+atc_status atc_init(int device);
+
+/* ---- synthetic inputs (deterministic, integer-only; no GPU needed for _host) --- */
+/* R-MAT, 2^scale vertices, edge_factor*2^scale samples, quadrant probabilities in
+   parts per million (Graph500: 570000, 190000, 190000).  Writes the raw samples. */
+atc_status atc_gen_rmat_host(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm,
+                             uint32_t c_ppm, uint64_t seed, int32_t* out_pairs, int nthreads);
+atc_status atc_gen_rmat_device(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm,
+                               uint32_t c_ppm, uint64_t seed, int32_t* out_pairs_dev, atc_stream s);
+/* Drops self-loops and repeats; writes each undirected edge once as (min,max) sorted,
+   or, with symmetric != 0, both directions sorted by (src,dst).  Capacity of `out`:
+   2*n_pairs pairs when symmetric, else n_pairs. */
+atc_status atc_simplify_host(const int32_t* pairs, uint64_t n_pairs, int symmetric,
+                             int32_t* out, uint64_t* n_out);
+
+/* ---- preTC: edge list -> oriented CSR on the device -----------------------------
+   Replaces bool preProcess(const char*, unsigned& edgeNum, unsigned& nodeNum[, ...])
+   (Hu/preTC.cu:64, Bisson/preTC.cu:77, Fox/preTC.cu:64) and TriCore's cal_degree /
+   redirect_edges / split (tricore/include/tricount.h:9-15).  Self-loops and repeated
+   pairs are dropped; degrees are those of the resulting simple graph.  With
+   ATC_ORDER_AORDER the vertices are first relabelled by A-order computed on the
+   simple graph, then oriented by `dir` on the new ids; `perm_out` (nullable, n_input
+   ints) receives the new id of every input id.  Returns ATC_ERR_UNSUPPORTED when
+   A-order is asked for on a graph where the reference A-order indexes outside its
+   arrays (see atc_aorder). */
+atc_status atc_pretc(const int32_t* pairs, uint64_t n_pairs, atc_dir dir, atc_order order,
+                     const atc_tuning* tuning, atc_csr* out, int32_t* perm_out, atc_stream s);
+atc_status atc_pretc_device(const int32_t* pairs_dev, uint64_t n_pairs, atc_dir dir, atc_order order,
+                            const atc_tuning* tuning, atc_csr* out, int32_t* perm_out, atc_stream s);
+/* Copies the CSR to host arrays (n+1 int64, m int32). */
+atc_status atc_csr_to_host(const atc_csr* csr, int64_t* offsets, int32_t* cols, atc_stream s);
+atc_status atc_csr_free(atc_csr* csr);
+
+/* ---- orientation and ordering as drop-ins for the reference programs ------------ */
+/* A-direction-seri <file> (edge_directing/A-direction-seri.cpp:170-288): writes the
+   oriented edge list (the bytes of lpBasedGraph.bin; capacity 2*n_pairs pairs) and,
+   if non-NULL, the peel priorities (max id + 1 ints). */
+atc_status atc_adirection(const int32_t* pairs, uint64_t n_pairs, int32_t* oriented_out,
+                          uint64_t* n_out, int32_t* prio_out, atc_stream s);
+/* A-order <file> (vertex_ordering/A-order/A-order.cpp:62-247) on the raw pairs,
+   repeats included: `lookup` (max id + 1 ints) = new id of every id (badLookUpTable);
+   `normal` / `reordered` (n_pairs pairs each, nullable) = the two output files.
+   ATC_ERR_UNSUPPORTED where the reference reads outside its arrays: no vertex of
+   runtime degree 2..4 or none of 5 or more (memoryDominatePos == 0, :111-119,144), or
+   more degree-2..4 vertices than the whole 40-vertex buckets hold (:165-177). */
+atc_status atc_aorder(const int32_t* pairs, uint64_t n_pairs, int32_t* lookup, int32_t* normal,
+                      int32_t* reordered, atc_stream s);
+
+/* ---- counting --------------------------------------------------------------------
+   Triangle count of the oriented CSR: sum_u sum_{v in N+(u)} |N+(u) ∩ N+(v)|, exact in
+   uint64.  Replaces the kernels' launch + host reduction in Hu/tc.cu:317-323,
+   Bisson/tc.cu:198-204, Fox/tc.cu:334-384, tricount_gpu.cu:337-408. */
+atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning,
+                  uint64_t* count, atc_stats* stats, atc_stream s);
+/* k-clique count (k >= 3) of the oriented CSR, exact in uint64.  Replaces
+   kcl_gpu_solver(std::string, unsigned k, AccType& total, size_t) (k-clique/kcl.h:6-7). */
+atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream s);
+
+/* ---- orientation-cost figures ----------------------------------------------------- */
+/* costFuncCal <file> <k> (tools/costFuncCal.cpp:15-88): out = {idPartCost,
+   degreePartCost, lpPartCost}, float sums in vertex order as the tool prints them. */
+atc_status atc_costfunc(const int32_t* pairs, uint64_t n_pairs, int32_t k, float* out, atc_stream s);
+/* verification <text file> (tools/verification.cpp:11-61) on already-parsed pairs:
+   out = {f_lp, f_degree}. */
+atc_status atc_verification(const int32_t* pairs, uint64_t n_pairs, float* out, atc_stream s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATC_H_ */

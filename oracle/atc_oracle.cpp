@@ -1,0 +1,599 @@
+// CPU ORACLE — TEST INFRASTRUCTURE ONLY.
+//
+// A plain C++ restatement of the reference's algorithms on the triangle-counting
+// path.  tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference leg
+// load it as the checker; the product library never links, loads or calls it.
+//
+// Pinning: tests/golden/golden.json holds the outputs of the reference's own CPU
+// programs (A-direction-seri, A-order, costFuncCal, verification and the other_order
+// OrgTriangleCount), compiled from their unmodified sources by oracle/Makefile and
+// run on seeded graphs by tests/golden/make_golden.py.  tests/test_oracle_golden.py
+// checks every function below against those fixtures.
+//
+// Every function cites the reference file:line it restates (paths are relative to
+// the pkumod/accelerating-TC tree).
+//
+// Build: g++ -O2 -std=c++17 -fPIC -shared -ffp-contract=off -pthread
+// (-ffp-contract=off keeps float arithmetic identical on x86-64 and aarch64.)
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <iterator>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Simple undirected graph: symmetric adjacency, each list sorted ascending,
+// duplicates and self-loops removed.  Vertex count = max id + 1 over all pairs
+// (self-loop-only vertices included), as every reference reader computes it
+// (Hu/preTC.cu:90-113, A-direction-seri.cpp:187-192, A-order.cpp:68-74).
+// ---------------------------------------------------------------------------
+struct Adj {
+  int64_t n = 0;
+  std::vector<int64_t> off;  // n + 1
+  std::vector<int32_t> nbr;  // off[n]
+};
+
+int64_t max_id(const int32_t* p, uint64_t np) {
+  int64_t mx = -1;
+  for (uint64_t i = 0; i < 2 * np; ++i) mx = std::max<int64_t>(mx, p[i]);
+  return mx;
+}
+
+Adj build_adj(const int32_t* p, uint64_t np) {
+  Adj g;
+  g.n = max_id(p, np) + 1;
+  std::vector<int64_t> cnt(g.n + 1, 0);
+  for (uint64_t i = 0; i < np; ++i) {
+    int32_t s = p[2 * i], d = p[2 * i + 1];
+    if (s == d) continue;
+    cnt[s + 1]++;
+    cnt[d + 1]++;
+  }
+  for (int64_t v = 0; v < g.n; ++v) cnt[v + 1] += cnt[v];
+  std::vector<int32_t> tmp(cnt[g.n]);
+  std::vector<int64_t> cur(cnt.begin(), cnt.end() - 1);
+  for (uint64_t i = 0; i < np; ++i) {
+    int32_t s = p[2 * i], d = p[2 * i + 1];
+    if (s == d) continue;
+    tmp[cur[s]++] = d;
+    tmp[cur[d]++] = s;
+  }
+  g.off.assign(g.n + 1, 0);
+  g.nbr.clear();
+  g.nbr.reserve(tmp.size());
+  for (int64_t v = 0; v < g.n; ++v) {
+    auto b = tmp.begin() + cnt[v], e = tmp.begin() + cnt[v + 1];
+    std::sort(b, e);
+    e = std::unique(b, e);
+    g.nbr.insert(g.nbr.end(), b, e);
+    g.off[v + 1] = (int64_t)g.nbr.size();
+  }
+  return g;
+}
+
+// Scalar merge count: other_order/set_operation.cpp:129-144 (intersect_count),
+// widened to 64 bits.
+inline uint64_t intersect_count(const int32_t* a, int64_t na, const int32_t* b, int64_t nb) {
+  int64_t i = 0, j = 0;
+  uint64_t r = 0;
+  while (i < na && j < nb) {
+    if (a[i] == b[j]) {
+      ++r; ++i; ++j;
+    } else if (a[i] < b[j]) {
+      ++i;
+    } else {
+      ++j;
+    }
+  }
+  return r;
+}
+
+template <class F>
+void parallel_for(int64_t n, int nthreads, int64_t chunk, F&& body) {
+  if (nthreads <= 1 || n <= chunk) {
+    for (int64_t i = 0; i < n; ++i) body(i, 0);
+    return;
+  }
+  std::atomic<int64_t> next(0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t)
+    th.emplace_back([&, t] {
+      for (;;) {
+        int64_t b = next.fetch_add(chunk);
+        if (b >= n) break;
+        int64_t e = std::min(n, b + chunk);
+        for (int64_t i = b; i < e; ++i) body(i, t);
+      }
+    });
+  for (auto& x : th) x.join();
+}
+
+// Length of the prefix of v's sorted list holding neighbours smaller than v:
+// the N-(v) lists OrgTriangleCount::build keeps (org_triangle_count.cpp:15-50).
+inline int64_t lower_len(const Adj& g, int64_t v) {
+  const int32_t* b = g.nbr.data() + g.off[v];
+  const int32_t* e = g.nbr.data() + g.off[v + 1];
+  return std::lower_bound(b, e, (int32_t)v) - b;
+}
+
+// ---------------------------------------------------------------------------
+// A-direction (edge_directing/A-direction-seri.cpp:35-153), restated with the
+// reference's own data layout: every neighbour listed twice, degrees doubled,
+// float threshold, frontier vectors.
+// ---------------------------------------------------------------------------
+std::vector<int> seri_peel(const std::vector<std::pair<int, int>>& edges, unsigned edgeNum, int nodeNum) {
+  float threshold = ((float)edgeNum) / nodeNum + 1;             // :37
+  std::vector<int> priority(nodeNum, -1);                          // :38-39
+  std::vector<int> frontier, next;
+  std::vector<int> degree(nodeNum, 0);
+  for (unsigned i = 0; i < edgeNum; ++i) {                         // :44-47
+    degree[edges[i].first]++;
+    degree[edges[i].second]++;
+  }
+  std::vector<int> rt(degree);                                     // :48-49
+  std::vector<long long> off(nodeNum, 0);                          // :50-54
+  for (int i = 0; i + 1 < nodeNum; ++i) off[i + 1] = off[i] + degree[i];
+  std::vector<int> all((size_t)edgeNum * 2);                       // :59-73
+  std::vector<long long> cur(off);
+  for (unsigned i = 0; i < edgeNum; ++i) {
+    int s = edges[i].first, d = edges[i].second;
+    all[cur[s]++] = d;
+    all[cur[d]++] = s;
+  }
+  int priorityNum = 0;
+  int threshold_old = threshold;                                   // :77
+  int peeled = 0;
+  for (;;) {                                                       // :79
+    frontier.clear();
+    next.clear();
+    for (int i = 0; i < nodeNum; ++i)                              // :83-89
+      if (rt[i] <= threshold && priority[i] == -1) {
+        frontier.push_back(i);
+        ++peeled;
+        priority[i] = priorityNum;
+      }
+    ++priorityNum;
+    while (!frontier.empty()) {                                    // :92-121
+      for (size_t f = 0; f < frontier.size(); ++f) {
+        int c = frontier[f];
+        const int* lst = all.data() + off[c];
+        for (int j = 0; j < degree[c]; ++j) {
+          int v = lst[j];
+          if (priority[v] != -1) {
+            if (priority[v] == priority[c] &&
+                (rt[v] > rt[c] || (rt[v] == rt[c] && v > c)))
+              rt[v]--;
+          } else {
+            rt[v]--;
+            if (rt[v] <= threshold) {
+              next.push_back(v);
+              ++peeled;
+              priority[v] = priorityNum;
+            }
+          }
+        }
+      }
+      std::swap(frontier, next);
+      next.clear();
+      ++priorityNum;
+    }
+    if (peeled >= nodeNum) break;                                  // :125-126
+    threshold += threshold_old;                                    // :127
+  }
+  return priority;
+}
+
+// ---------------------------------------------------------------------------
+// A-order tables (vertex_ordering/A-order/A-order.cpp:20-36).
+// ---------------------------------------------------------------------------
+const float kBw[10] = {0, 0, 271, 310, 399, 419, 458, 478, 524, 539};
+const float kLambda[10] = {0, 0, 145.51, 121.98, 53.26, 23.92, 16, 14, 12.94, 10.24};  // double literals narrowed, as in the reference
+
+float get_bandwidth(int len) {
+  if (len < 10) return kBw[len];
+  return 384.1 * std::pow(len, 0.1491);  // double product, narrowed to float on return
+}
+
+float get_equal_bandwidth(int len) {
+  if (len < 10) return kLambda[len] * std::sqrt(get_bandwidth(len)) / std::sqrt((float)len);
+  return 12 * std::sqrt(get_bandwidth(len)) / std::sqrt((float)len);
+}
+
+struct Bucket {
+  int id;
+  float ms;   // memorySuperiority
+  int slot;   // index of this bucket's member list (the reference keeps a vector pointer)
+};
+struct LessCmp {   // A-order.cpp:44-49
+  bool operator()(const Bucket& a, const Bucket& b) const {
+    return a.ms < b.ms || (a.ms == b.ms && a.id < b.id);
+  }
+};
+struct GreatCmp {  // A-order.cpp:50-55
+  bool operator()(const Bucket& a, const Bucket& b) const {
+    return a.ms > b.ms || (a.ms == b.ms && a.id > b.id);
+  }
+};
+struct IdSort {    // A-order.cpp:56-60
+  bool operator()(const Bucket& a, const Bucket& b) const { return a.id > b.id; }
+};
+
+}  // namespace
+
+extern "C" {
+
+// Status codes shared by the oracle entry points.
+enum { ORC_OK = 0, ORC_UNSUPPORTED = 5 };
+
+// Number of distinct undirected non-loop edges and the vertex count.
+void orc_simple_stats(const int32_t* pairs, uint64_t np, int64_t* n_out, int64_t* m_out) {
+  Adj g = build_adj(pairs, np);
+  *n_out = g.n;
+  *m_out = (int64_t)g.nbr.size() / 2;
+}
+
+// Triangle count of the simple graph underlying `pairs`: Σ_u Σ_{v∈N-(u)} |N-(u) ∩ N-(v)|
+// over the "smaller neighbour" lists, as OrgTriangleCount::triangle_count does
+// (other_order/org_triangle_count.cpp:57-79 with set_operation.cpp:129-144), in uint64.
+uint64_t orc_tc_count(const int32_t* pairs, uint64_t np, int nthreads) {
+  Adj g = build_adj(pairs, np);
+  std::vector<int64_t> low(g.n);
+  for (int64_t v = 0; v < g.n; ++v) low[v] = lower_len(g, v);
+  std::vector<uint64_t> part(std::max(1, nthreads), 0);
+  parallel_for(g.n, nthreads, 256, [&](int64_t u, int t) {
+    const int32_t* a = g.nbr.data() + g.off[u];
+    uint64_t s = 0;
+    for (int64_t k = 0; k < low[u]; ++k) {
+      int32_t v = a[k];
+      s += intersect_count(a, low[u], g.nbr.data() + g.off[v], low[v]);
+    }
+    part[t] += s;
+  });
+  uint64_t r = 0;
+  for (auto x : part) r += x;
+  return r;
+}
+
+// Same count restricted to "top" vertices u with u % stride == phase: the bounded
+// sample the CPU baseline times.  Returns the count; *edges_out receives Σ|N-(u)|
+// over the sampled u (the edges whose triangles were counted).
+uint64_t orc_tc_count_sample(const int64_t* off, const int32_t* nbr, int64_t n,
+                             int64_t stride, int64_t phase, int nthreads, int64_t* edges_out) {
+  // `off`/`nbr` are the symmetric simple CSR built by orc_symmetric_csr.
+  int64_t nsamp = (n - phase + stride - 1) / stride;
+  if (nsamp < 0) nsamp = 0;
+  auto low = [&](int64_t v) {
+    const int32_t* b = nbr + off[v];
+    const int32_t* e = nbr + off[v + 1];
+    return (int64_t)(std::lower_bound(b, e, (int32_t)v) - b);
+  };
+  std::vector<uint64_t> part(std::max(1, nthreads), 0);
+  std::vector<int64_t> epart(std::max(1, nthreads), 0);
+  parallel_for(nsamp, nthreads, 64, [&](int64_t i, int t) {
+    int64_t u = phase + i * stride;
+    const int32_t* a = nbr + off[u];
+    int64_t lu = low(u);
+    uint64_t s = 0;
+    for (int64_t k = 0; k < lu; ++k) {
+      int32_t v = a[k];
+      s += intersect_count(a, lu, nbr + off[v], low(v));
+    }
+    part[t] += s;
+    epart[t] += lu;
+  });
+  uint64_t r = 0;
+  int64_t e = 0;
+  for (size_t t = 0; t < part.size(); ++t) { r += part[t]; e += epart[t]; }
+  *edges_out = e;
+  return r;
+}
+
+// Symmetric simple CSR (int64 offsets, sorted lists): used by bench.py's CPU leg.
+// Call once with off == nullptr to get sizes (n_out, nnz_out), then with buffers.
+void orc_symmetric_csr(const int32_t* pairs, uint64_t np, int64_t* off, int32_t* nbr,
+                       int64_t* n_out, int64_t* nnz_out) {
+  Adj g = build_adj(pairs, np);
+  *n_out = g.n;
+  *nnz_out = (int64_t)g.nbr.size();
+  if (!off) return;
+  std::memcpy(off, g.off.data(), sizeof(int64_t) * (g.n + 1));
+  std::memcpy(nbr, g.nbr.data(), sizeof(int32_t) * g.nbr.size());
+}
+
+// A-direction-seri (edge_directing/A-direction-seri.cpp:170-288): reads pairs as the
+// READFROMFILE path does, peels, and writes the oriented edge list (the bytes of
+// lpBasedGraph.bin) into `out` (capacity 2*np ints).  `prio_out` (nullable, n ints)
+// receives the peel priorities.  Returns the number of oriented edges.
+int64_t orc_adirection(const int32_t* pairs, uint64_t np, int32_t* out, int32_t* prio_out) {
+  int nodeNum = 0;                                                  // :174
+  for (uint64_t i = 0; i < np; ++i) {                               // :188-191
+    if (pairs[2 * i] > nodeNum) nodeNum = pairs[2 * i];
+    if (pairs[2 * i + 1] > nodeNum) nodeNum = pairs[2 * i + 1];
+  }
+  nodeNum++;                                                        // :192
+  std::vector<std::vector<int>> nb(nodeNum);                        // :199
+  for (uint64_t i = 0; i < np; ++i) {                               // :215-221
+    int s = pairs[2 * i], e = pairs[2 * i + 1];
+    if (s == e) continue;
+    nb[s].push_back(e);
+    nb[e].push_back(s);
+  }
+  int totalEdge = 0;                                                // :197
+  for (int i = 0; i < nodeNum; ++i) {                               // :225-229
+    std::sort(nb[i].begin(), nb[i].end());
+    nb[i].erase(std::unique(nb[i].begin(), nb[i].end()), nb[i].end());
+    totalEdge += (int)nb[i].size();
+  }
+  std::vector<std::pair<int, int>> origin;                          // :242-248
+  origin.reserve(totalEdge);
+  for (int i = 0; i < nodeNum; ++i)
+    for (int x : nb[i]) origin.emplace_back(i, x);
+  std::vector<int> prio = seri_peel(origin, (unsigned)totalEdge, nodeNum);   // :252
+  int64_t k = 0;
+  for (int i = 0; i < nodeNum; ++i)                                 // :254-273
+    for (int c : nb[i])
+      if (prio[c] > prio[i] || (prio[c] == prio[i] && i < c)) {
+        out[2 * k] = i;
+        out[2 * k + 1] = c;
+        ++k;
+      }
+  if (prio_out) std::memcpy(prio_out, prio.data(), sizeof(int) * nodeNum);
+  return k;
+}
+
+// A-order (vertex_ordering/A-order/A-order.cpp:62-247).  Fills `lookup`
+// (maxNodeId+1 ints: badLookUpTable, the new id of every old id), `normal` and
+// `reordered` (2*np ints each: the bytes of the two output files).  Returns ORC_OK,
+// or ORC_UNSUPPORTED where the reference indexes outside its arrays (no vertex with
+// runtime degree in [2,4] or none >= 5, so memoryDominatePos == 0; or more such
+// vertices than whole buckets can hold).
+int orc_aorder(const int32_t* pairs, uint64_t np, int32_t* lookup, int32_t* normal, int32_t* reordered) {
+  const int BUCKETSIZE = 40;                                        // :14
+  int maxNodeId = 0;                                                // :65-74
+  std::vector<std::pair<int, int>> e(np);
+  for (uint64_t i = 0; i < np; ++i) {
+    int s = pairs[2 * i], d = pairs[2 * i + 1];
+    maxNodeId = s > maxNodeId ? s : maxNodeId;
+    maxNodeId = d > maxNodeId ? d : maxNodeId;
+    e[i] = {s, d};
+  }
+  std::vector<int> degree(maxNodeId + 1, 0);                        // :78-83
+  for (auto& x : e) { degree[x.first]++; degree[x.second]++; }
+  std::vector<int> rt(maxNodeId + 1, 0);                            // :86-99
+  for (auto& x : e) {
+    int s = x.first, d = x.second;
+    if (degree[s] > degree[d] || (degree[s] == degree[d] && s < d)) {
+      x.first = d;
+      x.second = s;
+      rt[d]++;
+    } else {
+      rt[s]++;
+    }
+  }
+  int maxRt = 0;                                                    // :100-104
+  for (int i = 0; i <= maxNodeId; ++i) maxRt = std::max(maxRt, rt[i]);
+  std::vector<std::vector<int>> bucket(maxRt + 1);                  // :106-109
+  for (int i = 0; i <= maxNodeId; ++i) bucket[rt[i]].push_back(i);
+  std::vector<std::pair<int, int>> idrt;                            // :110-119
+  unsigned memoryDominatePos = 0;
+  for (int i = 2; i <= maxRt; ++i) {
+    if (i == 5) memoryDominatePos = (unsigned)idrt.size();
+    for (int v : bucket[i]) idrt.emplace_back(v, i);
+  }
+  int totalBucketNum = (int)idrt.size() / BUCKETSIZE;               // :123
+  if (memoryDominatePos == 0 || memoryDominatePos > (unsigned)(BUCKETSIZE * totalBucketNum))
+    return ORC_UNSUPPORTED;
+  std::vector<Bucket> all(totalBucketNum);                          // :126-132
+  std::vector<std::vector<int>> members(totalBucketNum);
+  for (int i = 0; i < totalBucketNum; ++i) all[i] = Bucket{i, 0.0f, i};
+  std::make_heap(all.begin(), all.end(), GreatCmp());
+  std::vector<float> bw(maxRt + 1), ebw(maxRt + 1);                 // :134-139
+  for (int i = 0; i < maxRt + 1; ++i) {
+    bw[i] = get_bandwidth(i);
+    ebw[i] = get_equal_bandwidth(i);
+  }
+  int finished = 0;
+  for (int i = BUCKETSIZE * totalBucketNum - 1; i >= (int)memoryDominatePos; --i) {   // :144-157
+    std::pop_heap(all.begin(), all.end() - finished, GreatCmp());
+    Bucket& cb = *(all.rbegin() + finished);
+    int d = idrt[i].second;
+    members[cb.slot].push_back(idrt[i].first);
+    cb.ms += (bw[d] - ebw[d]) / BUCKETSIZE;
+    if ((int)members[cb.slot].size() >= BUCKETSIZE) ++finished;
+    else std::push_heap(all.begin(), all.end() - finished, GreatCmp());
+  }
+  std::make_heap(all.begin(), all.end() - finished, LessCmp());     // :163
+  for (unsigned i = 0; i < memoryDominatePos; ++i) {                // :165-177
+    std::pop_heap(all.begin(), all.end() - finished, LessCmp());
+    Bucket& cb = *(all.rbegin() + finished);
+    int d = idrt[i].second;
+    members[cb.slot].push_back(idrt[i].first);
+    cb.ms -= (ebw[d] - bw[d]) / BUCKETSIZE;
+    if ((int)members[cb.slot].size() >= BUCKETSIZE) ++finished;
+    else std::push_heap(all.begin(), all.end() - finished, LessCmp());
+  }
+  std::sort_heap(all.begin(), all.end(), IdSort());                 // :181 (not a heap under IdSort)
+  std::vector<int> order;                                           // :186-198
+  order.reserve(maxNodeId + 1);
+  for (int i = 0; i < totalBucketNum; ++i)
+    for (int v : members[all[i].slot]) order.push_back(v);
+  for (size_t i = (size_t)totalBucketNum * BUCKETSIZE; i < idrt.size(); ++i) order.push_back(idrt[i].first);
+  if (maxRt >= 1) for (int v : bucket[1]) order.push_back(v);
+  for (int v : bucket[0]) order.push_back(v);
+  for (int i = 0; i <= maxNodeId; ++i) lookup[order[i]] = i;        // :206-210
+  for (uint64_t i = 0; i < np; ++i) {                               // :219-228
+    normal[2 * i] = e[i].first;
+    normal[2 * i + 1] = e[i].second;
+    reordered[2 * i] = lookup[e[i].first];
+    reordered[2 * i + 1] = lookup[e[i].second];
+  }
+  return ORC_OK;
+}
+
+// k-clique count of the simple graph (k >= 3), the quantity kcl_gpu_solver
+// accumulates (k-clique/kcl.cu:147-215): embeddings of the DAG extended level by
+// level by vertices adjacent to every member (is_all_connected_dag), counted at
+// level k-2.  Restated as a depth-first intersection over N+(v) = {w > v}; the
+// count does not depend on the acyclic orientation.
+uint64_t orc_kclique(const int32_t* pairs, uint64_t np, int k, int nthreads) {
+  Adj g = build_adj(pairs, np);
+  if (k < 1) return 0;
+  if (k == 1) return (uint64_t)g.n;
+  if (k == 2) return (uint64_t)g.nbr.size() / 2;
+  std::vector<int64_t> hi(g.n);
+  for (int64_t v = 0; v < g.n; ++v) {
+    const int32_t* b = g.nbr.data() + g.off[v];
+    const int32_t* e = g.nbr.data() + g.off[v + 1];
+    hi[v] = std::upper_bound(b, e, (int32_t)v) - b;   // start of N+(v)
+  }
+  std::vector<uint64_t> part(std::max(1, nthreads), 0);
+  parallel_for(g.n, nthreads, 64, [&](int64_t u, int t) {
+    // levels[l] holds the candidate set after l+1 chosen vertices
+    std::vector<std::vector<int32_t>> lv(k);
+    lv[0].assign(g.nbr.begin() + g.off[u] + hi[u], g.nbr.begin() + g.off[u + 1]);
+    uint64_t cnt = 0;
+    // recursive lambda via explicit function object
+    struct Rec {
+      const Adj& g; const std::vector<int64_t>& hi; std::vector<std::vector<int32_t>>& lv; int k;
+      uint64_t go(int depth) {  // depth chosen vertices so far; candidates lv[depth-1]
+        const auto& c = lv[depth - 1];
+        if (depth == k - 1) return c.size();
+        uint64_t s = 0;
+        for (int32_t v : c) {
+          auto& nxt = lv[depth];
+          nxt.clear();
+          const int32_t* b = g.nbr.data() + g.off[v] + hi[v];
+          const int32_t* e = g.nbr.data() + g.off[v + 1];
+          std::set_intersection(c.begin(), c.end(), b, e, std::back_inserter(nxt));
+          if ((int)nxt.size() >= k - 1 - depth) s += go(depth + 1);
+        }
+        return s;
+      }
+    } rec{g, hi, lv, k};
+    cnt = rec.go(1);
+    part[t] += cnt;
+  });
+  uint64_t r = 0;
+  for (auto x : part) r += x;
+  return r;
+}
+
+// costFuncCal (tools/costFuncCal.cpp:15-88): out = {idPartCost, degreePartCost, lpPartCost}.
+void orc_costfunc(const int32_t* pairs, uint64_t np, int k, float* out) {
+  unsigned edgeNum = (unsigned)np;
+  unsigned maxNode = 0;
+  for (unsigned i = 0; i < edgeNum; ++i) {                          // :27-31
+    unsigned s = (unsigned)pairs[2 * i], d = (unsigned)pairs[2 * i + 1];
+    maxNode = s > maxNode ? s : maxNode;
+    maxNode = d > maxNode ? d : maxNode;
+  }
+  unsigned nodeNum = maxNode + 1;
+  float avg = (float)edgeNum / nodeNum;                             // :34
+  std::vector<int> deg(nodeNum, 0), idd(nodeNum, 0), dd(nodeNum, 0), lp(nodeNum, 0);
+  for (unsigned i = 0; i < edgeNum; ++i) {                          // :44-49
+    deg[pairs[2 * i]]++;
+    deg[pairs[2 * i + 1]]++;
+    lp[pairs[2 * i]]++;
+  }
+  for (unsigned i = 0; i < edgeNum; ++i) {                          // :50-61
+    int s = pairs[2 * i], d = pairs[2 * i + 1];
+    if (s < d) idd[s]++; else idd[d]++;
+    if (deg[s] < deg[d] || (deg[s] == deg[d] && s < d)) dd[s]++; else dd[d]++;
+  }
+  auto fabs_ = [](float a) { return a > 0 ? a : -a; };              // :11-13
+  float idPart = 0, dPart = 0, lpPart = 0;
+  float thr = k * avg;                                              // :66
+  for (int i = 0; i < (int)nodeNum; ++i) {                          // :67-82
+    float c = fabs_(idd[i] - avg);
+    if (idd[i] - avg > thr) idPart += c;
+    c = fabs_(dd[i] - avg);
+    if (dd[i] - avg > thr) dPart += c;
+    c = fabs_(lp[i] - avg);
+    if (lp[i] - avg > thr) lpPart += c;
+  }
+  out[0] = idPart;
+  out[1] = dPart;
+  out[2] = lpPart;
+}
+
+// verification (tools/verification.cpp:11-61, a text-input tool; the caller parses
+// the text): out = {f_lp, f_degree}.  The degree sum skips the last vertex (:58).
+void orc_verification(const int32_t* pairs, uint64_t np, float* out) {
+  int maxNodeId = 0;
+  for (uint64_t i = 0; i < np; ++i) {
+    maxNodeId = pairs[2 * i] > maxNodeId ? pairs[2 * i] : maxNodeId;
+    maxNodeId = pairs[2 * i + 1] > maxNodeId ? pairs[2 * i + 1] : maxNodeId;
+  }
+  float dAve = (float)np / (maxNodeId + 1);
+  std::vector<int> lpd(maxNodeId + 1, 0), deg(maxNodeId + 1, 0), rt(maxNodeId + 1, 0);
+  for (uint64_t i = 0; i < np; ++i) {
+    lpd[pairs[2 * i]]++;
+    deg[pairs[2 * i]]++;
+    deg[pairs[2 * i + 1]]++;
+  }
+  float f_lp = 0;
+  for (int i = 0; i <= maxNodeId; ++i) f_lp += std::abs(dAve - lpd[i]);
+  for (uint64_t i = 0; i < np; ++i) {
+    int s = pairs[2 * i], d = pairs[2 * i + 1];
+    if (deg[s] > deg[d] || (deg[s] == deg[d] && s < d)) rt[d]++;
+    else rt[s]++;
+  }
+  float f_deg = 0;
+  for (int i = 0; i < maxNodeId; ++i) f_deg += std::abs(rt[i] - dAve);
+  out[0] = f_lp;
+  out[1] = f_deg;
+}
+
+// Hu preTC CSR (Hu/preTC.cu:64-296): degree orientation over the raw pairs (src =
+// lower degree, ties to the larger id as src, :125-133), vertices of degree <= 1
+// dropped and ids compacted by prefix (:135-169), edges sorted by (src,dst) and merged
+// into CSR skipping self-loops and repeats (:186-284).  Outputs the CSR without the
+// kernel's sentinels: offsets (n+1 uint32), cols (m int32).  Returns n; *m_out = m.
+// Call with offsets == nullptr first to size the buffers.
+int64_t orc_hu_csr(const int32_t* pairs, uint64_t np, uint32_t* offsets, int32_t* cols, int64_t* m_out) {
+  int64_t mx = max_id(pairs, np);
+  int64_t nodeNum = mx + 1;
+  std::vector<int> deg(nodeNum, 0);
+  for (uint64_t i = 0; i < np; ++i) { deg[pairs[2 * i]]++; deg[pairs[2 * i + 1]]++; }
+  std::vector<int64_t> mini(nodeNum, 0);
+  int64_t tot = 0;
+  for (int64_t i = 0; i < nodeNum; ++i) { if (deg[i] <= 1) ++tot; mini[i] = tot; }
+  std::vector<uint64_t> keys;
+  keys.reserve(np);
+  for (uint64_t i = 0; i < np; ++i) {
+    uint32_t s = (uint32_t)pairs[2 * i], d = (uint32_t)pairs[2 * i + 1];
+    if (deg[s] > deg[d] || (deg[s] == deg[d] && s < d)) std::swap(s, d);
+    if (deg[s] <= 1 || deg[d] <= 1) continue;
+    if (s > 0) s -= (uint32_t)mini[s - 1];
+    if (d > 0) d -= (uint32_t)mini[d - 1];
+    if (s == d) continue;
+    keys.push_back(((uint64_t)s << 32) | d);
+  }
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  int64_t n = nodeNum - tot;
+  *m_out = (int64_t)keys.size();
+  if (!offsets) return n;
+  std::fill(offsets, offsets + n + 1, 0u);
+  for (auto k : keys) offsets[(k >> 32) + 1]++;
+  for (int64_t i = 0; i < n; ++i) offsets[i + 1] += offsets[i];
+  for (size_t i = 0; i < keys.size(); ++i) cols[i] = (int32_t)(keys[i] & 0xffffffffu);
+  return n;
+}
+
+// Directed-wedge count W = Σ_v d-(v)·d+(v) of an oriented CSR (offsets int64, n+1).
+uint64_t orc_wedges(const int64_t* off, const int32_t* cols, int64_t n) {
+  std::vector<uint64_t> indeg(n, 0);
+  for (int64_t i = 0; i < off[n]; ++i) indeg[cols[i]]++;
+  uint64_t w = 0;
+  for (int64_t v = 0; v < n; ++v) w += indeg[v] * (uint64_t)(off[v + 1] - off[v]);
+  return w;
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+"""ctypes loader for the CPU oracle (atc_oracle.cpp) — TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU legs as the checker
+or the timed CPU baseline.  The product library never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+_lib = None
+_P = C.c_void_p
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_simple_stats.argtypes = [_P, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.orc_tc_count.restype = C.c_uint64
+        L.orc_tc_count.argtypes = [_P, C.c_uint64, C.c_int]
+        L.orc_tc_count_sample.restype = C.c_uint64
+        L.orc_tc_count_sample.argtypes = [_P, _P, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_int64)]
+        L.orc_symmetric_csr.argtypes = [_P, C.c_uint64, _P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.orc_adirection.restype = C.c_int64
+        L.orc_adirection.argtypes = [_P, C.c_uint64, _P, _P]
+        L.orc_aorder.restype = C.c_int
+        L.orc_aorder.argtypes = [_P, C.c_uint64, _P, _P, _P]
+        L.orc_kclique.restype = C.c_uint64
+        L.orc_kclique.argtypes = [_P, C.c_uint64, C.c_int, C.c_int]
+        L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
+        L.orc_verification.argtypes = [_P, C.c_uint64, _P]
+        L.orc_hu_csr.restype = C.c_int64
+        L.orc_hu_csr.argtypes = [_P, C.c_uint64, _P, _P, C.POINTER(C.c_int64)]
+        L.orc_wedges.restype = C.c_uint64
+        L.orc_wedges.argtypes = [_P, _P, C.c_int64]
+        _lib = L
+    return _lib
+
+
+def _pairs(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a.reshape(-1, 2)
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def nthreads_default():
+    return os.cpu_count() or 1
+
+
+def simple_stats(pairs):
+    p = _pairs(pairs)
+    n, m = C.c_int64(0), C.c_int64(0)
+    lib().orc_simple_stats(_ptr(p), p.shape[0], C.byref(n), C.byref(m))
+    return n.value, m.value
+
+
+def tc_count(pairs, nthreads=None):
+    p = _pairs(pairs)
+    return lib().orc_tc_count(_ptr(p), p.shape[0], nthreads or nthreads_default())
+
+
+def symmetric_csr(pairs):
+    p = _pairs(pairs)
+    n, nnz = C.c_int64(0), C.c_int64(0)
+    lib().orc_symmetric_csr(_ptr(p), p.shape[0], None, None, C.byref(n), C.byref(nnz))
+    off = np.empty(n.value + 1, dtype=np.int64)
+    nbr = np.empty(max(nnz.value, 1), dtype=np.int32)
+    lib().orc_symmetric_csr(_ptr(p), p.shape[0], _ptr(off), _ptr(nbr), C.byref(n), C.byref(nnz))
+    return off, nbr
+
+
+def tc_count_sample(off, nbr, stride, phase=0, nthreads=None):
+    e = C.c_int64(0)
+    c = lib().orc_tc_count_sample(_ptr(off), _ptr(nbr), len(off) - 1, stride, phase,
+                                  nthreads or nthreads_default(), C.byref(e))
+    return c, e.value
+
+
+def adirection(pairs, want_prio=False):
+    p = _pairs(pairs)
+    out = np.empty((max(p.shape[0], 1), 2), dtype=np.int32)
+    prio = np.empty((int(p.max()) + 1) if p.size else 1, dtype=np.int32)
+    k = lib().orc_adirection(_ptr(p), p.shape[0], _ptr(out), _ptr(prio))
+    res = out[:k].copy()
+    return (res, prio) if want_prio else res
+
+
+UNSUPPORTED = 5
+
+
+def aorder(pairs):
+    """(lookup, normal, reordered), or None where the reference would read out of bounds."""
+    p = _pairs(pairs)
+    nin = (int(p.max()) + 1) if p.size else 1
+    lookup = np.empty(nin, dtype=np.int32)
+    normal = np.empty_like(p)
+    reordered = np.empty_like(p)
+    st = lib().orc_aorder(_ptr(p), p.shape[0], _ptr(lookup), _ptr(normal), _ptr(reordered))
+    if st == UNSUPPORTED:
+        return None
+    return lookup, normal, reordered
+
+
+def kclique(pairs, k, nthreads=None):
+    p = _pairs(pairs)
+    return lib().orc_kclique(_ptr(p), p.shape[0], k, nthreads or nthreads_default())
+
+
+def costfunc(pairs, k):
+    p = _pairs(pairs)
+    out = np.zeros(3, dtype=np.float32)
+    lib().orc_costfunc(_ptr(p), p.shape[0], k, _ptr(out))
+    return out
+
+
+def verification(pairs):
+    p = _pairs(pairs)
+    out = np.zeros(2, dtype=np.float32)
+    lib().orc_verification(_ptr(p), p.shape[0], _ptr(out))
+    return out
+
+
+def hu_csr(pairs):
+    p = _pairs(pairs)
+    m = C.c_int64(0)
+    n = lib().orc_hu_csr(_ptr(p), p.shape[0], None, None, C.byref(m))
+    off = np.empty(n + 1, dtype=np.uint32)
+    cols = np.empty(max(m.value, 1), dtype=np.int32)
+    lib().orc_hu_csr(_ptr(p), p.shape[0], _ptr(off), _ptr(cols), C.byref(m))
+    return off, cols[: m.value]
+
+
+def wedges(off, cols):
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    return lib().orc_wedges(_ptr(off), _ptr(cols), len(off) - 1)

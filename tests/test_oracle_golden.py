@@ -1,0 +1,113 @@
+"""The CPU oracle against the reference programs' own outputs (tests/golden).
+
+These pin the restatement in oracle/atc_oracle.cpp: A-direction orientation and A-order
+permutation byte for byte, costFuncCal / verification figures as the tools print them,
+and the OrgTriangleCount triangle counts.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden_input, load_golden
+
+CASES = sorted(load_golden()["cases"])
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.int32).tobytes()).hexdigest()
+
+
+def fmt6(x):
+    """C++ ostream default formatting (%g, 6 significant digits)."""
+    s = "%g" % np.float32(x)
+    return s
+
+
+def check_pairs(got, rec):
+    assert got.shape[0] == rec["count"]
+    assert sha(got) == rec["sha256"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_input_bytes(golden, name):
+    c = golden["cases"][name]
+    check_pairs(golden_input(c), c["input"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_adirection(golden, name):
+    c = golden["cases"][name]
+    check_pairs(oracle.adirection(golden_input(c)), c["adirection"])
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("which", ["aorder", "aorder_raw"])
+def test_aorder(golden, name, which):
+    c = golden["cases"][name]
+    g = golden_input(c)
+    src = oracle.adirection(g) if which == "aorder" else g
+    rec = c[which]
+    res = oracle.aorder(src)
+    if rec.get("unsupported"):
+        assert res is None
+        assert rec["ref_returncode"] != 0  # the reference crashed on it
+        return
+    assert res is not None
+    lookup, normal, reordered = res
+    check_pairs(normal, rec["normal"])
+    check_pairs(reordered, rec["reordered"])
+    assert np.array_equal(np.sort(lookup), np.arange(lookup.size))  # a permutation
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_costfunc(golden, name):
+    c = golden["cases"][name]
+    lp = oracle.adirection(golden_input(c))
+    for k, printed in c["costfunc"].items():
+        got = oracle.costfunc(lp, int(k))
+        assert [fmt6(x) for x in got] == printed
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_verification(golden, name):
+    c = golden["cases"][name]
+    lp = oracle.adirection(golden_input(c))
+    got = oracle.verification(lp)
+    assert [fmt6(x) for x in got] == c["verification"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_triangles(golden, name):
+    c = golden["cases"][name]
+    if "triangles" not in c:
+        pytest.skip("fixture made without the x86-only OrgTriangleCount")
+    assert oracle.tc_count(golden_input(c)) == c["triangles"]
+
+
+def test_kclique_identities():
+    # K_n has C(n,k) k-cliques; k=3 equals the triangle count.
+    from math import comb
+    for n in (5, 7, 9):
+        kn = np.array([(a, b) for a in range(n) for b in range(n) if a != b], dtype=np.int32)
+        for k in range(3, 8):
+            assert oracle.kclique(kn, k) == comb(n, k)
+    import atc
+    g = atc.rmat_graph(10, 16, 1)
+    assert oracle.kclique(g, 3) == oracle.tc_count(g)
+
+
+def test_hu_csr_matches_reference_rules():
+    # Hu's preTC CSR on a once-per-edge list: every vertex of degree >= 2 kept, lists
+    # oriented low degree -> high degree (ties: larger id is the source), sorted.
+    import atc
+    g = atc.rmat_graph(8, 8, 2, symmetric=False)
+    off, cols = oracle.hu_csr(g)
+    assert off[-1] == cols.size
+    for u in range(off.size - 1):
+        lst = cols[off[u]:off[u + 1]]
+        assert np.all(np.diff(lst) > 0)
+    # orientation preserves the triangle count
+    oriented = np.stack([np.repeat(np.arange(off.size - 1), np.diff(off)), cols], 1)
+    assert oracle.tc_count(oriented) == oracle.tc_count(g)
