@@ -265,6 +265,14 @@ def pretc(pairs, dir=Dir.DEGREE, order=Order.NONE, tuning=None, want_perm=False,
     return CSR(st, perm)
 
 
+def pretc_host_ptr(pairs_ptr, n_pairs, dir=Dir.DEGREE, order=Order.NONE, tuning=None, stream=None):
+    """atc_pretc on a raw host address (e.g. a pinned torch tensor's data_ptr())."""
+    st = CSRStruct()
+    _check(lib().atc_pretc(C.c_void_p(pairs_ptr), n_pairs, int(dir), int(order), _tuning(tuning), C.byref(st),
+                           None, stream))
+    return CSR(st)
+
+
 def pretc_device(pairs_dev_ptr, n_pairs, dir=Dir.DEGREE, order=Order.NONE, tuning=None, stream=None):
     st = CSRStruct()
     _check(lib().atc_pretc_device(C.c_void_p(pairs_dev_ptr), n_pairs, int(dir), int(order), _tuning(tuning),

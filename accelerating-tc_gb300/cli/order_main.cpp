@@ -1,0 +1,79 @@
+// Drop-in command lines for the reference's orientation / ordering / cost tools:
+//
+//   a_direction_seri <edges.bin>     edge_directing/A-direction-seri.cpp:170-288
+//        writes lpBasedGraph (text "src dst") and lpBasedGraph.bin in the working directory
+//   a_order <edges.bin>              vertex_ordering/A-order/A-order.cpp:62-247
+//        writes normal and reordered in the working directory
+//   cost_func_cal <edges.bin> <k>    tools/costFuncCal.cpp:15-95 (prints the three costs)
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <vector>
+
+#include "atc.h"
+
+static int fail(const char* what, atc_status s) {
+  fprintf(stderr, "%s failed: %s: %s\n", what, atc_status_string(s), atc_last_error());
+  return 1;
+}
+
+static bool read_pairs(const char* path, std::vector<int32_t>& pairs) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return false;
+  fseek(f, 0, SEEK_END);
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  size_t n = sz > 0 ? (size_t)sz / 8 : 0;
+  pairs.resize(2 * n);
+  size_t got = n ? fread(pairs.data(), 8, n, f) : 0;
+  fclose(f);
+  return got == n;
+}
+
+static bool write_pairs(const char* path, const int32_t* p, size_t n) {
+  FILE* f = fopen(path, "wb");
+  if (!f) return false;
+  size_t w = n ? fwrite(p, 8, n, f) : 0;
+  fclose(f);
+  return w == n;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 2) { fprintf(stderr, "usage: %s <edges.bin>%s\n", argv[0], argc > 2 ? "" : " [k]"); return 2; }
+  std::vector<int32_t> pairs;
+  if (!read_pairs(argv[1], pairs)) { fprintf(stderr, "cannot read %s\n", argv[1]); return 1; }
+  uint64_t np = pairs.size() / 2;
+  atc_status s = atc_init(0);
+  if (s != ATC_OK) return fail("atc_init", s);
+#if defined(ATC_PROGRAM_A_DIRECTION_SERI)
+  std::vector<int32_t> out(2 * (np ? np : 1));
+  uint64_t n_out = 0;
+  s = atc_adirection(pairs.data(), np, out.data(), &n_out, nullptr, nullptr);
+  if (s != ATC_OK) return fail("atc_adirection", s);
+  FILE* t = fopen("lpBasedGraph", "w");
+  if (!t) return 1;
+  for (uint64_t i = 0; i < n_out; ++i) fprintf(t, "%d %d\n", out[2 * i], out[2 * i + 1]);
+  fclose(t);
+  if (!write_pairs("lpBasedGraph.bin", out.data(), n_out)) return 1;
+  std::cout << "we have dealed with " << n_out << " edges up to now" << std::endl;
+#elif defined(ATC_PROGRAM_A_ORDER)
+  int32_t mx = 0;
+  for (int32_t x : pairs) mx = x > mx ? x : mx;
+  std::vector<int32_t> lookup((size_t)mx + 1), normal(pairs.size()), reordered(pairs.size());
+  s = atc_aorder(pairs.data(), np, lookup.data(), normal.data(), reordered.data(), nullptr);
+  if (s != ATC_OK) return fail("atc_aorder", s);
+  if (!write_pairs("normal", normal.data(), np) || !write_pairs("reordered", reordered.data(), np)) return 1;
+#elif defined(ATC_PROGRAM_COST_FUNC_CAL)
+  if (argc < 3) { fprintf(stderr, "usage: %s <edges.bin> <k>\n", argv[0]); return 2; }
+  float c[3];
+  s = atc_costfunc(pairs.data(), np, atoi(argv[2]), c, nullptr);
+  if (s != ATC_OK) return fail("atc_costfunc", s);
+  std::cout << "idPartCost: " << c[0] << std::endl;
+  std::cout << "degreePartCost: " << c[1] << std::endl;
+  std::cout << "lpPartCost: " << c[2] << std::endl;
+#else
+#error "define one ATC_PROGRAM_*"
+#endif
+  return 0;
+}

@@ -1,0 +1,60 @@
+// Declarations shared between libatc translation units (not part of the ABI).
+#pragma once
+
+#include "common.cuh"
+
+namespace atc {
+
+// ---- device primitives (prims.cu; CUB radix sort / scan / select) ----------------
+// Sorts n keys on bits [begin_bit, end_bit).  `keys` and `alt` are two buffers of n
+// elements; on return `keys` points at the sorted data (the two may be swapped).
+atc_status sort_keys_u64(uint64_t*& keys, uint64_t*& alt, size_t n, int begin_bit, int end_bit, cudaStream_t s);
+// Unique over sorted keys; *n_out (host) receives the count.
+atc_status unique_u64(const uint64_t* in, uint64_t* out, size_t n, size_t* n_out, cudaStream_t s);
+// out[i] = sum_{j<i} in[j], for n elements.
+atc_status exclusive_scan_i64(const int64_t* in, int64_t* out, size_t n, cudaStream_t s);
+atc_status exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, size_t n, cudaStream_t s);
+
+// Bits needed to hold ids in [0, n): at least 1.
+inline int id_bits(int64_t n) {
+  int b = 1;
+  while (b < 62 && (int64_t(1) << b) < n) ++b;
+  return b;
+}
+
+// Canonical simple edge list on the device: keys (a << B) | b with a < b, sorted,
+// duplicate-free, self-loops removed.
+struct SimpleEdges {
+  DevBuf<uint64_t> keys;   // m
+  int64_t m = 0;
+  int64_t n_in = 0;        // max input id + 1
+  int bits = 1;            // B
+};
+
+// Validates ids (>= 0), finds n_in and builds the canonical simple edge list.
+atc_status build_simple_edges(const int2* pairs, uint64_t np, SimpleEdges* out, cudaStream_t s);
+// Simple degree of every vertex (n_in ints) from canonical keys.
+atc_status simple_degrees(const SimpleEdges& e, int32_t* deg, cudaStream_t s);
+
+// A-direction peel priorities (edge_directing/A-direction-seri.cpp:35-153) of the simple
+// graph given by canonical keys: prio (n_in ints, device).  stats: number of waves.
+atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* prio, int* waves_out,
+                           cudaStream_t s);
+
+// A-order lookup (vertex_ordering/A-order/A-order.cpp:62-210) of an edge list with
+// repeats counted.  Edges come either as int2 pairs or as canonical keys (exactly one
+// non-null).  n_v = max id + 1 over the edges.  lookup: n_v ints (device).  If
+// oriented != nullptr (pairs input only) it receives the degree-oriented pairs (the
+// "normal" file).  Returns ATC_ERR_UNSUPPORTED where the reference reads outside its
+// arrays.
+atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v,
+                         int32_t* lookup, int2* oriented, cudaStream_t s);
+
+// Private part of an atc_csr.
+struct CsrPriv {
+  int32_t* esrc = nullptr;       // m: source vertex of every edge, in edge order
+  unsigned long long* counter = nullptr;  // 2 x u64 scratch for counting kernels
+  int bits = 1;
+};
+
+}  // namespace atc

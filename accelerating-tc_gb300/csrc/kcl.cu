@@ -1,0 +1,166 @@
+// k-clique counting on an oriented CSR (k >= 3), exact in uint64.
+//
+// The reference (k-clique/kcl.cu:147-215, Pangolin) materialises every level of the
+// embedding list in HBM: per level it counts extensions (extend_alloc, :16-50), scans
+// them (thrust::exclusive_scan, :197) and writes the next level (extend_insert,
+// :115-145), counting instead of writing at level k-2.  Here each warp walks the
+// search tree of one oriented edge (u, v) depth first, so nothing but a small stack of
+// candidate sets is ever stored:
+//
+//   C0 = N+(u) ∩ N+(v);  C(l+1) = C(l) ∩ N+(w) for the w chosen from C(l);
+//   with k-1 vertices chosen, every element of the current candidate set completes a
+//   k-clique, so the last level is counted, never stored.
+//
+// Orientation is acyclic, so every k-clique is found once, from its first two vertices
+// in orientation order — the same count kcl_gpu_solver accumulates.  Intersections:
+// lanes take the elements of the candidate set (a subset of N+(u)), binary-search each
+// in N+(w), and ballot/popc compact the hits in order into the next level, which lives
+// in the warp's slice of a scratch buffer ((k-2) x max out-degree ints per warp).
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace atc {
+
+namespace {
+
+__device__ __forceinline__ bool kc_has(const int32_t* a, int64_t n, int32_t x) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo < n && a[lo] == x;
+}
+
+// Writes P ∩ L (P given, L sorted) into out in P's order; returns the size (all lanes).
+__device__ __forceinline__ int warp_intersect(const int32_t* P, int np, const int32_t* L, int64_t nl, int32_t* out,
+                                              int lane) {
+  int total = 0;
+  for (int base = 0; base < np; base += 32) {
+    int j = base + lane;
+    bool hit = j < np && kc_has(L, nl, P[j]);
+    unsigned mask = __ballot_sync(0xffffffffu, hit);
+    if (hit && out) out[total + __popc(mask & ((1u << lane) - 1))] = P[j];
+    total += __popc(mask);
+  }
+  __syncwarp();
+  return total;
+}
+
+constexpr int kKcWarps = 8;
+constexpr int kMaxK = 16;
+
+__global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, const int32_t* cols, const int32_t* esrc,
+                                                          int64_t m, int k, int cap, int32_t* scratch,
+                                                          unsigned long long* out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * kKcWarps + w;
+  const int64_t warps = (int64_t)gridDim.x * kKcWarps;
+  const int levels = k - 2;
+  int32_t* buf = scratch + gw * (int64_t)levels * cap;
+  unsigned long long cnt = 0, bytes = 0;
+  int size[kMaxK];
+  int idx[kMaxK];
+  for (int64_t e = gw; e < m; e += warps) {
+    int32_t u = esrc[e], v = cols[e];
+    int64_t ub = off[u], ud = off[u + 1] - ub;
+    int64_t vb = off[v], vd = off[v + 1] - vb;
+    bytes += 4ull * (unsigned long long)vd;
+    // C0 = N+(u) ∩ N+(v), in the order of N+(u)
+    int c0 = warp_intersect(cols + ub, (int)ud, cols + vb, vd, levels > 1 ? buf : nullptr, lane);
+    if (levels == 1) {
+      cnt += c0;
+      continue;
+    }
+    if (c0 < levels) continue;  // not enough candidates for k-2 more vertices
+    size[0] = c0;
+    idx[0] = 0;
+    int l = 0;  // level whose candidates are being chosen from
+    while (l >= 0) {
+      if (idx[l] >= size[l]) {
+        --l;
+        if (l >= 0) ++idx[l];
+        continue;
+      }
+      // choose x from C(l); the next level is all of C(l) ∩ N+(x) (lists are sorted by
+      // id, not by orientation order, so no prefix of C(l) can be skipped)
+      int32_t x = buf[(int64_t)l * cap + idx[l]];
+      int64_t xb = off[x], xd = off[x + 1] - xb;
+      bytes += 4ull * (unsigned long long)xd;
+      const int32_t* P = buf + (int64_t)l * cap;
+      if (l == levels - 2) {
+        cnt += warp_intersect(P, size[l], cols + xb, xd, nullptr, lane);  // k-th vertices
+        ++idx[l];
+      } else {
+        int c = warp_intersect(P, size[l], cols + xb, xd, buf + (int64_t)(l + 1) * cap, lane);
+        if (c >= levels - 1 - l) {
+          ++l;
+          size[l] = c;
+          idx[l] = 0;
+        } else {
+          ++idx[l];
+        }
+      }
+    }
+  }
+  if (lane != 0) { cnt = 0; bytes = 0; }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+  }
+  if (lane == 0) {
+    if (cnt) atomicAdd(out, cnt);
+    if (bytes) atomicAdd(out + 1, bytes);
+  }
+}
+
+}  // namespace
+
+}  // namespace atc
+
+using namespace atc;
+
+extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
+  ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
+  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  cudaStream_t s = as_stream(st);
+  *count = 0;
+  unsigned long long h[2] = {0, 0};
+  EventTimer tm;
+  int launches = 0;
+  if (csr->m > 0) {
+    CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+    int cap = std::max(csr->max_outdeg, 1);
+    int levels = (int)k - 2;
+    int bps = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kcl_kernel, kKcWarps * 32, 0);
+    if (bps < 1) bps = 1;
+    int64_t grid = (int64_t)sm_count() * bps;
+    // keep the scratch within 4 GiB
+    int64_t per_warp = (int64_t)levels * cap * 4;
+    while (grid > sm_count() && grid * kKcWarps * per_warp > (4ll << 30)) grid /= 2;
+    DevBuf<int32_t> scratch;
+    ATC_TRY(scratch.alloc((size_t)grid * kKcWarps * levels * cap, s));
+    tm.start(s);
+    ATC_CK(cudaMemsetAsync(pv->counter, 0, 2 * sizeof(unsigned long long), s));
+    kcl_kernel<<<(unsigned)grid, kKcWarps * 32, 0, s>>>(csr->offsets, csr->cols, pv->esrc, csr->m, (int)k, cap,
+                                                         scratch.p, pv->counter);
+    ATC_CK(cudaGetLastError());
+    tm.stop(s);
+    launches = 1;
+    ATC_CK(cudaMemcpyAsync(h, pv->counter, sizeof(h), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    *count = h[0];
+  }
+  if (stats) {
+    stats->kernel_ms = csr->m > 0 ? tm.ms() : 0.0f;
+    stats->total_ms = stats->kernel_ms;
+    stats->alg_bytes = h[1];
+    stats->wedges = (uint64_t)csr->wedges;
+    stats->kernel_used = 0;
+    stats->launches = launches;
+  }
+  return ATC_OK;
+}

@@ -1,0 +1,152 @@
+// A-direction peel on the GPU, level-synchronous.
+//
+// The reference peels serially (edge_directing/A-direction-seri.cpp:35-153): each outer
+// step admits every unpeeled vertex whose runtime degree rt (twice its remaining degree)
+// is <= a float threshold, then repeats waves in which every frontier vertex lowers rt of
+// each unpeeled neighbour by 2 and a neighbour that reaches the threshold joins the next
+// wave with the next priority.  Which vertices cross in a wave depends only on the set
+// of frontier vertices (rt falls by exactly 2 per frontier neighbour until it crosses),
+// never on the order the serial loop visits them, and the rt of already-peeled vertices
+// (changed by the tie rule at :99-103) never feeds back into a priority.  A wave is
+// therefore one parallel pass: atomicSub(rt[y], 2) on each unpeeled neighbour; the one
+// subtraction that takes rt from above the threshold to at or below it admits y.  The
+// float threshold arithmetic runs on the host exactly as in the reference (:37, :77, :127).
+#include <vector>
+
+#include "internal.cuh"
+
+namespace atc {
+
+namespace {
+
+__global__ void sym_scatter_kernel(const uint64_t* keys, int64_t m, int B, unsigned long long* cur, int32_t* adj) {
+  uint64_t mask = (1ull << B) - 1;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    uint64_t k = keys[i];
+    int32_t a = (int32_t)(k >> B), b = (int32_t)(k & mask);
+    adj[atomicAdd(&cur[a], 1ull)] = b;
+    adj[atomicAdd(&cur[b], 1ull)] = a;
+  }
+}
+
+__global__ void peel_init_kernel(const int32_t* deg, int64_t n, int32_t* rt, int32_t* prio) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    rt[v] = 2 * deg[v];
+    prio[v] = -1;
+  }
+}
+
+// Outer step (A-direction-seri.cpp:83-89): admit every unpeeled v with rt[v] <= thr.
+__global__ void peel_scan_kernel(const int32_t* rt, int32_t* prio, int64_t n, float thr, int32_t p,
+                                 int32_t* frontier, int* count) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    if (prio[v] == -1 && (float)rt[v] <= thr) {
+      prio[v] = p;
+      frontier[atomicAdd(count, 1)] = (int32_t)v;
+    }
+  }
+}
+
+// One wave (A-direction-seri.cpp:92-121): a warp per frontier vertex, lanes over its
+// neighbours.  prio[y] only ever moves from -1 to a value, so a stale -1 read costs at
+// most a harmless extra decrement of an already-admitted vertex.
+__global__ void peel_wave_kernel(const int32_t* frontier, int nf, const int64_t* off, const int32_t* adj,
+                                 int32_t* rt, int32_t* prio, float thr, int32_t p, int32_t* next, int* count) {
+  int lane = threadIdx.x & 31;
+  int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; f < nf; f += warps) {
+    int32_t x = frontier[f];
+    int64_t b = off[x], e = off[x + 1];
+    for (int64_t j = b + lane; j < e; j += 32) {
+      int32_t y = adj[j];
+      if (*(volatile int32_t*)&prio[y] != -1) continue;
+      int32_t old = atomicSub(&rt[y], 2);
+      if ((float)old > thr && (float)(old - 2) <= thr) {
+        prio[y] = p;
+        next[atomicAdd(count, 1)] = y;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* prio, int* waves_out, cudaStream_t s) {
+  int64_t n = e.n_in, m = e.m;
+  *waves_out = 0;
+  if (n == 0) return ATC_OK;
+  // symmetric adjacency (lists unsorted: the peel only needs neighbour sets)
+  DevBuf<int64_t> off;
+  DevBuf<unsigned long long> cur;
+  DevBuf<int32_t> adj, rt, fa, fb;
+  DevBuf<int> cnt;
+  ATC_TRY(off.alloc(n + 1, s));
+  ATC_TRY(exclusive_scan_i32_to_i64(deg, off.p, n, s));
+  int64_t total = 2 * m;
+  ATC_CK(cudaMemcpyAsync(off.p + n, &total, sizeof(total), cudaMemcpyHostToDevice, s));
+  ATC_TRY(cur.alloc(n, s));
+  ATC_CK(cudaMemcpyAsync(cur.p, off.p, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s));
+  ATC_TRY(adj.alloc(total, s));
+  if (m) sym_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(e.keys.p, m, e.bits, cur.p, adj.p);
+  ATC_CK(cudaGetLastError());
+  cur.release();
+  ATC_TRY(rt.alloc(n, s));
+  ATC_TRY(fa.alloc(n, s));
+  ATC_TRY(fb.alloc(n, s));
+  ATC_TRY(cnt.alloc(1, s));
+  peel_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(deg, n, rt.p, prio);
+  ATC_CK(cudaGetLastError());
+
+  // Host-side threshold arithmetic, as A-direction-seri.cpp:37,77,127 (edgeNum = 2m as
+  // unsigned, nodeNum = max id + 1 as int).
+  unsigned edgeNum = (unsigned)total;
+  int nodeNum = (int)n;
+  float threshold = ((float)edgeNum) / nodeNum + 1;
+  int threshold_old = threshold;
+  int32_t p = 0;
+  int64_t peeled = 0;
+  int waves = 0;
+  int32_t* F = fa.p;
+  int32_t* N = fb.p;
+  int hcnt = 0;
+  for (;;) {
+    ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int), s));
+    peel_scan_kernel<<<grid_for(n, 256), 256, 0, s>>>(rt.p, prio, n, threshold, p, F, cnt.p);
+    ATC_CK(cudaGetLastError());
+    ATC_CK(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    int nf = hcnt;
+    peeled += nf;
+    ++p;
+    while (nf > 0) {
+      ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int), s));
+      peel_wave_kernel<<<grid_for((int64_t)nf * 32, 256), 256, 0, s>>>(F, nf, off.p, adj.p, rt.p, prio, threshold, p,
+                                                                      N, cnt.p);
+      ATC_CK(cudaGetLastError());
+      ATC_CK(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      ATC_CK(cudaStreamSynchronize(s));
+      std::swap(F, N);
+      nf = hcnt;
+      peeled += nf;
+      ++p;
+      ++waves;
+    }
+    if (peeled >= n) break;
+    float grown = threshold + threshold_old;
+    if (!(grown > threshold)) {
+      // float addition no longer moves the threshold: the serial reference would loop
+      // forever here (runtime degrees above 2^24 are needed to get this far)
+      set_error("A-direction threshold stopped growing at %g with %lld vertices unpeeled", (double)threshold,
+                (long long)(n - peeled));
+      return ATC_ERR_UNSUPPORTED;
+    }
+    threshold = grown;
+  }
+  *waves_out = waves;
+  return ATC_OK;
+}
+
+}  // namespace atc

@@ -1,0 +1,468 @@
+// preTC on the GPU: raw int32 pairs -> simple graph -> [A-order relabel] -> orientation
+// -> [degree<=1 pruning] -> oriented CSR resident in HBM.
+//
+// Stands in for preProcess() of Hu/Bisson/Fox (Hu/preTC.cu:64-296, Bisson/preTC.cu:77-293,
+// Fox/preTC.cu:64-208) and TriCore's cal_degree / redirect_edges / split
+// (tricore/src/tricount_gpu.cu:49-203).  Where the reference sorts edges in host buckets
+// and merges them into CSR on one CPU thread, everything here stays on the device:
+// 64-bit (src << B | dst) keys are radix-sorted once and the CSR offsets are read off
+// the sorted keys.
+#include <climits>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace atc {
+
+namespace {
+
+constexpr uint64_t kSentinel = ~0ull;
+
+__global__ void minmax_kernel(const int2* p, uint64_t np, int* mn, int* mx) {
+  int lo = INT_MAX, hi = INT_MIN;
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < np; i += stride) {
+    int2 e = p[i];
+    lo = min(lo, min(e.x, e.y));
+    hi = max(hi, max(e.x, e.y));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(mn, lo);
+    atomicMax(mx, hi);
+  }
+}
+
+__global__ void canon_kernel(const int2* p, uint64_t np, int B, uint64_t* keys) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < np; i += stride) {
+    int2 e = p[i];
+    if (e.x == e.y) {
+      keys[i] = kSentinel;
+    } else {
+      uint64_t lo = (uint32_t)min(e.x, e.y), hi = (uint32_t)max(e.x, e.y);
+      keys[i] = (lo << B) | hi;
+    }
+  }
+}
+
+__global__ void degree_kernel(const uint64_t* keys, int64_t m, int B, int32_t* deg) {
+  uint64_t mask = (1ull << B) - 1;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    uint64_t k = keys[i];
+    atomicAdd(&deg[k >> B], 1);
+    atomicAdd(&deg[k & mask], 1);
+  }
+}
+
+struct OrientArgs {
+  const int32_t* deg;   // simple degree, by input id
+  const int32_t* prio;  // A-direction priority, by input id (ADIRECTION only)
+  const int32_t* perm;  // new id of every input id (A-order), or null
+  const int32_t* cmap;  // compacted id of every (new) id when pruning, or null
+  int dir;
+  int bin;              // B of the input keys
+  int bout;             // B of the output keys
+};
+
+// Orientation rules (each decides src for the edge {x, y} given on new ids xn, yn):
+//   ID            src = larger id                       Bisson/preTC.cu:135-144, Fox/preTC.cu:94-98
+//   DEGREE        lower degree; tie -> larger id        Hu/preTC.cu:125-133, A-order.cpp:91-96
+//   DEGREE_LOWID  lower degree; tie -> smaller id       tricount_gpu.cu:76-78
+//   ADIRECTION    lower priority; tie -> smaller id     A-direction-seri.cpp:259-261
+__global__ void orient_kernel(const uint64_t* ek, int64_t m, OrientArgs a, uint64_t* out,
+                              unsigned long long* dropped) {
+  uint64_t mask = (1ull << a.bin) - 1;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long drop = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    uint64_t k = ek[i];
+    int32_t x = (int32_t)(k >> a.bin), y = (int32_t)(k & mask);
+    int32_t dx = a.deg[x], dy = a.deg[y];
+    if (a.cmap && (dx <= 1 || dy <= 1)) {
+      out[i] = kSentinel;
+      ++drop;
+      continue;
+    }
+    int32_t xn = a.perm ? a.perm[x] : x, yn = a.perm ? a.perm[y] : y;
+    bool x_src;
+    switch (a.dir) {
+      case ATC_DIR_ID: x_src = xn > yn; break;
+      case ATC_DIR_DEGREE: x_src = dx < dy || (dx == dy && xn > yn); break;
+      case ATC_DIR_DEGREE_LOWID: x_src = dx < dy || (dx == dy && xn < yn); break;
+      default: {
+        int32_t px = a.prio[x], py = a.prio[y];
+        x_src = py > px || (py == px && xn < yn);
+      }
+    }
+    int32_t s = x_src ? xn : yn, d = x_src ? yn : xn;
+    if (a.cmap) {
+      s = a.cmap[s];
+      d = a.cmap[d];
+    }
+    out[i] = ((uint64_t)(uint32_t)s << a.bout) | (uint32_t)d;
+  }
+  for (int o = 16; o > 0; o >>= 1) drop += __shfl_xor_sync(0xffffffffu, drop, o);
+  if ((threadIdx.x & 31) == 0 && drop) atomicAdd(dropped, drop);
+}
+
+// offsets[v] = first index whose source is >= v, for v in [0, n]; sentinels sort last.
+__global__ void offsets_kernel(const uint64_t* k, int64_t m, int B, int64_t n, int64_t* off) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v <= n; v += stride) {
+    int64_t lo = 0, hi = m;
+    while (lo < hi) {
+      int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)(k[mid] >> B) < v) lo = mid + 1; else hi = mid;
+    }
+    off[v] = lo;
+  }
+}
+
+__global__ void split_kernel(const uint64_t* k, int64_t m, int B, int32_t* cols, int32_t* esrc) {
+  uint64_t mask = (1ull << B) - 1;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    uint64_t x = k[i];
+    cols[i] = (int32_t)(x & mask);
+    esrc[i] = (int32_t)(x >> B);
+  }
+}
+
+__global__ void indeg_kernel(const int32_t* cols, int64_t m, int32_t* indeg) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) atomicAdd(&indeg[cols[i]], 1);
+}
+
+__global__ void wedge_kernel(const int64_t* off, const int32_t* indeg, int64_t n, unsigned long long* w,
+                             int* maxout) {
+  unsigned long long s = 0;
+  int mo = 0;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    int64_t d = off[v + 1] - off[v];
+    s += (unsigned long long)indeg[v] * (unsigned long long)d;
+    mo = max(mo, (int)d);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    mo = max(mo, __shfl_xor_sync(0xffffffffu, mo, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(w, s);
+    atomicMax(maxout, mo);
+  }
+}
+
+__global__ void keep_kernel(const int32_t* deg, const int32_t* perm, int64_t n, int32_t* keep) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    int32_t nv = perm ? perm[v] : (int32_t)v;
+    keep[nv] = deg[v] >= 2 ? 1 : 0;
+  }
+}
+
+__global__ void i64_to_i32_kernel(const int64_t* in, int64_t n, int32_t* out) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (int32_t)in[i];
+}
+
+__global__ void iota_kernel(int32_t* p, int64_t n) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) p[i] = (int32_t)i;
+}
+
+__global__ void keys_to_pairs_kernel(const uint64_t* k, int64_t m, int B, int2* out) {
+  uint64_t mask = (1ull << B) - 1;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride)
+    out[i] = make_int2((int32_t)(k[i] >> B), (int32_t)(k[i] & mask));
+}
+
+// Largest "hi" endpoint over canonical keys: the largest id that has an edge.
+__global__ void max_hi_kernel(const uint64_t* k, int64_t m, int B, int* mx) {
+  uint64_t mask = (1ull << B) - 1;
+  int best = 0;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride)
+    best = max(best, (int)(k[i] & mask));
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, best);
+}
+
+void keep_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) return;
+  uint64_t thr = UINT64_MAX;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+}
+
+}  // namespace
+
+atc_status build_simple_edges(const int2* pairs, uint64_t np, SimpleEdges* out, cudaStream_t s) {
+  keep_pool();
+  out->m = 0;
+  out->n_in = 0;
+  out->bits = 1;
+  if (np == 0) return ATC_OK;
+  DevBuf<int> mm;
+  ATC_TRY(mm.alloc(2, s));
+  int init[2] = {INT_MAX, INT_MIN};
+  ATC_CK(cudaMemcpyAsync(mm.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  minmax_kernel<<<grid_for(np, 256), 256, 0, s>>>(pairs, np, mm.p, mm.p + 1);
+  ATC_CK(cudaGetLastError());
+  int h[2];
+  ATC_CK(cudaMemcpyAsync(h, mm.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (h[0] < 0) {
+    set_error("negative vertex id %d in the input pairs", h[0]);
+    return ATC_ERR_INVALID;
+  }
+  out->n_in = (int64_t)h[1] + 1;
+  out->bits = id_bits(out->n_in);
+  DevBuf<uint64_t> a, b;
+  ATC_TRY(a.alloc(np, s));
+  ATC_TRY(b.alloc(np, s));
+  canon_kernel<<<grid_for(np, 256), 256, 0, s>>>(pairs, np, out->bits, a.p);
+  ATC_CK(cudaGetLastError());
+  uint64_t* ka = a.p;
+  uint64_t* kb = b.p;
+  ATC_TRY(sort_keys_u64(ka, kb, np, 0, 2 * out->bits, s));
+  size_t nu = 0;
+  ATC_TRY(unique_u64(ka, kb, np, &nu, s));
+  uint64_t last = 0;
+  if (nu) {
+    ATC_CK(cudaMemcpyAsync(&last, kb + nu - 1, sizeof(last), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+  }
+  out->m = (int64_t)nu - (nu && last == kSentinel ? 1 : 0);
+  // keep whichever buffer holds the unique keys
+  if (kb == b.p) { out->keys = std::move(b); } else { out->keys = std::move(a); }
+  return ATC_OK;
+}
+
+atc_status simple_degrees(const SimpleEdges& e, int32_t* deg, cudaStream_t s) {
+  ATC_CK(cudaMemsetAsync(deg, 0, sizeof(int32_t) * e.n_in, s));
+  if (e.m) degree_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, e.bits, deg);
+  ATC_CK(cudaGetLastError());
+  return ATC_OK;
+}
+
+static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_order order, const atc_tuning* t,
+                             atc_csr* out, int32_t* perm_out, cudaStream_t s) {
+  ATC_CHECK_ARG(out != nullptr, "out is NULL");
+  ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION, "unknown atc_dir");
+  ATC_CHECK_ARG(order == ATC_ORDER_NONE || order == ATC_ORDER_AORDER, "unknown atc_order");
+  *out = atc_csr{};
+  bool prune = t && t->prune_deg1;
+  SimpleEdges e;
+  ATC_TRY(build_simple_edges(pairs, np, &e, s));
+  int64_t n_in = e.n_in;
+  DevBuf<int32_t> deg, prio, perm, cmap;
+  ATC_TRY(deg.alloc(n_in, s));
+  ATC_TRY(simple_degrees(e, deg.p, s));
+  if (order == ATC_ORDER_AORDER) {
+    // A-order sees the simple graph with each edge once, as when it reads the output
+    // of A-direction-seri; its id range ends at the largest id that has an edge.
+    ATC_TRY(perm.alloc(n_in, s));
+    iota_kernel<<<grid_for(n_in, 256), 256, 0, s>>>(perm.p, n_in);
+    ATC_CK(cudaGetLastError());
+    int64_t n_v = 0;
+    if (e.m) {
+      DevBuf<int> mx;
+      ATC_TRY(mx.alloc(1, s));
+      ATC_CK(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
+      max_hi_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, e.bits, mx.p);
+      ATC_CK(cudaGetLastError());
+      int h = 0;
+      ATC_CK(cudaMemcpyAsync(&h, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      ATC_CK(cudaStreamSynchronize(s));
+      n_v = (int64_t)h + 1;
+    }
+    ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s));
+  }
+  if (dir == ATC_DIR_ADIRECTION) {
+    ATC_TRY(prio.alloc(n_in, s));
+    int waves = 0;
+    ATC_TRY(peel_priorities(e, deg.p, prio.p, &waves, s));
+  }
+  int64_t n = n_in;
+  if (prune) {
+    DevBuf<int32_t> keep;
+    DevBuf<int64_t> pre;
+    ATC_TRY(keep.alloc(n_in + 1, s));
+    ATC_TRY(pre.alloc(n_in + 1, s));
+    ATC_CK(cudaMemsetAsync(keep.p, 0, sizeof(int32_t) * (n_in + 1), s));
+    keep_kernel<<<grid_for(n_in, 256), 256, 0, s>>>(deg.p, perm.p, n_in, keep.p);
+    ATC_CK(cudaGetLastError());
+    ATC_TRY(exclusive_scan_i32_to_i64(keep.p, pre.p, n_in + 1, s));
+    ATC_TRY(cmap.alloc(n_in + 1, s));
+    i64_to_i32_kernel<<<grid_for(n_in + 1, 256), 256, 0, s>>>(pre.p, n_in + 1, cmap.p);
+    ATC_CK(cudaGetLastError());
+    int64_t kept = 0;
+    ATC_CK(cudaMemcpyAsync(&kept, pre.p + n_in, sizeof(kept), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    n = kept;
+  }
+  int bout = id_bits(n);
+  DevBuf<uint64_t> k1, k2;
+  DevBuf<unsigned long long> dropped;
+  ATC_TRY(k1.alloc(e.m, s));
+  ATC_TRY(k2.alloc(e.m, s));
+  ATC_TRY(dropped.alloc(1, s));
+  ATC_CK(cudaMemsetAsync(dropped.p, 0, sizeof(unsigned long long), s));
+  OrientArgs oa{deg.p, prio.p, perm.p, cmap.p, (int)dir, e.bits, bout};
+  if (e.m) orient_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, oa, k1.p, dropped.p);
+  ATC_CK(cudaGetLastError());
+  e.keys.release();
+  uint64_t* ka = k1.p;
+  uint64_t* kb = k2.p;
+  ATC_TRY(sort_keys_u64(ka, kb, e.m, 0, 2 * bout, s));
+  unsigned long long hdrop = 0;
+  ATC_CK(cudaMemcpyAsync(&hdrop, dropped.p, sizeof(hdrop), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  int64_t m = e.m - (int64_t)hdrop;
+
+  // Own buffers of the CSR.  cols gets 16 ints of padding so that 16-byte-rounded bulk
+  // copies of any list stay inside the allocation.
+  DevBuf<int64_t> off;
+  DevBuf<int32_t> cols, esrc, indeg;
+  DevBuf<unsigned long long> counter;
+  ATC_TRY(off.alloc(n + 1, s));
+  ATC_TRY(cols.alloc(m + 16, s));
+  ATC_TRY(esrc.alloc(m + 16, s));
+  ATC_TRY(counter.alloc(4, s));
+  ATC_CK(cudaMemsetAsync(cols.p + m, 0, sizeof(int32_t) * 16, s));
+  offsets_kernel<<<grid_for(n + 1, 256), 256, 0, s>>>(ka, m, bout, n, off.p);
+  ATC_CK(cudaGetLastError());
+  if (m) split_kernel<<<grid_for(m, 256), 256, 0, s>>>(ka, m, bout, cols.p, esrc.p);
+  ATC_CK(cudaGetLastError());
+  // W = sum_v indeg(v) * outdeg(v) and the largest out-degree
+  ATC_TRY(indeg.alloc(n + 1, s));
+  ATC_CK(cudaMemsetAsync(indeg.p, 0, sizeof(int32_t) * (n + 1), s));
+  ATC_CK(cudaMemsetAsync(counter.p, 0, sizeof(unsigned long long) * 4, s));
+  if (m) indeg_kernel<<<grid_for(m, 256), 256, 0, s>>>(cols.p, m, indeg.p);
+  if (n) wedge_kernel<<<grid_for(n, 256), 256, 0, s>>>(off.p, indeg.p, n, counter.p, (int*)(counter.p + 1));
+  ATC_CK(cudaGetLastError());
+  unsigned long long hw[2] = {0, 0};
+  ATC_CK(cudaMemcpyAsync(hw, counter.p, sizeof(hw), cudaMemcpyDeviceToHost, s));
+  if (perm_out && order == ATC_ORDER_AORDER && n_in)
+    ATC_CK(cudaMemcpyAsync(perm_out, perm.p, sizeof(int32_t) * n_in, cudaMemcpyDeviceToHost, s));
+  else if (perm_out && n_in) {
+    std::vector<int32_t> id(n_in);
+    for (int64_t i = 0; i < n_in; ++i) id[i] = (int32_t)i;
+    std::copy(id.begin(), id.end(), perm_out);
+  }
+  ATC_CK(cudaStreamSynchronize(s));
+
+  CsrPriv* pv = new CsrPriv();
+  pv->esrc = esrc.detach();
+  pv->counter = counter.detach();
+  pv->bits = bout;
+  out->n = n;
+  out->m = m;
+  out->offsets = off.detach();
+  out->cols = cols.detach();
+  out->n_input = n_in;
+  out->wedges = (int64_t)hw[0];
+  out->dir = (int32_t)dir;
+  out->order = (int32_t)order;
+  out->pruned = prune ? 1 : 0;
+  out->max_outdeg = (int32_t)(hw[1] & 0xffffffffu);
+  out->priv = pv;
+  return ATC_OK;
+}
+
+}  // namespace atc
+
+using namespace atc;
+
+extern "C" atc_status atc_pretc_device(const int32_t* pairs_dev, uint64_t np, atc_dir dir, atc_order order,
+                                       const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) {
+  ATC_CHECK_ARG(np == 0 || pairs_dev != nullptr, "pairs_dev is NULL");
+  return pretc_impl(reinterpret_cast<const int2*>(pairs_dev), np, dir, order, t, out, perm_out, as_stream(s));
+}
+
+extern "C" atc_status atc_pretc(const int32_t* pairs, uint64_t np, atc_dir dir, atc_order order,
+                                const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) {
+  ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
+  cudaStream_t st = as_stream(s);
+  keep_pool();
+  DevBuf<int2> d;
+  ATC_TRY(d.alloc(np, st));
+  if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
+  return pretc_impl(d.p, np, dir, order, t, out, perm_out, st);
+}
+
+extern "C" atc_status atc_csr_to_host(const atc_csr* csr, int64_t* offsets, int32_t* cols, atc_stream s) {
+  ATC_CHECK_ARG(csr != nullptr && offsets != nullptr && cols != nullptr, "NULL argument");
+  cudaStream_t st = as_stream(s);
+  ATC_CK(cudaMemcpyAsync(offsets, csr->offsets, sizeof(int64_t) * (csr->n + 1), cudaMemcpyDeviceToHost, st));
+  if (csr->m) ATC_CK(cudaMemcpyAsync(cols, csr->cols, sizeof(int32_t) * csr->m, cudaMemcpyDeviceToHost, st));
+  ATC_CK(cudaStreamSynchronize(st));
+  return ATC_OK;
+}
+
+extern "C" atc_status atc_csr_free(atc_csr* csr) {
+  if (!csr) return ATC_OK;
+  if (csr->offsets) cudaFree(csr->offsets);
+  if (csr->cols) cudaFree(csr->cols);
+  if (csr->priv) {
+    CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+    if (pv->esrc) cudaFree(pv->esrc);
+    if (pv->counter) cudaFree(pv->counter);
+    delete pv;
+  }
+  *csr = atc_csr{};
+  return ATC_OK;
+}
+
+// A-direction-seri as a library call: orient the simple graph by peel priority and emit
+// the edges sorted by (src, dst) — the byte order of lpBasedGraph.bin (A-direction-seri.cpp:254-273).
+extern "C" atc_status atc_adirection(const int32_t* pairs, uint64_t np, int32_t* oriented_out, uint64_t* n_out,
+                                     int32_t* prio_out, atc_stream st) {
+  ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
+  ATC_CHECK_ARG(np == 0 || (pairs != nullptr && oriented_out != nullptr), "NULL array");
+  cudaStream_t s = as_stream(st);
+  keep_pool();
+  *n_out = 0;
+  DevBuf<int2> d;
+  ATC_TRY(d.alloc(np, s));
+  if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, s));
+  SimpleEdges e;
+  ATC_TRY(build_simple_edges(d.p, np, &e, s));
+  d.release();
+  if (e.n_in == 0) return ATC_OK;
+  DevBuf<int32_t> deg, prio;
+  ATC_TRY(deg.alloc(e.n_in, s));
+  ATC_TRY(prio.alloc(e.n_in, s));
+  ATC_TRY(simple_degrees(e, deg.p, s));
+  int waves = 0;
+  ATC_TRY(peel_priorities(e, deg.p, prio.p, &waves, s));
+  DevBuf<uint64_t> k1, k2;
+  DevBuf<unsigned long long> dropped;
+  ATC_TRY(k1.alloc(e.m, s));
+  ATC_TRY(k2.alloc(e.m, s));
+  ATC_TRY(dropped.alloc(1, s));
+  OrientArgs oa{deg.p, prio.p, nullptr, nullptr, ATC_DIR_ADIRECTION, e.bits, e.bits};
+  if (e.m) orient_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, oa, k1.p, dropped.p);
+  ATC_CK(cudaGetLastError());
+  uint64_t* ka = k1.p;
+  uint64_t* kb = k2.p;
+  ATC_TRY(sort_keys_u64(ka, kb, e.m, 0, 2 * e.bits, s));
+  DevBuf<int2> o;
+  ATC_TRY(o.alloc(e.m, s));
+  if (e.m) keys_to_pairs_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(ka, e.m, e.bits, o.p);
+  ATC_CK(cudaGetLastError());
+  if (e.m) ATC_CK(cudaMemcpyAsync(oriented_out, o.p, sizeof(int2) * e.m, cudaMemcpyDeviceToHost, s));
+  if (prio_out) ATC_CK(cudaMemcpyAsync(prio_out, prio.p, sizeof(int32_t) * e.n_in, cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  *n_out = (uint64_t)e.m;
+  return ATC_OK;
+}

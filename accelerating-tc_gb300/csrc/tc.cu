@@ -1,0 +1,560 @@
+// Triangle counting on an oriented CSR: the four kernel families of the reference,
+// re-designed for sm_103a.  All count sum_u sum_{v in N+(u)} |N+(u) ∩ N+(v)| exactly in
+// uint64; every warp reduces its lanes with shuffles and adds once to a 64-bit counter.
+//
+//   Hu-style      Hu/tc.cu:22-201       CTA per balanced vertex range; runs of
+//                                        consecutive N+(u) staged in shared memory; a
+//                                        warp per edge streams N+(v) (coalesced) and
+//                                        binary-searches each element in the staged N+(u).
+//   Bisson-style  Bisson/tc.cu:18-104   out-degree > cutover: CTA per row, N+(u) as a
+//                                        bitmap (shared memory over [min,max] of the
+//                                        row, or a per-CTA global bitmap), one bit test
+//                                        per candidate; smaller rows: warp per row, row
+//                                        in shared memory, binary search.
+//   Fox-style     Fox/tc.cu:18-125,     per-edge work min*log2(max+2); edges binned on
+//                 316-384                the device into 1,2,4,...,32 threads per edge;
+//                                        each thread searches a slice of the shorter list
+//                                        in the longer one.
+//   TriCore-style tricount_gpu.cu:215-290  warp per edge; 32 pivots of the longer list
+//                                        in shared memory bracket each element of the
+//                                        shorter list, then a binary search inside the
+//                                        bracket.
+#include <cmath>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace atc {
+
+struct CsrView {
+  const int64_t* off;
+  const int32_t* cols;
+  const int32_t* esrc;
+  int64_t n, m;
+};
+
+namespace {
+
+__device__ __forceinline__ void warp_add_count(unsigned long long c, unsigned long long* out) {
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// Number of elements < x in a sorted list (lower bound), list in any address space.
+__device__ __forceinline__ bool bsearch_has(const int32_t* a, int64_t n, int32_t x) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    int32_t y = a[mid];
+    if (y < x) lo = mid + 1; else hi = mid;
+  }
+  return lo < n && a[lo] == x;
+}
+
+__device__ __forceinline__ bool bsearch_has32(const int32_t* a, int n, int32_t x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo < n && a[lo] == x;
+}
+
+// ============================== TriCore-style ======================================
+constexpr int kTriWarps = 8;
+
+__global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsigned long long* out) {
+  __shared__ int32_t piv[kTriWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long cnt = 0;
+  const int64_t warps = (int64_t)gridDim.x * kTriWarps;
+  for (int64_t e = (int64_t)blockIdx.x * kTriWarps + w; e < g.m; e += warps) {
+    int32_t u = g.esrc[e], v = g.cols[e];
+    int64_t au = g.off[u], du = g.off[u + 1] - au;
+    int64_t av = g.off[v], dv = g.off[v + 1] - av;
+    const int32_t* A = g.cols + (du >= dv ? au : av);
+    const int32_t* Bl = g.cols + (du >= dv ? av : au);
+    int64_t da = du >= dv ? du : dv, db = du >= dv ? dv : du;
+    if (db == 0) continue;
+    piv[w][lane] = A[(int64_t)lane * da / 32];
+    __syncwarp();
+    for (int64_t j = lane; j < db; j += 32) {
+      int32_t x = Bl[j];
+      // k = number of pivots <= x
+      int lo = 0, hi = 32;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (piv[w][mid] <= x) lo = mid + 1; else hi = mid;
+      }
+      if (lo == 0) continue;                 // x < A[0]
+      if (piv[w][lo - 1] == x) { ++cnt; continue; }
+      int64_t b = (int64_t)(lo - 1) * da / 32 + 1;  // strictly inside the bracket
+      int64_t e2 = lo == 32 ? da : (int64_t)lo * da / 32;
+      if (b < e2 && bsearch_has(A + b, e2 - b, x)) ++cnt;
+    }
+    __syncwarp();
+  }
+  warp_add_count(cnt, out);
+}
+
+// ============================== Fox-style ==========================================
+// Work of an edge (Fox/tc.cu:22-31): min(d+u, d+v) * log2(max + 2), as an int.
+__device__ __forceinline__ int fox_work(int64_t du, int64_t dv) {
+  int64_t big = du > dv ? du : dv, small = du > dv ? dv : du;
+  double wv = (double)small * log2((double)big + 2.0);
+  return wv > 2147483647.0 ? 2147483647 : (int)wv;
+}
+
+__global__ void fox_maxwork_kernel(CsrView g, int* maxw) {
+  int best = 0;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.m; e += stride) {
+    int32_t u = g.esrc[e], v = g.cols[e];
+    best = max(best, fox_work(g.off[u + 1] - g.off[u], g.off[v + 1] - g.off[v]));
+  }
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxw, best);
+}
+
+struct FoxBins {
+  int bound[7];  // work thresholds: bin b holds work in [bound[b], bound[b+1])
+};
+
+__device__ __forceinline__ int fox_bin(const FoxBins& fb, int wk) {
+  int b = 0;
+#pragma unroll
+  for (int i = 1; i < 6; ++i) b += wk >= fb.bound[i];
+  return b;
+}
+
+__global__ void fox_hist_kernel(CsrView g, FoxBins fb, unsigned long long* hist) {
+  __shared__ unsigned int h[6];
+  if (threadIdx.x < 6) h[threadIdx.x] = 0;
+  __syncthreads();
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.m; e += stride) {
+    int32_t u = g.esrc[e], v = g.cols[e];
+    atomicAdd(&h[fox_bin(fb, fox_work(g.off[u + 1] - g.off[u], g.off[v + 1] - g.off[v]))], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)h[threadIdx.x]);
+}
+
+__global__ void fox_scatter_kernel(CsrView g, FoxBins fb, unsigned long long* cursor, int64_t* list) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.m; e += stride) {
+    int32_t u = g.esrc[e], v = g.cols[e];
+    int b = fox_bin(fb, fox_work(g.off[u + 1] - g.off[u], g.off[v + 1] - g.off[v]));
+    list[atomicAdd(&cursor[b], 1ull)] = e;
+  }
+}
+
+// T threads per edge (Fox/tc.cu:64-125): each thread takes every T-th element of the
+// shorter list and binary-searches it in the longer list.
+template <int T>
+__global__ void __launch_bounds__(256) fox_kernel(CsrView g, const int64_t* list, int64_t cnt_edges,
+                                                  unsigned long long* out) {
+  unsigned long long cnt = 0;
+  const int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int sub = (int)(gid % T);
+  const int64_t groups = (int64_t)gridDim.x * blockDim.x / T;
+  for (int64_t i = gid / T; i < cnt_edges; i += groups) {
+    int64_t e = list[i];
+    int32_t u = g.esrc[e], v = g.cols[e];
+    int64_t au = g.off[u], du = g.off[u + 1] - au;
+    int64_t av = g.off[v], dv = g.off[v + 1] - av;
+    const int32_t* L = g.cols + (du >= dv ? au : av);   // longer
+    const int32_t* S = g.cols + (du >= dv ? av : au);   // shorter
+    int64_t dl = du >= dv ? du : dv, ds = du >= dv ? dv : du;
+    for (int64_t j = sub; j < ds; j += T) cnt += bsearch_has(L, dl, S[j]);
+  }
+  warp_add_count(cnt, out);
+}
+
+// Fox's interleave (Fox/tc.cu:127-183): a bin's edges are sorted by the length of
+// their longer list, cut into groups of 32 and dealt round-robin over `nblk` blocks, so
+// every block gets a mix of long and short edges.  Group g = sec*nblk + first moves to
+// rank first*q + min(first, r) + sec (q, r = ngroups / nblk, ngroups % nblk): a
+// bijection on the groups; the tail of fewer than 32 edges stays in place.
+__global__ void fox_lenkey_kernel(CsrView g, const int64_t* list, int64_t nb, uint64_t* keys) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += stride) {
+    int64_t e = list[i];
+    int32_t u = g.esrc[e], v = g.cols[e];
+    int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+    uint64_t mx = (uint64_t)(du > dv ? du : dv);
+    if (mx > 0x7fffffffull) mx = 0x7fffffffull;
+    keys[i] = (mx << 32) | (uint64_t)i;
+  }
+}
+
+__global__ void fox_deal_kernel(const uint64_t* keys, const int64_t* list, int64_t nb, int64_t nblk, int64_t* out) {
+  int64_t ngroups = nb / 32;
+  int64_t q = nblk > 0 ? ngroups / nblk : 0, r = nblk > 0 ? ngroups % nblk : 0;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb; i += stride) {
+    int64_t src = list[keys[i] & 0xffffffffull];
+    int64_t grp = i / 32, dst = i;
+    if (grp < ngroups && nblk > 1) {
+      int64_t first = grp % nblk, sec = grp / nblk;
+      dst = (first * q + (first < r ? first : r) + sec) * 32 + (i % 32);
+    }
+    out[dst] = src;
+  }
+}
+
+// ============================== Hu-style ===========================================
+constexpr int kHuWarps = 8;
+constexpr int kHuStage = 6144;  // ints of N+(u) staged per CTA (24 KB)
+
+// Per-vertex work used to cut the vertex range into CTAs of equal work: the wedges
+// u -> v -> w it opens plus its own list (a balanced form of Hu/tc.cu:22-35).
+__global__ void hu_work_kernel(CsrView g, int64_t* work) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < g.n; u += stride) {
+    int64_t b = g.off[u], e = g.off[u + 1];
+    int64_t s = (e - b) + 1;
+    for (int64_t j = b; j < e; ++j) {
+      int32_t v = g.cols[j];
+      s += g.off[v + 1] - g.off[v];
+    }
+    work[u] = s;
+  }
+}
+
+// start[b] = first vertex whose work prefix reaches b * total / nb (Hu/tc.cu:292-301).
+__global__ void hu_cut_kernel(const int64_t* prefix, int64_t n, int64_t total, int nb, int32_t* start) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b > nb) return;
+  if (b == nb) { start[b] = (int32_t)n; return; }
+  int64_t target = (int64_t)((__int128)total * b / nb);
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (prefix[mid] < target) lo = mid + 1; else hi = mid;
+  }
+  start[b] = (int32_t)lo;
+}
+
+__global__ void __launch_bounds__(kHuWarps * 32) hu_kernel(CsrView g, const int32_t* start, unsigned long long* out) {
+  __shared__ int32_t stage[kHuStage];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long cnt = 0;
+  int32_t u0 = start[blockIdx.x], uend = start[blockIdx.x + 1];
+  while (u0 < uend) {
+    // the run [u0, u1): consecutive lists that fit the stage together (at least one)
+    int64_t E0 = g.off[u0];
+    int32_t u1 = u0 + 1;
+    while (u1 < uend && g.off[u1 + 1] - E0 <= kHuStage) ++u1;
+    int64_t E1 = g.off[u1];
+    bool staged = E1 - E0 <= kHuStage;
+    if (staged) {
+      for (int64_t j = threadIdx.x; j < E1 - E0; j += blockDim.x) stage[j] = g.cols[E0 + j];
+    }
+    __syncthreads();
+    for (int64_t e = E0 + w; e < E1; e += kHuWarps) {
+      int32_t u = g.esrc[e];
+      int32_t v = staged ? stage[e - E0] : g.cols[e];
+      int64_t ub = g.off[u], ud = g.off[u + 1] - ub;
+      const int32_t* Nu = staged ? stage + (ub - E0) : g.cols + ub;
+      int64_t vb = g.off[v], vd = g.off[v + 1] - vb;
+      for (int64_t j = lane; j < vd; j += 32) cnt += bsearch_has(Nu, ud, g.cols[vb + j]);
+    }
+    __syncthreads();
+    u0 = u1;
+  }
+  warp_add_count(cnt, out);
+}
+
+// ============================== Bisson-style =======================================
+constexpr int kBiWarps = 8;
+constexpr int kBiBitmapWords = 16384;  // 64 KB shared bitmap = 524288 ids
+
+__global__ void bisson_classify_kernel(CsrView g, int cutover, int32_t* hubs, int32_t* smalls, int* counts) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < g.n; u += stride) {
+    int64_t d = g.off[u + 1] - g.off[u];
+    if (d == 0) continue;
+    if (d > cutover) hubs[atomicAdd(&counts[0], 1)] = (int32_t)u;
+    else smalls[atomicAdd(&counts[1], 1)] = (int32_t)u;
+  }
+}
+
+// Rows of out-degree <= cutover (Bisson/tc.cu:63-87): warp per row, row copied to the
+// warp's shared slot; lanes stream each N+(v) and binary-search the row.
+template <int CAP>
+__global__ void __launch_bounds__(kBiWarps * 32) bisson_small_kernel(CsrView g, const int32_t* rows, int nrows,
+                                                                   unsigned long long* out) {
+  __shared__ int32_t row[kBiWarps][CAP];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long cnt = 0;
+  const int warps = gridDim.x * kBiWarps;
+  for (int r = blockIdx.x * kBiWarps + w; r < nrows; r += warps) {
+    int32_t u = rows[r];
+    int64_t ub = g.off[u];
+    int du = (int)(g.off[u + 1] - ub);
+    for (int j = lane; j < du; j += 32) row[w][j] = g.cols[ub + j];
+    __syncwarp();
+    for (int k = 0; k < du; ++k) {
+      int32_t v = row[w][k];
+      int64_t vb = g.off[v], vd = g.off[v + 1] - vb;
+      for (int64_t j = lane; j < vd; j += 32) cnt += bsearch_has32(row[w], du, g.cols[vb + j]);
+    }
+    __syncwarp();
+  }
+  warp_add_count(cnt, out);
+}
+
+// Rows of out-degree > cutover (Bisson/tc.cu:36-62): CTA per row.  N+(u) becomes a
+// bitmap over [lo, hi] = [min, max] of the row: in shared memory when the span fits,
+// else in this CTA's slice of a global bitmap over all vertices.  Only the words the
+// row touched are cleared afterwards, never the whole bitmap.
+__global__ void __launch_bounds__(kBiWarps * 32) bisson_hub_kernel(CsrView g, const int32_t* hubs, int nhubs,
+                                                                 uint32_t* gbits, int64_t gwords,
+                                                                 unsigned long long* out) {
+  extern __shared__ uint32_t sbits[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long cnt = 0;
+  uint32_t* mybits = gbits + (int64_t)blockIdx.x * gwords;
+  for (int j = threadIdx.x; j < kBiBitmapWords; j += blockDim.x) sbits[j] = 0;
+  __syncthreads();
+  for (int h = blockIdx.x; h < nhubs; h += gridDim.x) {
+    int32_t u = hubs[h];
+    int64_t ub = g.off[u], du = g.off[u + 1] - ub;
+    const int32_t* Nu = g.cols + ub;
+    int32_t lo = Nu[0], hi = Nu[du - 1];
+    bool shared_map = (int64_t)hi - lo < (int64_t)kBiBitmapWords * 32;
+    uint32_t* bits = shared_map ? sbits : mybits;
+    int32_t base = shared_map ? lo : 0;
+    for (int64_t j = threadIdx.x; j < du; j += blockDim.x) {
+      int32_t x = Nu[j] - base;
+      atomicOr(&bits[x >> 5], 1u << (x & 31));
+    }
+    __syncthreads();
+    for (int64_t k = w; k < du; k += kBiWarps) {
+      int32_t v = Nu[k];
+      int64_t vb = g.off[v], vd = g.off[v + 1] - vb;
+      for (int64_t j = lane; j < vd; j += 32) {
+        int32_t x = g.cols[vb + j];
+        if (x < lo || x > hi) continue;
+        x -= base;
+        cnt += (bits[x >> 5] >> (x & 31)) & 1u;
+      }
+    }
+    __syncthreads();
+    for (int64_t j = threadIdx.x; j < du; j += blockDim.x) bits[(Nu[j] - base) >> 5] = 0;
+    __syncthreads();
+  }
+  warp_add_count(cnt, out);
+}
+
+int blocks_per_sm(const void* kernel, int block, size_t smem) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, block, smem) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
+
+}  // namespace
+
+// ---- family drivers ----------------------------------------------------------------
+static atc_status run_tricore(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
+                              int* launches) {
+  int grid = t && t->tricore_blocks > 0 ? t->tricore_blocks
+                                        : sm_count() * blocks_per_sm((const void*)tricore_kernel, kTriWarps * 32, 0);
+  tricore_kernel<<<grid, kTriWarps * 32, 0, s>>>(g, ctr);
+  ATC_CK(cudaGetLastError());
+  *launches += 1;
+  return ATC_OK;
+}
+
+static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
+                          int* launches) {
+  DevBuf<int> mx;
+  DevBuf<unsigned long long> hist, cursor;
+  ATC_TRY(mx.alloc(1, s));
+  ATC_TRY(hist.alloc(6, s));
+  ATC_TRY(cursor.alloc(6, s));
+  ATC_CK(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
+  ATC_CK(cudaMemsetAsync(hist.p, 0, sizeof(unsigned long long) * 6, s));
+  fox_maxwork_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, mx.p);
+  ATC_CK(cudaGetLastError());
+  int maxw = 0;
+  ATC_CK(cudaMemcpyAsync(&maxw, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  // Bin boundaries of Fox/tc.cu:318-331: partition points 8^((log8(max)-1)(i-1)/32 + 1)
+  // for i = 2, 4, ..., 32; bin i threads holds work in [pp(i), pp(2i)).
+  int wpt = t && t->fox_work_per_thread > 1 ? t->fox_work_per_thread : 8;
+  FoxBins fb;
+  fb.bound[0] = INT32_MIN;
+  double maxPow = maxw > 0 ? std::log((double)maxw) / std::log((double)wpt) : 0.0;
+  int k = 1;
+  for (int i = 2; i <= 32; i *= 2, ++k) {
+    double index = (maxPow - 1) * (i - 1) / 32.0 + 1;
+    long double pp = powl((long double)wpt, (long double)index);
+    fb.bound[k] = pp > 2147483647.0L ? 2147483647 : (int)pp;
+  }
+  fb.bound[6] = INT32_MAX;
+  fox_hist_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, fb, hist.p);
+  ATC_CK(cudaGetLastError());
+  unsigned long long h[6];
+  ATC_CK(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  unsigned long long start[7];
+  start[0] = 0;
+  for (int b = 0; b < 6; ++b) start[b + 1] = start[b] + h[b];
+  ATC_CK(cudaMemcpyAsync(cursor.p, start, sizeof(unsigned long long) * 6, cudaMemcpyHostToDevice, s));
+  DevBuf<int64_t> list, list2;
+  ATC_TRY(list.alloc(g.m, s));
+  fox_scatter_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, fb, cursor.p, list.p);
+  ATC_CK(cudaGetLastError());
+  *launches += 3;
+  const int64_t* L = list.p;
+  if (t && t->fox_rearrange) {
+    ATC_TRY(list2.alloc(g.m, s));
+    for (int b = 0; b < 6; ++b) {
+      int64_t nb = (int64_t)h[b];
+      if (nb == 0) continue;
+      DevBuf<uint64_t> k1, k2;
+      ATC_TRY(k1.alloc(nb, s));
+      ATC_TRY(k2.alloc(nb, s));
+      fox_lenkey_kernel<<<grid_for(nb, 256), 256, 0, s>>>(g, list.p + start[b], nb, k1.p);
+      ATC_CK(cudaGetLastError());
+      uint64_t* ka = k1.p;
+      uint64_t* kb = k2.p;
+      ATC_TRY(sort_keys_u64(ka, kb, nb, 0, 63, s));
+      int64_t edges_per_block = 256 >> b;
+      int64_t nblk = nb / edges_per_block;
+      fox_deal_kernel<<<grid_for(nb, 256), 256, 0, s>>>(ka, list.p + start[b], nb, nblk, list2.p + start[b]);
+      ATC_CK(cudaGetLastError());
+      *launches += 2;
+    }
+    L = list2.p;
+  }
+  int sms = sm_count();
+  for (int b = 0; b < 6; ++b) {
+    int64_t nb = (int64_t)h[b];
+    if (nb == 0) continue;
+    const int64_t* Lb = L + start[b];
+    int64_t threads = nb << b;
+    unsigned grid = (unsigned)std::min<int64_t>((threads + 255) / 256, (int64_t)sms * 8);
+    switch (b) {
+      case 0: fox_kernel<1><<<grid, 256, 0, s>>>(g, Lb, nb, ctr); break;
+      case 1: fox_kernel<2><<<grid, 256, 0, s>>>(g, Lb, nb, ctr); break;
+      case 2: fox_kernel<4><<<grid, 256, 0, s>>>(g, Lb, nb, ctr); break;
+      case 3: fox_kernel<8><<<grid, 256, 0, s>>>(g, Lb, nb, ctr); break;
+      case 4: fox_kernel<16><<<grid, 256, 0, s>>>(g, Lb, nb, ctr); break;
+      default: fox_kernel<32><<<grid, 256, 0, s>>>(g, Lb, nb, ctr); break;
+    }
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  ATC_CK(cudaStreamSynchronize(s));  // `start` / `h` live on this frame
+  return ATC_OK;
+}
+
+static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
+                         int* launches) {
+  int nb = t && t->hu_blocks > 0 ? t->hu_blocks
+                                 : sm_count() * blocks_per_sm((const void*)hu_kernel, kHuWarps * 32, 0) * 4;
+  DevBuf<int64_t> work, prefix;
+  DevBuf<int32_t> start;
+  ATC_TRY(work.alloc(g.n + 1, s));
+  ATC_TRY(prefix.alloc(g.n + 1, s));
+  ATC_TRY(start.alloc(nb + 1, s));
+  hu_work_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, work.p);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaMemsetAsync(work.p + g.n, 0, sizeof(int64_t), s));
+  ATC_TRY(exclusive_scan_i64(work.p, prefix.p, g.n + 1, s));
+  int64_t total = 0;
+  ATC_CK(cudaMemcpyAsync(&total, prefix.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  hu_cut_kernel<<<(nb + 1 + 255) / 256, 256, 0, s>>>(prefix.p, g.n, total, nb, start.p);
+  ATC_CK(cudaGetLastError());
+  hu_kernel<<<nb, kHuWarps * 32, 0, s>>>(g, start.p, ctr);
+  ATC_CK(cudaGetLastError());
+  *launches += 4;
+  return ATC_OK;
+}
+
+static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
+                             int* launches) {
+  int cut = t && t->bisson_cutover > 0 ? t->bisson_cutover : 32;
+  if (cut > 64) cut = 64;
+  DevBuf<int32_t> hubs, smalls;
+  DevBuf<int> counts;
+  ATC_TRY(hubs.alloc(g.n, s));
+  ATC_TRY(smalls.alloc(g.n, s));
+  ATC_TRY(counts.alloc(2, s));
+  ATC_CK(cudaMemsetAsync(counts.p, 0, sizeof(int) * 2, s));
+  bisson_classify_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, cut, hubs.p, smalls.p, counts.p);
+  ATC_CK(cudaGetLastError());
+  int hc[2];
+  ATC_CK(cudaMemcpyAsync(hc, counts.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  *launches += 1;
+  if (hc[1]) {
+    int bps = blocks_per_sm((const void*)bisson_small_kernel<64>, kBiWarps * 32, 0);
+    unsigned grid = (unsigned)std::min<int64_t>((hc[1] + kBiWarps - 1) / kBiWarps, (int64_t)sm_count() * bps);
+    if (cut <= 32) bisson_small_kernel<32><<<grid, kBiWarps * 32, 0, s>>>(g, smalls.p, hc[1], ctr);
+    else bisson_small_kernel<64><<<grid, kBiWarps * 32, 0, s>>>(g, smalls.p, hc[1], ctr);
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  if (hc[0]) {
+    size_t smem = sizeof(uint32_t) * kBiBitmapWords;
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_hub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int bps = blocks_per_sm((const void*)bisson_hub_kernel, kBiWarps * 32, smem);
+    int grid = std::min(hc[0], sm_count() * bps);
+    int64_t gwords = (g.n + 31) / 32 + 1;
+    DevBuf<uint32_t> gbits;
+    ATC_TRY(gbits.alloc((size_t)gwords * grid, s));
+    ATC_CK(cudaMemsetAsync(gbits.p, 0, sizeof(uint32_t) * gwords * grid, s));
+    bisson_hub_kernel<<<grid, kBiWarps * 32, smem, s>>>(g, hubs.p, hc[0], gbits.p, gwords, ctr);
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  return ATC_OK;
+}
+
+}  // namespace atc
+
+using namespace atc;
+
+extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint64_t* count,
+                             atc_stats* stats, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
+  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  ATC_CHECK_ARG(kernel >= ATC_KERNEL_AUTO && kernel <= ATC_KERNEL_TRICORE, "unknown atc_kernel");
+  cudaStream_t s = as_stream(st);
+  *count = 0;
+  if (kernel == ATC_KERNEL_AUTO) kernel = ATC_KERNEL_BISSON;
+  CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+  int launches = 0;
+  EventTimer tm;
+  if (csr->m > 0) {
+    CsrView g{csr->offsets, csr->cols, pv->esrc, csr->n, csr->m};
+    unsigned long long* ctr = pv->counter;
+    tm.start(s);
+    ATC_CK(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
+    switch (kernel) {
+      case ATC_KERNEL_HU: ATC_TRY(run_hu(g, tuning, ctr, s, &launches)); break;
+      case ATC_KERNEL_BISSON: ATC_TRY(run_bisson(g, tuning, ctr, s, &launches)); break;
+      case ATC_KERNEL_FOX: ATC_TRY(run_fox(g, tuning, ctr, s, &launches)); break;
+      default: ATC_TRY(run_tricore(g, tuning, ctr, s, &launches)); break;
+    }
+    tm.stop(s);
+    unsigned long long h = 0;
+    ATC_CK(cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    *count = h;
+  }
+  if (stats) {
+    stats->kernel_ms = csr->m > 0 ? tm.ms() : 0.0f;
+    stats->total_ms = stats->kernel_ms;
+    stats->wedges = (uint64_t)csr->wedges;
+    stats->alg_bytes = 4ull * (uint64_t)(csr->n + 1) + 4ull * (uint64_t)csr->m + 4ull * (uint64_t)csr->wedges + 8ull;
+    stats->kernel_used = (int32_t)kernel;
+    stats->launches = launches;
+  }
+  return ATC_OK;
+}

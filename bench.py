@@ -1,0 +1,344 @@
+"""Benchmark: triangle-counting throughput (undirected edges per second) on one GB300.
+
+Workload (default): seeded R-MAT scale 24, edge factor 16 (a,b,c = .57,.19,.19), raw
+samples deduplicated on the device, A-order relabelling + A-direction orientation
+(the reference's "A-direction + A-order then each kernel" configuration).
+
+A step counts the triangles of the resident oriented CSR once with the headline kernel
+(AUTO).  `value` = undirected simple edges / device time of a step (CSR already in HBM;
+the 1+ GB CSR exceeds the 129 MB L2, so no flush is needed between steps).  `e2e` is the
+same metric through the public C ABI with host buffers: every step copies the raw
+int32 pairs from pinned host memory, builds the CSR (dedup, A-order, A-direction),
+counts and reads the count back.  Every kernel family is also timed ("kernels").
+
+--impl reference times the reference's CPU triangle count (the oracle restatement of
+OrgTriangleCount's scalar merge, all host threads) on a bounded vertex sample of the same
+graph and prints the same JSON line with "impl": "reference".
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--scale S] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "accelerating-tc_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "TC edges/s (1 GB300), HBM % of roofline; batched/learned vs plain, exact counts"
+UNIT = "edges/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--scale", type=int, default=24)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(a):
+    return {
+        "workload": "R-MAT scale %d edge factor %d (a,b,c=.57,.19,.19) seed %d; A-order + A-direction; int32 CSR"
+        % (a.scale, a.edge_factor, a.seed),
+        "scale": a.scale,
+        "edge_factor": a.edge_factor,
+        "seed": a.seed,
+        "direction": "A-direction",
+        "ordering": "A-order",
+        "l2": "CSR larger than L2 (129 MB); no flush between steps",
+    }
+
+
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_for(cfg, kernel_name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    rec = d.get("%s|scale%d" % (kernel_name, cfg["scale"]))
+    return rec.get("dram_bytes_per_launch") if rec else None
+
+
+# ---------------------------------------------------------------------------------------
+def cpu_baseline(g_lower_off, g_lower_cols, m_total, target_s):
+    """Times the oracle's scalar-merge triangle count on a strided vertex sample."""
+    import oracle
+    n = g_lower_off.size - 1
+    nthreads = os.cpu_count() or 1
+    stride = max(1, n // 2048)
+    t0 = time.perf_counter()
+    _, e = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride, 0, nthreads)
+    dt = time.perf_counter() - t0
+    # grow the sample to about target_s seconds
+    if dt > 0:
+        stride = max(1, int(stride * dt / max(target_s, 0.1)))
+    t0 = time.perf_counter()
+    cnt, e = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride, 0, nthreads)
+    dt = time.perf_counter() - t0
+    return {"value": e / dt if dt > 0 else None, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "every %d-th vertex u (%d of %d) with all its lower-neighbour edges (%d edges of %d); %.1f s"
+            % (stride, (n + stride - 1) // stride, n, e, m_total, dt),
+            "machine": os.uname().machine}
+
+
+# ---------------------------------------------------------------------------------------
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import atc
+    import oracle
+    t0 = time.perf_counter()
+    raw = atc.gen_rmat(a.scale, a.edge_factor, a.seed)
+    loff, lcols = oracle.lower_csr(raw)
+    m = int(loff[-1])
+    setup = time.perf_counter() - t0
+    nthreads = os.cpu_count() or 1
+    n = loff.size - 1
+    # stride so one step is about a.cpu_seconds / (steps + warmup) of work
+    steps, warm = max(1, a.steps), max(0, a.warmup)
+    per_step = max(0.5, a.cpu_seconds * 2 / (steps + warm))
+    stride = max(1, n // 1024)
+    t1 = time.perf_counter()
+    oracle.tc_count_lower_sample(loff, lcols, stride, 0, nthreads)
+    dt = time.perf_counter() - t1
+    stride = max(1, int(stride * dt / per_step)) if dt > 0 else stride
+    for i in range(warm):
+        oracle.tc_count_lower_sample(loff, lcols, stride, i % stride, nthreads)
+    edges, secs = 0, 0.0
+    for i in range(steps):
+        t1 = time.perf_counter()
+        _, e = oracle.tc_count_lower_sample(loff, lcols, stride, (warm + i) % stride, nthreads)
+        secs += time.perf_counter() - t1
+        edges += e
+    v = edges / secs if secs > 0 else None
+    cfg = workload_config(a)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": secs / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded R-MAT)", "config": cfg,
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "per step every %d-th vertex u with all its smaller-neighbour edges "
+                                   "(OrgTriangleCount scalar merge, other_order/set_operation.cpp:129-144); "
+                                   "graph build %.1f s untimed" % (stride, setup)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "graph": {"n": int(n), "m": m},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
+def run_ours(a):
+    import torch
+    import atc
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    atc.init(local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    # ---- input: raw R-MAT samples generated on the device (replicas: same graph per rank)
+    nraw = a.edge_factor << a.scale
+    raw = torch.empty((nraw, 2), dtype=torch.int32, device="cuda")
+    rc = atc.lib().atc_gen_rmat_device(a.scale, a.edge_factor, *atc.GRAPH500, a.seed, raw.data_ptr(), sp)
+    assert rc == 0, atc.lib().atc_last_error()
+    host_raw = torch.empty((nraw, 2), dtype=torch.int32, pin_memory=True)
+    host_raw.copy_(raw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    csr = atc.pretc_device(raw.data_ptr(), nraw, atc.Dir.ADIRECTION, atc.Order.AORDER, stream=sp)
+    pretc_s = time.perf_counter() - t0
+    del raw
+    torch.cuda.empty_cache()
+    m = csr.m
+
+    # ---- every kernel family once (count check + per-kernel time)
+    kernels = {}
+    counts = {}
+    for k in (atc.Kernel.HU, atc.Kernel.BISSON, atc.Kernel.FOX, atc.Kernel.TRICORE):
+        atc.tc(csr, k, stream=sp)
+        c, st = atc.tc(csr, k, stream=sp)
+        counts[k.name] = c
+        kernels[k.name.lower()] = {"ms": st.kernel_ms, "edges_per_s": m / (st.kernel_ms * 1e-3) if st.kernel_ms else None,
+                                   "hbm_frac_alg": st.alg_bytes / (st.kernel_ms * 1e-3) / 1e9 / measured_peak()[0]
+                                   if st.kernel_ms else None}
+    assert len(set(counts.values())) == 1, counts
+    best = min(kernels, key=lambda k: kernels[k]["ms"])
+
+    # ---- value: K steps of the headline kernel on the resident CSR
+    head = atc.Kernel.AUTO
+    for _ in range(max(3, a.warmup)):
+        atc.tc(csr, head, stream=sp)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kms = []
+    launches = 0
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            c, st = atc.tc(csr, head, stream=sp)
+            kms.append(st.kernel_ms)
+            launches += st.launches
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    total_ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / a.steps
+    value = m * a.steps * world / (total_ms * 1e-3)
+    head_count = c
+    assert head_count == counts["HU"]
+    alg = st.alg_bytes
+    kern_ms = statistics.mean(kms)
+    peak, peak_kind = measured_peak()
+    achieved = alg / (kern_ms * 1e-3) / 1e9
+
+    # ---- e2e: public C ABI from pinned host buffers
+    e2e_ms = []
+    for i in range(a.e2e_steps + 1):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w0 = time.perf_counter()
+        c2 = atc.pretc_host_ptr(host_raw.data_ptr(), nraw, atc.Dir.ADIRECTION, atc.Order.AORDER, stream=sp)
+        cnt, _ = atc.tc(c2, head, stream=sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - w0) * 1e3
+        c2.free()
+        assert cnt == head_count
+        if i > 0:  # first pass warms the allocator pools
+            e2e_ms.append(max(wall, e0.elapsed_time(e1)))
+    e2e_step = statistics.mean(e2e_ms)
+    e2e_value = m * world / (e2e_step * 1e-3)
+
+    cfg = workload_config(a)
+    kname = {1: "hu", 2: "bisson", 3: "fox", 4: "tricore"}.get(st.kernel_used, "auto")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded R-MAT generated on the device)", "config": cfg,
+        "graph": {"n": csr.n, "m": m, "wedges": csr.wedges, "max_outdeg": csr.max_outdeg, "triangles": head_count},
+        "headline_kernel": kname, "fastest_kernel": best, "kernels": kernels,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic_for(cfg, kname), "peak_source": peak_kind,
+                     "alg_bytes_per_launch": alg, "kernel_ms": kern_ms},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nraw * 8, "d2h_bytes_per_step": 8,
+                "ms_per_step": e2e_step, "steps": len(e2e_ms)},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "pretc_s_first_call": pretc_s,
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        import oracle
+        off, cols = oracle.lower_csr(host_raw.numpy())
+        line["cpu_baseline"] = cpu_baseline(off, cols, m, a.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -260,29 +260,58 @@ uint64_t orc_tc_count(const int32_t* pairs, uint64_t np, int nthreads) {
   return r;
 }
 
-// Same count restricted to "top" vertices u with u % stride == phase: the bounded
-// sample the CPU baseline times.  Returns the count; *edges_out receives Σ|N-(u)|
-// over the sampled u (the edges whose triangles were counted).
-uint64_t orc_tc_count_sample(const int64_t* off, const int32_t* nbr, int64_t n,
-                             int64_t stride, int64_t phase, int nthreads, int64_t* edges_out) {
-  // `off`/`nbr` are the symmetric simple CSR built by orc_symmetric_csr.
-  int64_t nsamp = (n - phase + stride - 1) / stride;
-  if (nsamp < 0) nsamp = 0;
-  auto low = [&](int64_t v) {
-    const int32_t* b = nbr + off[v];
-    const int32_t* e = nbr + off[v + 1];
-    return (int64_t)(std::lower_bound(b, e, (int32_t)v) - b);
-  };
+// Lower CSR of the simple graph: for every vertex u the sorted, duplicate-free list of
+// its smaller neighbours (the N-(u) lists of OrgTriangleCount::build,
+// org_triangle_count.cpp:15-50).  Threaded.  Call with off == nullptr to size it.
+void orc_lower_csr(const int32_t* p, uint64_t np, int64_t* off, int32_t* nbr, int64_t* n_out, int64_t* nnz_out,
+                   int nthreads) {
+  int64_t n = max_id(p, np) + 1;
+  std::vector<int64_t> cnt(n + 1, 0);
+  for (uint64_t i = 0; i < np; ++i) {
+    int32_t a = p[2 * i], b = p[2 * i + 1];
+    if (a != b) cnt[std::max(a, b) + 1]++;
+  }
+  for (int64_t v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
+  std::vector<int32_t> tmp(cnt[n]);
+  std::vector<int64_t> cur(cnt.begin(), cnt.end() - 1);
+  for (uint64_t i = 0; i < np; ++i) {
+    int32_t a = p[2 * i], b = p[2 * i + 1];
+    if (a != b) tmp[cur[std::max(a, b)]++] = std::min(a, b);
+  }
+  std::vector<int64_t> len(n, 0);
+  parallel_for(n, nthreads, 4096, [&](int64_t v, int) {
+    auto b = tmp.begin() + cnt[v], e = tmp.begin() + cnt[v + 1];
+    std::sort(b, e);
+    len[v] = std::unique(b, e) - b;
+  });
+  *n_out = n;
+  int64_t total = 0;
+  for (int64_t v = 0; v < n; ++v) total += len[v];
+  *nnz_out = total;
+  if (!off) return;
+  off[0] = 0;
+  for (int64_t v = 0; v < n; ++v) off[v + 1] = off[v] + len[v];
+  parallel_for(n, nthreads, 4096, [&](int64_t v, int) {
+    std::memcpy(nbr + off[v], tmp.data() + cnt[v], sizeof(int32_t) * len[v]);
+  });
+}
+
+// Triangle count over a lower CSR restricted to the vertices u = phase + i*stride (the
+// bounded sample the CPU baseline times): Σ_u Σ_{v∈N-(u)} |N-(u) ∩ N-(v)| with the
+// scalar merge of set_operation.cpp:129-144.  *edges_out = Σ|N-(u)| over the sample.
+uint64_t orc_tc_count_lower_sample(const int64_t* off, const int32_t* nbr, int64_t n, int64_t stride,
+                                   int64_t phase, int nthreads, int64_t* edges_out) {
+  int64_t nsamp = phase < n ? (n - phase + stride - 1) / stride : 0;
   std::vector<uint64_t> part(std::max(1, nthreads), 0);
   std::vector<int64_t> epart(std::max(1, nthreads), 0);
-  parallel_for(nsamp, nthreads, 64, [&](int64_t i, int t) {
+  parallel_for(nsamp, nthreads, 16, [&](int64_t i, int t) {
     int64_t u = phase + i * stride;
     const int32_t* a = nbr + off[u];
-    int64_t lu = low(u);
+    int64_t lu = off[u + 1] - off[u];
     uint64_t s = 0;
     for (int64_t k = 0; k < lu; ++k) {
       int32_t v = a[k];
-      s += intersect_count(a, lu, nbr + off[v], low(v));
+      s += intersect_count(a, lu, nbr + off[v], off[v + 1] - off[v]);
     }
     part[t] += s;
     epart[t] += lu;

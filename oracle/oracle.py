@@ -31,8 +31,10 @@ def lib():
         L.orc_simple_stats.argtypes = [_P, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.orc_tc_count.restype = C.c_uint64
         L.orc_tc_count.argtypes = [_P, C.c_uint64, C.c_int]
-        L.orc_tc_count_sample.restype = C.c_uint64
-        L.orc_tc_count_sample.argtypes = [_P, _P, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_int64)]
+        L.orc_tc_count_lower_sample.restype = C.c_uint64
+        L.orc_tc_count_lower_sample.argtypes = [_P, _P, C.c_int64, C.c_int64, C.c_int64, C.c_int,
+                                                C.POINTER(C.c_int64)]
+        L.orc_lower_csr.argtypes = [_P, C.c_uint64, _P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int]
         L.orc_symmetric_csr.argtypes = [_P, C.c_uint64, _P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.orc_adirection.restype = C.c_int64
         L.orc_adirection.argtypes = [_P, C.c_uint64, _P, _P]
@@ -85,10 +87,23 @@ def symmetric_csr(pairs):
     return off, nbr
 
 
-def tc_count_sample(off, nbr, stride, phase=0, nthreads=None):
+def lower_csr(pairs, nthreads=None):
+    """Per-vertex sorted lists of smaller neighbours of the simple graph (int64 offsets)."""
+    p = _pairs(pairs)
+    n, nnz = C.c_int64(0), C.c_int64(0)
+    nt = nthreads or nthreads_default()
+    lib().orc_lower_csr(_ptr(p), p.shape[0], None, None, C.byref(n), C.byref(nnz), nt)
+    off = np.empty(n.value + 1, dtype=np.int64)
+    nbr = np.empty(max(nnz.value, 1), dtype=np.int32)
+    lib().orc_lower_csr(_ptr(p), p.shape[0], _ptr(off), _ptr(nbr), C.byref(n), C.byref(nnz), nt)
+    return off, nbr
+
+
+def tc_count_lower_sample(off, nbr, stride, phase=0, nthreads=None):
+    """(triangles, edges) over the vertices phase, phase+stride, ... of a lower CSR."""
     e = C.c_int64(0)
-    c = lib().orc_tc_count_sample(_ptr(off), _ptr(nbr), len(off) - 1, stride, phase,
-                                  nthreads or nthreads_default(), C.byref(e))
+    c = lib().orc_tc_count_lower_sample(_ptr(off), _ptr(nbr), len(off) - 1, stride, phase,
+                                        nthreads or nthreads_default(), C.byref(e))
     return c, e.value
 
 

@@ -1,0 +1,66 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol the header
+declares, rejects bad arguments before touching the device, and its host-side
+generators are deterministic."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import atc
+
+
+def test_exports_every_declared_symbol():
+    lib = atc.lib()
+    names = atc.header_symbols()
+    assert len(names) >= 17
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version_and_status_strings():
+    assert "sm_103a" in atc.version()
+    lib = atc.lib()
+    for s in atc.Status:
+        assert lib.atc_status_string(int(s))
+
+
+def test_rmat_host_deterministic():
+    a = atc.gen_rmat(10, 4, seed=9, nthreads=1)
+    b = atc.gen_rmat(10, 4, seed=9, nthreads=7)
+    assert np.array_equal(a, b)
+    c = atc.gen_rmat(10, 4, seed=10)
+    assert not np.array_equal(a, c)
+    assert a.min() >= 0 and a.max() < 1024
+
+
+def test_rmat_skew():
+    # quadrant a = 0.57 puts most mass on low ids
+    a = atc.gen_rmat(12, 16, seed=1)
+    assert (a < 2048).mean() > 0.7
+
+
+def test_simplify():
+    p = np.array([[1, 2], [2, 1], [3, 3], [0, 5], [5, 0], [1, 2]], dtype=np.int32)
+    assert atc.simplify(p, symmetric=False).tolist() == [[0, 5], [1, 2]]
+    assert atc.simplify(p, symmetric=True).tolist() == [[0, 5], [1, 2], [2, 1], [5, 0]]
+
+
+def test_argument_checks_without_gpu():
+    lib = atc.lib()
+    st = atc.CSRStruct()
+    # NULL pairs with a non-zero count is rejected before any device work
+    assert lib.atc_pretc(None, 5, 0, 0, None, C.byref(st), None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_pretc(None, 0, 9, 0, None, C.byref(st), None, None) in (atc.Status.ERR_INVALID,)
+    cnt = C.c_uint64()
+    assert lib.atc_tc(None, 0, None, C.byref(cnt), None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_kcl(C.byref(st), 2, C.byref(cnt), None, None) == atc.Status.ERR_INVALID
+    buf = np.zeros(4, dtype=np.int32)
+    assert lib.atc_gen_rmat_host(40, 1, 570000, 190000, 190000, 1, buf.ctypes.data, 1) == atc.Status.ERR_INVALID
+    assert lib.atc_gen_rmat_host(4, 1, 900000, 190000, 190000, 1, buf.ctypes.data, 1) == atc.Status.ERR_INVALID
+    with pytest.raises(atc.ATCError):
+        atc.simplify(np.array([[-1, 2]], dtype=np.int32))
+
+
+def test_csr_free_is_idempotent():
+    st = atc.CSRStruct()
+    assert atc.lib().atc_csr_free(C.byref(st)) == 0

@@ -1,0 +1,297 @@
+"""GPU parity: libatc (through its C ABI) against the reference programs' golden outputs
+and the CPU oracle, on the same seeded inputs.
+
+Integer results must be identical: triangle / k-clique counts, the A-direction
+orientation, the A-order permutation and its output files, the CSR.  The cost figures
+must print identically to the reference tools.
+"""
+import hashlib
+from math import comb
+
+import numpy as np
+import pytest
+
+import atc
+import oracle
+from conftest import golden_input, load_golden
+
+pytestmark = pytest.mark.gpu
+
+CASES = sorted(load_golden()["cases"])
+KERNELS = [atc.Kernel.HU, atc.Kernel.BISSON, atc.Kernel.FOX, atc.Kernel.TRICORE]
+DIRS = [atc.Dir.ID, atc.Dir.DEGREE, atc.Dir.DEGREE_LOWID, atc.Dir.ADIRECTION]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.int32).tobytes()).hexdigest()
+
+
+def fmt6(x):
+    return "%g" % np.float32(x)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _init(gpu_ready):
+    yield
+
+
+# ---- orientation / ordering: bit-exact against the reference programs -----------------
+@pytest.mark.parametrize("name", CASES)
+def test_adirection_matches_reference(golden, name):
+    c = golden["cases"][name]
+    got, prio = atc.adirection(golden_input(c), want_prio=True)
+    assert got.shape[0] == c["adirection"]["count"]
+    assert sha(got) == c["adirection"]["sha256"]
+    _, oprio = oracle.adirection(golden_input(c), want_prio=True)
+    assert np.array_equal(prio, oprio)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("which", ["aorder", "aorder_raw"])
+def test_aorder_matches_reference(golden, name, which):
+    c = golden["cases"][name]
+    g = golden_input(c)
+    src = oracle.adirection(g) if which == "aorder" else g
+    rec = c[which]
+    if rec.get("unsupported"):
+        with pytest.raises(atc.ATCError) as ei:
+            atc.aorder(src)
+        assert ei.value.status == atc.Status.ERR_UNSUPPORTED
+        return
+    lookup, normal, reordered = atc.aorder(src)
+    assert sha(normal) == rec["normal"]["sha256"]
+    assert sha(reordered) == rec["reordered"]["sha256"]
+    olookup, _, _ = oracle.aorder(src)
+    assert np.array_equal(lookup, olookup)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_costs_match_reference(golden, name):
+    c = golden["cases"][name]
+    lp = oracle.adirection(golden_input(c))
+    for k, printed in c["costfunc"].items():
+        assert [fmt6(x) for x in atc.costfunc(lp, int(k))] == printed
+    assert [fmt6(x) for x in atc.verification(lp)] == c["verification"]
+
+
+# ---- counts ------------------------------------------------------------------------------
+@pytest.mark.parametrize("name", CASES)
+def test_counts_all_kernels_and_directions(golden, name):
+    c = golden["cases"][name]
+    g = golden_input(c)
+    want = oracle.tc_count(g)
+    if "triangles" in c:
+        assert want == c["triangles"]
+    for d in DIRS:
+        csr = atc.pretc(g, d)
+        for k in KERNELS:
+            got, st = atc.tc(csr, k)
+            assert got == want, (d.name, k.name)
+            assert st.kernel_used == int(k)
+        csr.free()
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if n.startswith("rmat_s1")])
+def test_counts_with_aorder_and_prune(golden, name):
+    g = golden_input(golden["cases"][name])
+    want = oracle.tc_count(g)
+    for d in DIRS:
+        for prune in (0, 1):
+            csr = atc.pretc(g, d, atc.Order.AORDER, tuning={"prune_deg1": prune}, want_perm=True)
+            assert np.array_equal(np.sort(csr.perm), np.arange(csr.perm.size))
+            for k in KERNELS:
+                assert atc.tc(csr, k)[0] == want, (d.name, prune, k.name)
+
+
+def test_tuning_knobs_do_not_change_counts():
+    g = atc.rmat_graph(12, 16, 3)
+    want = oracle.tc_count(g)
+    csr = atc.pretc(g, atc.Dir.ID)  # id orientation: long lists, hubs
+    for t in ({"bisson_cutover": 8}, {"bisson_cutover": 64}, {"fox_rearrange": 1}, {"fox_work_per_thread": 4},
+              {"hu_blocks": 7}, {"tricore_blocks": 3}, {"hu_blocks": 2000}):
+        for k in KERNELS:
+            assert atc.tc(csr, k, tuning=t)[0] == want, (t, k.name)
+
+
+# ---- CSR layout ----------------------------------------------------------------------------
+def test_pretc_degree_pruned_equals_hu_csr():
+    # Hu's preTC on a once-per-edge list (what A-direction-seri writes)
+    g = oracle.adirection(atc.rmat_graph(12, 16, 7))
+    off, cols = atc.pretc(g, atc.Dir.DEGREE, tuning={"prune_deg1": 1}).to_host()
+    hoff, hcols = oracle.hu_csr(g)
+    assert np.array_equal(off, hoff.astype(np.int64))
+    assert np.array_equal(cols, hcols)
+
+
+@pytest.mark.parametrize("d", DIRS)
+def test_csr_invariants_and_wedges(d):
+    g = atc.rmat_graph(11, 16, 5)
+    n, m = oracle.simple_stats(g)
+    csr = atc.pretc(g, d)
+    off, cols = csr.to_host()
+    assert csr.n == n and csr.m == m
+    assert off[0] == 0 and off[-1] == m
+    for u in range(n):
+        lst = cols[off[u]:off[u + 1]]
+        assert np.all(np.diff(lst) > 0)
+    assert csr.wedges == oracle.wedges(off, cols)
+    assert csr.max_outdeg == int(np.diff(off).max())
+
+
+def test_adirection_csr_is_reference_orientation():
+    g = atc.rmat_graph(12, 16, 7)
+    off, cols = atc.pretc(g, atc.Dir.ADIRECTION).to_host()
+    src = np.repeat(np.arange(off.size - 1), np.diff(off)).astype(np.int32)
+    lp = np.stack([src, cols], 1)
+    assert np.array_equal(lp, oracle.adirection(g))
+
+
+def test_aorder_perm_in_pipeline_matches_reference_program():
+    # pipeline A-order = the A-order program run on A-direction-seri's output
+    g = atc.rmat_graph(12, 16, 7)
+    csr = atc.pretc(g, atc.Dir.DEGREE, atc.Order.AORDER, want_perm=True)
+    lookup, _, _ = oracle.aorder(oracle.adirection(g))
+    assert np.array_equal(csr.perm[: lookup.size], lookup)
+    assert np.array_equal(csr.perm[lookup.size:], np.arange(lookup.size, csr.perm.size))
+
+
+# ---- k-cliques --------------------------------------------------------------------------------
+@pytest.mark.parametrize("k", [3, 4, 5, 6, 7])
+def test_kcl_matches_oracle(k):
+    g = atc.rmat_graph(10, 16, 1)
+    want = oracle.kclique(g, k)
+    for d in (atc.Dir.ADIRECTION, atc.Dir.DEGREE, atc.Dir.ID):
+        csr = atc.pretc(g, d)
+        assert atc.kcl(csr, k)[0] == want, (d.name, k)
+
+
+def test_kcl_complete_graphs():
+    for n in (5, 9, 17, 40):
+        kn = np.array([(a, b) for a in range(n) for b in range(n) if a != b], dtype=np.int32)
+        csr = atc.pretc(kn, atc.Dir.ADIRECTION)
+        for k in range(3, 9):
+            assert atc.kcl(csr, k)[0] == comb(n, k), (n, k)
+
+
+def test_kcl_three_equals_triangles():
+    g = atc.rmat_graph(13, 16, 2)
+    csr = atc.pretc(g, atc.Dir.ADIRECTION)
+    assert atc.kcl(csr, 3)[0] == atc.tc(csr, atc.Kernel.AUTO)[0] == oracle.tc_count(g)
+
+
+# ---- edge cases --------------------------------------------------------------------------------
+def test_empty_and_degenerate_inputs():
+    empty = np.zeros((0, 2), dtype=np.int32)
+    for k in KERNELS:
+        csr = atc.pretc(empty, atc.Dir.DEGREE)
+        assert csr.n == 0 and csr.m == 0
+        assert atc.tc(csr, k)[0] == 0
+    loops = np.array([[3, 3], [7, 7]], dtype=np.int32)
+    csr = atc.pretc(loops, atc.Dir.ADIRECTION)
+    assert csr.m == 0 and csr.n == 8 and atc.tc(csr)[0] == 0
+    one = np.array([[0, 1]], dtype=np.int32)
+    for d in DIRS:
+        csr = atc.pretc(one, d)
+        assert csr.m == 1 and atc.tc(csr)[0] == 0
+    tri_sparse = np.array([[5, 2_000_000], [2_000_000, 77], [77, 5]], dtype=np.int32)
+    for d in DIRS:
+        for k in KERNELS:
+            assert atc.tc(atc.pretc(tri_sparse, d), k)[0] == 1
+
+
+def test_negative_id_rejected():
+    with pytest.raises(atc.ATCError) as ei:
+        atc.pretc(np.array([[0, 1], [-4, 2]], dtype=np.int32))
+    assert ei.value.status == atc.Status.ERR_INVALID
+
+
+def test_duplicates_and_reverse_pairs_counted_once():
+    tri = np.array([[0, 1], [1, 2], [2, 0]], dtype=np.int32)
+    noisy = np.concatenate([tri, tri[:, ::-1], tri, [[1, 1]]]).astype(np.int32)
+    for d in DIRS:
+        for k in KERNELS:
+            assert atc.tc(atc.pretc(noisy, d), k)[0] == 1
+
+
+def test_hub_heavy_graph():
+    # a star of 3000 leaves plus a clique among 60 of them: long lists on both sides
+    hub = [(0, i) for i in range(1, 3001)]
+    cl = [(a, b) for a in range(1, 61) for b in range(a + 1, 61)]
+    g = np.array(hub + cl, dtype=np.int32)
+    want = oracle.tc_count(g)
+    assert want == comb(60, 2) + comb(60, 3)
+    for d in DIRS:
+        csr = atc.pretc(g, d)
+        for k in KERNELS:
+            assert atc.tc(csr, k)[0] == want, (d.name, k.name)
+        for t in ({"bisson_cutover": 1},):
+            assert atc.tc(csr, atc.Kernel.BISSON, tuning=t)[0] == want
+
+
+def test_device_generator_matches_host():
+    import torch
+    n = 16 << 12
+    buf = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+    rc = atc.lib().atc_gen_rmat_device(12, 16, 570000, 190000, 190000, 5, buf.data_ptr(), None)
+    assert rc == 0
+    assert np.array_equal(buf.cpu().numpy(), atc.gen_rmat(12, 16, 5))
+
+
+def test_pretc_device_input_matches_host_input():
+    import torch
+    g = atc.rmat_graph(11, 16, 4)
+    d = torch.from_numpy(g).cuda()
+    c1 = atc.pretc_device(d.data_ptr(), g.shape[0], atc.Dir.ADIRECTION)
+    c2 = atc.pretc(g, atc.Dir.ADIRECTION)
+    o1, k1 = c1.to_host()
+    o2, k2 = c2.to_host()
+    assert np.array_equal(o1, o2) and np.array_equal(k1, k2)
+
+
+def test_rmat_s16_config_counts(golden):
+    # the reference's CPU-runnable configuration: R-MAT s16 ef16, A-direction, Hu-style
+    c = golden["cases"]["rmat_s16_ef16_seed1"]
+    g = golden_input(c)
+    csr = atc.pretc(g, atc.Dir.ADIRECTION)
+    for k in KERNELS:
+        assert atc.tc(csr, k)[0] == c["triangles"]
+
+
+@pytest.mark.parametrize("scale", [18, 20])
+def test_larger_graphs_all_kernels_agree_with_oracle(scale):
+    g = atc.rmat_graph(scale, 16, 11)
+    want = oracle.tc_count(g)
+    for d, o in ((atc.Dir.ADIRECTION, atc.Order.AORDER), (atc.Dir.DEGREE, atc.Order.NONE), (atc.Dir.ID, atc.Order.NONE)):
+        csr = atc.pretc(g, d, o)
+        for k in KERNELS:
+            assert atc.tc(csr, k)[0] == want, (scale, d.name, k.name)
+
+
+def test_cli_dropins(tmp_path):
+    import os
+    import subprocess
+    g = atc.rmat_graph(10, 16, 1)
+    want = oracle.tc_count(g)
+    e = tmp_path / "E.bin"
+    g.tofile(e)
+    u64 = (g[:, 0].astype(np.uint64) << np.uint64(32)) | g[:, 1].astype(np.uint32).astype(np.uint64)
+    (tmp_path / "E.u64").write_bytes(u64.tobytes())
+    bindir = os.path.join(os.path.dirname(atc.LIB_PATH), "bin")
+    line = "There are %d triangles in the input graph." % want
+    for cmd in (["tc_hu", "-f", str(e)], ["tc_bisson", "-f", str(e), "0"], ["tc_fox", "-f", str(e), "1"],
+                ["tric_gpu", "-f", str(tmp_path / "E.u64")]):
+        r = subprocess.run([os.path.join(bindir, cmd[0])] + cmd[1:], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        assert line in r.stdout
+    r = subprocess.run([os.path.join(bindir, "a_direction_seri"), str(e)], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lp = np.fromfile(tmp_path / "lpBasedGraph.bin", dtype=np.int32).reshape(-1, 2)
+    assert np.array_equal(lp, oracle.adirection(g))
+    r = subprocess.run([os.path.join(bindir, "a_order"), str(tmp_path / "lpBasedGraph.bin")], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, normal, reordered = oracle.aorder(lp)
+    assert np.array_equal(np.fromfile(tmp_path / "reordered", dtype=np.int32).reshape(-1, 2), reordered)
+    r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout
