@@ -79,6 +79,7 @@ class CSRStruct(C.Structure):
         ("order", C.c_int32),
         ("pruned", C.c_int32),
         ("max_outdeg", C.c_int32),
+        ("wedges_min", C.c_int64),
         ("priv", C.c_void_p),
     ]
 
@@ -89,6 +90,7 @@ class StatsStruct(C.Structure):
         ("total_ms", C.c_float),
         ("alg_bytes", C.c_uint64),
         ("wedges", C.c_uint64),
+        ("alg_bytes_min", C.c_uint64),
         ("kernel_used", C.c_int32),
         ("launches", C.c_int32),
     ]
@@ -100,6 +102,7 @@ class Stats:
     total_ms: float
     alg_bytes: int
     wedges: int
+    alg_bytes_min: int
     kernel_used: int
     launches: int
 
@@ -217,6 +220,10 @@ class CSR:
         return self._st.wedges
 
     @property
+    def wedges_min(self):
+        return self._st.wedges_min
+
+    @property
     def max_outdeg(self):
         return self._st.max_outdeg
 
@@ -281,7 +288,7 @@ def pretc_device(pairs_dev_ptr, n_pairs, dir=Dir.DEGREE, order=Order.NONE, tunin
 
 
 def _stats(s: StatsStruct):
-    return Stats(s.kernel_ms, s.total_ms, s.alg_bytes, s.wedges, s.kernel_used, s.launches)
+    return Stats(s.kernel_ms, s.total_ms, s.alg_bytes, s.wedges, s.alg_bytes_min, s.kernel_used, s.launches)
 
 
 def tc(csr: CSR, kernel=Kernel.AUTO, tuning=None, stream=None):

@@ -159,6 +159,7 @@ extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, a
     stats->total_ms = stats->kernel_ms;
     stats->alg_bytes = h[1];
     stats->wedges = (uint64_t)csr->wedges;
+    stats->alg_bytes_min = h[1];
     stats->kernel_used = 0;
     stats->launches = launches;
   }

@@ -158,6 +158,21 @@ __global__ void wedge_kernel(const int64_t* off, const int32_t* indeg, int64_t n
   }
 }
 
+// sum over edges of min(outdeg(u), outdeg(v)): the elements a shorter-list-probing
+// kernel must stream.
+__global__ void wedge_min_kernel(const int64_t* off, const int32_t* cols, const int32_t* esrc, int64_t m,
+                                 unsigned long long* out) {
+  unsigned long long s = 0;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    int32_t u = esrc[i], v = cols[i];
+    int64_t du = off[u + 1] - off[u], dv = off[v + 1] - off[v];
+    s += (unsigned long long)(du < dv ? du : dv);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
 __global__ void keep_kernel(const int32_t* deg, const int32_t* perm, int64_t n, int32_t* keep) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
@@ -349,8 +364,9 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   ATC_CK(cudaMemsetAsync(counter.p, 0, sizeof(unsigned long long) * 4, s));
   if (m) indeg_kernel<<<grid_for(m, 256), 256, 0, s>>>(cols.p, m, indeg.p);
   if (n) wedge_kernel<<<grid_for(n, 256), 256, 0, s>>>(off.p, indeg.p, n, counter.p, (int*)(counter.p + 1));
+  if (m) wedge_min_kernel<<<grid_for(m, 256), 256, 0, s>>>(off.p, cols.p, esrc.p, m, counter.p + 2);
   ATC_CK(cudaGetLastError());
-  unsigned long long hw[2] = {0, 0};
+  unsigned long long hw[3] = {0, 0, 0};
   ATC_CK(cudaMemcpyAsync(hw, counter.p, sizeof(hw), cudaMemcpyDeviceToHost, s));
   if (perm_out && order == ATC_ORDER_AORDER && n_in)
     ATC_CK(cudaMemcpyAsync(perm_out, perm.p, sizeof(int32_t) * n_in, cudaMemcpyDeviceToHost, s));
@@ -375,6 +391,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   out->order = (int32_t)order;
   out->pruned = prune ? 1 : 0;
   out->max_outdeg = (int32_t)(hw[1] & 0xffffffffu);
+  out->wedges_min = (int64_t)hw[2];
   out->priv = pv;
   return ATC_OK;
 }

@@ -267,82 +267,239 @@ __global__ void __launch_bounds__(kHuWarps * 32) hu_kernel(CsrView g, const int3
 }
 
 // ============================== Bisson-style =======================================
-constexpr int kBiWarps = 8;
-constexpr int kBiBitmapWords = 16384;  // 64 KB shared bitmap = 524288 ids
+// The reference keeps a bitmap of N+(u) for rows longer than 32 and streams every N+(v),
+// v in N+(u), through it (Bisson/tc.cu:36-62): one bit test per directed wedge, W tests
+// in all.  Here every edge {u, v} is handed to its endpoint h with the longer list; N+(h)
+// becomes a set in shared memory (hash table, or bitmap over [min, max] of the list) and
+// the shorter list of the partner is streamed through it.  That tests
+// sum_edges min(d+u, d+v) elements instead of W, with one shared-memory probe each.
+//   light groups (d+h <= kLightMax): a warp per chunk of partners, N+(h) staged in the
+//     warp's shared slot and binary-searched (the reference's <=32 branch, :63-87);
+//   heavy groups: a CTA per chunk of partners, N+(h) as a hash table (d+h <= kHashMax)
+//     or a bitmap (span < kTabWords*32), else binary search in global memory.
+// Chunks are taken from a device work counter (one atomicAdd per chunk; no waiting).
+constexpr int kBgWarps = 8;
+constexpr int kLightMax = 64;
+constexpr int kLightChunk = 256;
+constexpr int kHeavyChunk = 2048;
+constexpr int kTabWords = 16384;   // 64 KB: hash slots or bitmap words
+constexpr int kHashMax = kTabWords / 4;  // load factor <= 1/4
 
-__global__ void bisson_classify_kernel(CsrView g, int cutover, int32_t* hubs, int32_t* smalls, int* counts) {
+struct GroupItem {
+  int32_t h;
+  int32_t mode;  // heavy: 0 hash, 1 bitmap, 2 global search
+  int64_t b, e;  // partner range in the grouped list
+};
+
+__device__ __forceinline__ bool longer_is_u(int32_t u, int32_t v, int64_t du, int64_t dv) {
+  return du > dv || (du == dv && u < v);
+}
+
+// Pass 1: partners per group, with warp-aggregated atomics (edges of one source are
+// contiguous, so runs of one h are common).
+__global__ void group_count_kernel(CsrView g, int32_t* cnt) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < g.n; u += stride) {
-    int64_t d = g.off[u + 1] - g.off[u];
-    if (d == 0) continue;
-    if (d > cutover) hubs[atomicAdd(&counts[0], 1)] = (int32_t)u;
-    else smalls[atomicAdd(&counts[1], 1)] = (int32_t)u;
+  int64_t m_pad = (g.m + 31) & ~31ll;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
+    int32_t h = -1;
+    if (e < g.m) {
+      int32_t u = g.esrc[e], v = g.cols[e];
+      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      if (du > 0 && dv > 0) h = longer_is_u(u, v, du, dv) ? u : v;
+    }
+    unsigned same = __match_any_sync(0xffffffffu, h);
+    int lead = __ffs(same) - 1;
+    if (h >= 0 && (int)(threadIdx.x & 31) == lead) atomicAdd(&cnt[h], __popc(same));
   }
 }
 
-// Rows of out-degree <= cutover (Bisson/tc.cu:63-87): warp per row, row copied to the
-// warp's shared slot; lanes stream each N+(v) and binary-search the row.
-template <int CAP>
-__global__ void __launch_bounds__(kBiWarps * 32) bisson_small_kernel(CsrView g, const int32_t* rows, int nrows,
+// Pass 2: scatter partners into their group (order inside a group is irrelevant).
+__global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t m_pad = (g.m + 31) & ~31ll;
+  const int lane = threadIdx.x & 31;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
+    int32_t h = -1, p = 0;
+    if (e < g.m) {
+      int32_t u = g.esrc[e], v = g.cols[e];
+      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      if (du > 0 && dv > 0) {
+        bool hu = longer_is_u(u, v, du, dv);
+        h = hu ? u : v;
+        p = hu ? v : u;
+      }
+    }
+    unsigned same = __match_any_sync(0xffffffffu, h);
+    int lead = __ffs(same) - 1;
+    int base = 0;
+    if (h >= 0 && lane == lead) base = atomicAdd(&cur[h], __popc(same));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    if (h >= 0) plist[gstart[h] + base + __popc(same & ((1u << lane) - 1))] = p;
+  }
+}
+
+// Pass 3: cut every group into chunks (work items) of at most kLightChunk / kHeavyChunk
+// partners; a heavy chunk picks hash, bitmap or plain search for N+(h).
+__global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* light, int* nlight, GroupItem* heavy,
+                                   int* nheavy, int light_max) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
+    int64_t b = gstart[h], e = gstart[h + 1];
+    if (b == e) continue;
+    int64_t hb = g.off[h], dh = g.off[h + 1] - hb;
+    if (dh <= light_max) {
+      int64_t k = (e - b + kLightChunk - 1) / kLightChunk;
+      int at = atomicAdd(nlight, (int)k);
+      for (int64_t c = 0; c < k; ++c)
+        light[at + c] = GroupItem{(int32_t)h, 0, b + c * kLightChunk, min(e, b + (c + 1) * kLightChunk)};
+    } else {
+      int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
+      int32_t mode = dh <= kHashMax ? 0 : (span < kTabWords * 32 ? 1 : 2);
+      int64_t k = (e - b + kHeavyChunk - 1) / kHeavyChunk;
+      int at = atomicAdd(nheavy, (int)k);
+      for (int64_t c = 0; c < k; ++c)
+        heavy[at + c] = GroupItem{(int32_t)h, mode, b + c * kHeavyChunk, min(e, b + (c + 1) * kHeavyChunk)};
+    }
+  }
+}
+
+// Streams the lists of partners plist[i0, i0+32), plist[i0+step, ...), ... (< i1)
+// through `probe`, 32 partners at a time:
+// a warp prefix sum over their lengths spreads the elements over the lanes, so short
+// lists do not leave lanes idle.  sx/sp: the warp's 32-entry shared scratch.
+template <class Probe>
+__device__ __forceinline__ unsigned long long stream_partners(const CsrView& g, const int32_t* plist, int64_t i0,
+                                                              int64_t i1, int64_t step, int lane, int* sx,
+                                                              int64_t* sp, Probe probe) {
+  unsigned long long cnt = 0;
+  for (int64_t base = i0; base < i1; base += step) {
+    int64_t i = base + lane;
+    int len = 0;
+    int64_t pb = 0;
+    if (i < i1) {
+      int32_t p = plist[i];
+      pb = g.off[p];
+      len = (int)(g.off[p + 1] - pb);
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    sx[lane] = incl - len;
+    sp[lane] = pb;
+    __syncwarp();
+    int k = 0;
+    for (int t = lane; t < total; t += 32) {
+      while (k < 31 && sx[k + 1] <= t) ++k;
+      cnt += probe(g.cols[sp[k] + (t - sx[k])]);
+    }
+    __syncwarp();
+  }
+  return cnt;
+}
+
+__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
+
+__global__ void __launch_bounds__(kBgWarps * 32) bisson_light_kernel(CsrView g, const int32_t* plist,
+                                                                   const GroupItem* items, int nitems,
                                                                    unsigned long long* out) {
-  __shared__ int32_t row[kBiWarps][CAP];
+  __shared__ int32_t row[kBgWarps][kLightMax];
+  __shared__ int sx[kBgWarps][32];
+  __shared__ int64_t sp[kBgWarps][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned long long cnt = 0;
-  const int warps = gridDim.x * kBiWarps;
-  for (int r = blockIdx.x * kBiWarps + w; r < nrows; r += warps) {
-    int32_t u = rows[r];
-    int64_t ub = g.off[u];
-    int du = (int)(g.off[u + 1] - ub);
-    for (int j = lane; j < du; j += 32) row[w][j] = g.cols[ub + j];
+  for (int it = blockIdx.x * kBgWarps + w; it < nitems; it += gridDim.x * kBgWarps) {
+    GroupItem gi = items[it];
+    int64_t hb = g.off[gi.h];
+    int dh = (int)(g.off[gi.h + 1] - hb);
+    for (int j = lane; j < dh; j += 32) row[w][j] = g.cols[hb + j];
     __syncwarp();
-    for (int k = 0; k < du; ++k) {
-      int32_t v = row[w][k];
-      int64_t vb = g.off[v], vd = g.off[v + 1] - vb;
-      for (int64_t j = lane; j < vd; j += 32) cnt += bsearch_has32(row[w], du, g.cols[vb + j]);
-    }
+    const int32_t* r = row[w];
+    cnt += stream_partners(g, plist, gi.b, gi.e, 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
+      int lo = 0, hi = dh;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (r[mid] < x) lo = mid + 1; else hi = mid;
+      }
+      return lo < dh && r[lo] == x;
+    });
     __syncwarp();
   }
   warp_add_count(cnt, out);
 }
 
-// Rows of out-degree > cutover (Bisson/tc.cu:36-62): CTA per row.  N+(u) becomes a
-// bitmap over [lo, hi] = [min, max] of the row: in shared memory when the span fits,
-// else in this CTA's slice of a global bitmap over all vertices.  Only the words the
-// row touched are cleared afterwards, never the whole bitmap.
-__global__ void __launch_bounds__(kBiWarps * 32) bisson_hub_kernel(CsrView g, const int32_t* hubs, int nhubs,
-                                                                 uint32_t* gbits, int64_t gwords,
-                                                                 unsigned long long* out) {
-  extern __shared__ uint32_t sbits[];
+__global__ void __launch_bounds__(kBgWarps * 32) bisson_heavy_kernel(CsrView g, const int32_t* plist,
+                                                                   const GroupItem* items, int nitems, int* next,
+                                                                   unsigned long long* out) {
+  extern __shared__ int32_t tab[];  // kTabWords
+  __shared__ int sx[kBgWarps][32];
+  __shared__ int64_t sp[kBgWarps][32];
+  __shared__ int cur_item;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned long long cnt = 0;
-  uint32_t* mybits = gbits + (int64_t)blockIdx.x * gwords;
-  for (int j = threadIdx.x; j < kBiBitmapWords; j += blockDim.x) sbits[j] = 0;
-  __syncthreads();
-  for (int h = blockIdx.x; h < nhubs; h += gridDim.x) {
-    int32_t u = hubs[h];
-    int64_t ub = g.off[u], du = g.off[u + 1] - ub;
-    const int32_t* Nu = g.cols + ub;
-    int32_t lo = Nu[0], hi = Nu[du - 1];
-    bool shared_map = (int64_t)hi - lo < (int64_t)kBiBitmapWords * 32;
-    uint32_t* bits = shared_map ? sbits : mybits;
-    int32_t base = shared_map ? lo : 0;
-    for (int64_t j = threadIdx.x; j < du; j += blockDim.x) {
-      int32_t x = Nu[j] - base;
-      atomicOr(&bits[x >> 5], 1u << (x & 31));
-    }
+  for (;;) {
+    if (threadIdx.x == 0) cur_item = atomicAdd(next, 1);
     __syncthreads();
-    for (int64_t k = w; k < du; k += kBiWarps) {
-      int32_t v = Nu[k];
-      int64_t vb = g.off[v], vd = g.off[v + 1] - vb;
-      for (int64_t j = lane; j < vd; j += 32) {
-        int32_t x = g.cols[vb + j];
-        if (x < lo || x > hi) continue;
-        x -= base;
-        cnt += (bits[x >> 5] >> (x & 31)) & 1u;
+    int it = cur_item;
+    if (it >= nitems) break;
+    GroupItem gi = items[it];
+    int64_t hb = g.off[gi.h];
+    int64_t dh = g.off[gi.h + 1] - hb;
+    const int32_t* Nh = g.cols + hb;
+    if (gi.mode == 0) {
+      uint32_t cap = 64;
+      while (cap < 4 * (uint32_t)dh) cap <<= 1;
+      const uint32_t mask = cap - 1;
+      for (uint32_t j = threadIdx.x; j < cap; j += blockDim.x) tab[j] = -1;
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) {
+        int32_t x = Nh[j];
+        uint32_t s = hash_slot(x, mask);
+        for (uint32_t n = 0; n < cap; ++n) {
+          if (atomicCAS(&tab[s], -1, x) == -1) break;
+          s = (s + 1) & mask;
+        }
       }
+      __syncthreads();
+      cnt += stream_partners(g, plist, gi.b + w * 32, gi.e, kBgWarps * 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
+        uint32_t s = hash_slot(x, mask);
+        for (uint32_t n = 0; n < cap; ++n) {
+          int32_t y = tab[s];
+          if (y == x) return 1u;
+          if (y == -1) return 0u;
+          s = (s + 1) & mask;
+        }
+        return 0u;
+      });
+    } else if (gi.mode == 1) {
+      const int32_t lo = Nh[0], hi = Nh[dh - 1];
+      const int words = ((hi - lo) >> 5) + 1;
+      uint32_t* bits = reinterpret_cast<uint32_t*>(tab);
+      for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0u;
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) {
+        int32_t x = Nh[j] - lo;
+        atomicOr(&bits[x >> 5], 1u << (x & 31));
+      }
+      __syncthreads();
+      cnt += stream_partners(g, plist, gi.b + w * 32, gi.e, kBgWarps * 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
+        if (x < lo || x > hi) return 0u;
+        x -= lo;
+        return (bits[x >> 5] >> (x & 31)) & 1u;
+      });
+    } else {
+      cnt += stream_partners(g, plist, gi.b + w * 32, gi.e, kBgWarps * 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
+        int64_t lo = 0, hi = dh;
+        while (lo < hi) {
+          int64_t mid = (lo + hi) >> 1;
+          if (Nh[mid] < x) lo = mid + 1; else hi = mid;
+        }
+        return lo < dh && Nh[lo] == x;
+      });
     }
-    __syncthreads();
-    for (int64_t j = threadIdx.x; j < du; j += blockDim.x) bits[(Nu[j] - base) >> 5] = 0;
     __syncthreads();
   }
   warp_add_count(cnt, out);
@@ -478,38 +635,52 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
 
 static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                              int* launches) {
-  int cut = t && t->bisson_cutover > 0 ? t->bisson_cutover : 32;
-  if (cut > 64) cut = 64;
-  DevBuf<int32_t> hubs, smalls;
-  DevBuf<int> counts;
-  ATC_TRY(hubs.alloc(g.n, s));
-  ATC_TRY(smalls.alloc(g.n, s));
-  ATC_TRY(counts.alloc(2, s));
-  ATC_CK(cudaMemsetAsync(counts.p, 0, sizeof(int) * 2, s));
-  bisson_classify_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, cut, hubs.p, smalls.p, counts.p);
+  int light_max = t && t->bisson_cutover > 0 ? std::min(t->bisson_cutover, kLightMax) : 32;
+  DevBuf<int32_t> cnt, cur, plist;
+  DevBuf<int64_t> gstart;
+  DevBuf<int> counters;  // nlight, nheavy, next
+  ATC_TRY(cnt.alloc(g.n + 1, s));
+  ATC_TRY(cur.alloc(g.n, s));
+  ATC_TRY(gstart.alloc(g.n + 1, s));
+  ATC_TRY(counters.alloc(3, s));
+  ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (g.n + 1), s));
+  ATC_CK(cudaMemsetAsync(cur.p, 0, sizeof(int32_t) * g.n, s));
+  ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 3, s));
+  group_count_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, cnt.p);
+  ATC_CK(cudaGetLastError());
+  ATC_TRY(exclusive_scan_i32_to_i64(cnt.p, gstart.p, g.n + 1, s));
+  int64_t total = 0;
+  ATC_CK(cudaMemcpyAsync(&total, gstart.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  ATC_TRY(plist.alloc(total + 1, s));
+  group_scatter_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, gstart.p, cur.p, plist.p);
+  ATC_CK(cudaGetLastError());
+  // items: at most one per group plus one per chunk boundary
+  int64_t max_items = g.n + total / kLightChunk + 1;
+  DevBuf<GroupItem> light, heavy;
+  ATC_TRY(light.alloc(max_items, s));
+  ATC_TRY(heavy.alloc(max_items, s));
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, light.p, counters.p, heavy.p, counters.p + 1,
+                                                        light_max);
   ATC_CK(cudaGetLastError());
   int hc[2];
-  ATC_CK(cudaMemcpyAsync(hc, counts.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
-  *launches += 1;
+  *launches += 4;
   if (hc[1]) {
-    int bps = blocks_per_sm((const void*)bisson_small_kernel<64>, kBiWarps * 32, 0);
-    unsigned grid = (unsigned)std::min<int64_t>((hc[1] + kBiWarps - 1) / kBiWarps, (int64_t)sm_count() * bps);
-    if (cut <= 32) bisson_small_kernel<32><<<grid, kBiWarps * 32, 0, s>>>(g, smalls.p, hc[1], ctr);
-    else bisson_small_kernel<64><<<grid, kBiWarps * 32, 0, s>>>(g, smalls.p, hc[1], ctr);
+    size_t smem = sizeof(int32_t) * kTabWords;
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_heavy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    int bps = blocks_per_sm((const void*)bisson_heavy_kernel, kBgWarps * 32, smem);
+    int grid = std::min(hc[1], sm_count() * bps);
+    bisson_heavy_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, heavy.p, hc[1], counters.p + 2, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
   if (hc[0]) {
-    size_t smem = sizeof(uint32_t) * kBiBitmapWords;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_hub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_hub_kernel, kBiWarps * 32, smem);
-    int grid = std::min(hc[0], sm_count() * bps);
-    int64_t gwords = (g.n + 31) / 32 + 1;
-    DevBuf<uint32_t> gbits;
-    ATC_TRY(gbits.alloc((size_t)gwords * grid, s));
-    ATC_CK(cudaMemsetAsync(gbits.p, 0, sizeof(uint32_t) * gwords * grid, s));
-    bisson_hub_kernel<<<grid, kBiWarps * 32, smem, s>>>(g, hubs.p, hc[0], gbits.p, gwords, ctr);
+    int bps = blocks_per_sm((const void*)bisson_light_kernel, kBgWarps * 32, 0);
+    unsigned grid = (unsigned)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
+    bisson_light_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist.p, light.p, hc[0], ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
@@ -553,6 +724,8 @@ extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tu
     stats->total_ms = stats->kernel_ms;
     stats->wedges = (uint64_t)csr->wedges;
     stats->alg_bytes = 4ull * (uint64_t)(csr->n + 1) + 4ull * (uint64_t)csr->m + 4ull * (uint64_t)csr->wedges + 8ull;
+    stats->alg_bytes_min =
+        4ull * (uint64_t)(csr->n + 1) + 4ull * (uint64_t)csr->m + 4ull * (uint64_t)csr->wedges_min + 8ull;
     stats->kernel_used = (int32_t)kernel;
     stats->launches = launches;
   }

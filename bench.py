@@ -147,18 +147,21 @@ def cpu_baseline(g_lower_off, g_lower_cols, m_total, target_s):
     import oracle
     n = g_lower_off.size - 1
     nthreads = os.cpu_count() or 1
-    stride = max(1, n // 2048)
-    t0 = time.perf_counter()
-    _, e = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride, 0, nthreads)
-    dt = time.perf_counter() - t0
-    # grow the sample to about target_s seconds
+    stride = max(1, n // 1024)
+    for _ in range(3):  # calibrate the stride to about target_s seconds of CPU work
+        t0 = time.perf_counter()
+        oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride, 1, nthreads)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 4 or stride == 1:
+            break
+        stride = max(1, int(stride * dt / target_s * 1.2)) if dt > 0 else stride // 16
     if dt > 0:
-        stride = max(1, int(stride * dt / max(target_s, 0.1)))
+        stride = max(1, int(round(stride * dt / target_s)))
     t0 = time.perf_counter()
     cnt, e = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride, 0, nthreads)
     dt = time.perf_counter() - t0
     return {"value": e / dt if dt > 0 else None, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": "every %d-th vertex u (%d of %d) with all its lower-neighbour edges (%d edges of %d); %.1f s"
+            "sample": "every %d-th vertex u (%d of %d) with all its smaller-neighbour edges (%d of %d edges); %.1f s"
             % (stride, (n + stride - 1) // stride, n, e, m_total, dt),
             "machine": os.uname().machine}
 
@@ -311,11 +314,15 @@ def run_ours(a):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded R-MAT generated on the device)", "config": cfg,
-        "graph": {"n": csr.n, "m": m, "wedges": csr.wedges, "max_outdeg": csr.max_outdeg, "triangles": head_count},
+        "graph": {"n": csr.n, "m": m, "wedges": csr.wedges, "wedges_min": csr.wedges_min,
+                  "max_outdeg": csr.max_outdeg, "triangles": head_count},
         "headline_kernel": kname, "fastest_kernel": best, "kernels": kernels,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic_for(cfg, kname), "peak_source": peak_kind,
-                     "alg_bytes_per_launch": alg, "kernel_ms": kern_ms},
+                     "alg_bytes_per_launch": alg, "kernel_ms": kern_ms,
+                     "alg_bytes_min_per_launch": st.alg_bytes_min,
+                     "achieved_min": st.alg_bytes_min / (kern_ms * 1e-3) / 1e9,
+                     "frac_min": st.alg_bytes_min / (kern_ms * 1e-3) / 1e9 / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nraw * 8, "d2h_bytes_per_step": 8,
                 "ms_per_step": e2e_step, "steps": len(e2e_ms)},
         "gpu_launches": launches,

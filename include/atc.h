@@ -92,14 +92,16 @@ typedef struct atc_csr {
   int32_t order;        /* atc_order used */
   int32_t pruned;       /* 1 when degree<=1 vertices were removed */
   int32_t max_outdeg;
+  int64_t wedges_min;   /* sum over edges (u,v) of min(outdeg(u), outdeg(v)) */
   void* priv;           /* library-internal */
 } atc_csr;
 
 typedef struct atc_stats {
   float kernel_ms;       /* device time of the counting kernels (events on the stream) */
   float total_ms;        /* device time of the whole call */
-  uint64_t alg_bytes;    /* 4(n+1) + 4m + 4W + 8: the bytes every kernel family must read */
+  uint64_t alg_bytes;    /* 4(n+1) + 4m + 4W + 8: every candidate N+(v), v in N+(u), read once */
   uint64_t wedges;       /* W of the counted CSR */
+  uint64_t alg_bytes_min; /* 4(n+1) + 4m + 4*wedges_min + 8: only the shorter list of each edge read */
   int32_t kernel_used;   /* atc_kernel actually run */
   int32_t launches;      /* kernel launches made by the call */
 } atc_stats;
