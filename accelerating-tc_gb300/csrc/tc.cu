@@ -270,24 +270,27 @@ __global__ void __launch_bounds__(kHuWarps * 32) hu_kernel(CsrView g, const int3
 // The reference keeps a bitmap of N+(u) for rows longer than 32 and streams every N+(v),
 // v in N+(u), through it (Bisson/tc.cu:36-62): one bit test per directed wedge, W tests
 // in all.  Here every edge {u, v} is handed to its endpoint h with the longer list; N+(h)
-// becomes a set in shared memory (hash table, or bitmap over [min, max] of the list) and
-// the shorter list of the partner is streamed through it.  That tests
-// sum_edges min(d+u, d+v) elements instead of W, with one shared-memory probe each.
-//   light groups (d+h <= kLightMax): a warp per chunk of partners, N+(h) staged in the
-//     warp's shared slot and binary-searched (the reference's <=32 branch, :63-87);
-//   heavy groups: a CTA per chunk of partners, N+(h) as a hash table (d+h <= kHashMax)
-//     or a bitmap (span < kTabWords*32), else binary search in global memory.
-// Chunks are taken from a device work counter (one atomicAdd per chunk; no waiting).
+// becomes a set in shared memory and the shorter list of the partner is streamed
+// through it.  That tests sum_edges min(d+u, d+v) elements instead of W.
+//   warp items (d+h <= kWarpMax): a warp per chunk of partners, no block barriers; N+(h)
+//     either copied sorted into the warp's slot and binary-searched (d+h <= cutover, the
+//     reference's <=32 branch, Bisson/tc.cu:63-87) or inserted into a warp-private hash
+//     table of kWarpSlots slots (load factor <= 1/4);
+//   block items (d+h > kWarpMax): a CTA per chunk of partners; N+(h) as a block hash
+//     table sized to the largest such list, or a bitmap over [min, max] of the list, or
+//     (lists too long for both) binary search in global memory.
+// Chunks come from device work counters (one atomicAdd per chunk; nothing waits on them).
 constexpr int kBgWarps = 8;
-constexpr int kLightMax = 64;
-constexpr int kLightChunk = 256;
-constexpr int kHeavyChunk = 2048;
-constexpr int kTabWords = 16384;   // 64 KB: hash slots or bitmap words
-constexpr int kHashMax = kTabWords / 4;  // load factor <= 1/4
+constexpr int kWarpMax = 256;       // longest N+(h) handled by one warp
+constexpr int kWarpSlots = 1024;    // warp-private hash slots (4 KB)
+constexpr int kWarpChunk = 512;     // partners per warp item
+constexpr int kBlockChunk = 2048;   // partners per block item
+constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
+constexpr int kHashMax = kTabWords / 4;
 
 struct GroupItem {
   int32_t h;
-  int32_t mode;  // heavy: 0 hash, 1 bitmap, 2 global search
+  int32_t mode;  // warp: 0 sorted copy, 1 hash; block: 0 hash, 1 bitmap, 2 global search
   int64_t b, e;  // partner range in the grouped list
 };
 
@@ -338,48 +341,85 @@ __global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* 
   }
 }
 
-// Pass 3: cut every group into chunks (work items) of at most kLightChunk / kHeavyChunk
-// partners; a heavy chunk picks hash, bitmap or plain search for N+(h).
-__global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* light, int* nlight, GroupItem* heavy,
-                                   int* nheavy, int light_max) {
+// Pass 3: cut every group into work items; counters[0] = warp items, [1] = block items,
+// [3] = longest N+(h) among block items.
+__global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* witems, GroupItem* bitems,
+                                   int* counters, int cutover) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
     int64_t b = gstart[h], e = gstart[h + 1];
     if (b == e) continue;
     int64_t hb = g.off[h], dh = g.off[h + 1] - hb;
-    if (dh <= light_max) {
-      int64_t k = (e - b + kLightChunk - 1) / kLightChunk;
-      int at = atomicAdd(nlight, (int)k);
+    if (dh <= kWarpMax) {
+      int32_t mode = dh <= cutover ? 0 : 1;
+      int64_t k = (e - b + kWarpChunk - 1) / kWarpChunk;
+      int at = atomicAdd(&counters[0], (int)k);
       for (int64_t c = 0; c < k; ++c)
-        light[at + c] = GroupItem{(int32_t)h, 0, b + c * kLightChunk, min(e, b + (c + 1) * kLightChunk)};
+        witems[at + c] = GroupItem{(int32_t)h, mode, b + c * kWarpChunk, min(e, b + (c + 1) * kWarpChunk)};
     } else {
       int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
       int32_t mode = dh <= kHashMax ? 0 : (span < kTabWords * 32 ? 1 : 2);
-      int64_t k = (e - b + kHeavyChunk - 1) / kHeavyChunk;
-      int at = atomicAdd(nheavy, (int)k);
+      if (mode == 0) atomicMax(&counters[3], (int)dh);
+      else atomicMax(&counters[3], kHashMax);
+      int64_t k = (e - b + kBlockChunk - 1) / kBlockChunk;
+      int at = atomicAdd(&counters[1], (int)k);
       for (int64_t c = 0; c < k; ++c)
-        heavy[at + c] = GroupItem{(int32_t)h, mode, b + c * kHeavyChunk, min(e, b + (c + 1) * kHeavyChunk)};
+        bitems[at + c] = GroupItem{(int32_t)h, mode, b + c * kBlockChunk, min(e, b + (c + 1) * kBlockChunk)};
     }
   }
 }
 
-// Streams the lists of partners plist[i0, i0+32), plist[i0+step, ...), ... (< i1)
-// through `probe`, 32 partners at a time:
-// a warp prefix sum over their lengths spreads the elements over the lanes, so short
-// lists do not leave lanes idle.  sx/sp: the warp's 32-entry shared scratch.
-template <class Probe>
-__device__ __forceinline__ unsigned long long stream_partners(const CsrView& g, const int32_t* plist, int64_t i0,
-                                                              int64_t i1, int64_t step, int lane, int* sx,
-                                                              int64_t* sp, Probe probe) {
-  unsigned long long cnt = 0;
-  for (int64_t base = i0; base < i1; base += step) {
+__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
+
+// Linear-probing lookup; the table always has empty slots, and `cap` bounds the walk.
+__device__ __forceinline__ unsigned hash_has(const int32_t* tab, uint32_t mask, int32_t x) {
+  uint32_t s = hash_slot(x, mask);
+  int32_t y = tab[s];
+  if (y == x) return 1u;
+  for (uint32_t n = 0; y != -1 && n <= mask; ++n) {
+    s = (s + 1) & mask;
+    y = tab[s];
+    if (y == x) return 1u;
+  }
+  return 0u;
+}
+
+// Inserts x (not yet present); concurrent inserters use atomicCAS.
+__device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t x) {
+  uint32_t s = hash_slot(x, mask);
+  for (uint32_t n = 0; n <= mask; ++n) {
+    if (atomicCAS(&tab[s], -1, x) == -1) return;
+    s = (s + 1) & mask;
+  }
+}
+
+// Empties the slot holding x (x present); keys are cleared only by the thread that
+// inserted them, so the walk always reaches x.
+__device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t x) {
+  uint32_t s = hash_slot(x, mask);
+  for (uint32_t n = 0; n <= mask; ++n) {
+    if (tab[s] == x) { tab[s] = -1; return; }
+    s = (s + 1) & mask;
+  }
+}
+
+// Streams the lists of partners plist[i0, i0+32), then the batch `next_batch()` gives,
+// through `probe`.  A warp prefix sum over the 32 lengths spreads the elements over
+// the lanes, so short lists do not leave lanes idle; each lane keeps the current
+// partner's start in registers.  sx/sp: the warp's 32-entry shared scratch.
+template <class NextBatch, class Probe>
+__device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
+                                                    int lane, int* sx, int64_t* sp, NextBatch next_batch,
+                                                    Probe probe) {
+  unsigned cnt = 0;
+  for (int64_t base = next_batch(); base < i1; base = next_batch()) {
     int64_t i = base + lane;
     int len = 0;
     int64_t pb = 0;
     if (i < i1) {
-      int32_t p = plist[i];
-      pb = g.off[p];
-      len = (int)(g.off[p + 1] - pb);
+      int32_t p = __ldg(plist + i);
+      pb = __ldg(g.off + p);
+      len = (int)(__ldg(g.off + p + 1) - pb);
     }
     int incl = len;
 #pragma unroll
@@ -387,93 +427,120 @@ __device__ __forceinline__ unsigned long long stream_partners(const CsrView& g, 
       int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
     sx[lane] = incl - len;
     sp[lane] = pb;
     __syncwarp();
     int k = 0;
+    int kx = sx[0], knext = sx[1];
+    int64_t kp = sp[0];
     for (int t = lane; t < total; t += 32) {
-      while (k < 31 && sx[k + 1] <= t) ++k;
-      cnt += probe(g.cols[sp[k] + (t - sx[k])]);
+      while (k < 31 && knext <= t) {
+        ++k;
+        kx = knext;
+        kp = sp[k];
+        knext = k < 31 ? sx[k + 1] : total;
+      }
+      cnt += probe(__ldg(g.cols + kp + (t - kx)));
     }
     __syncwarp();
   }
   return cnt;
 }
 
-__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
-
-__global__ void __launch_bounds__(kBgWarps * 32) bisson_light_kernel(CsrView g, const int32_t* plist,
-                                                                   const GroupItem* items, int nitems,
-                                                                   unsigned long long* out) {
-  __shared__ int32_t row[kBgWarps][kLightMax];
+__global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
+                                                                  const GroupItem* items, int nitems, int* next,
+                                                                  unsigned long long* out) {
+  __shared__ int32_t tab[kBgWarps][kWarpSlots];
   __shared__ int sx[kBgWarps][32];
   __shared__ int64_t sp[kBgWarps][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned long long cnt = 0;
-  for (int it = blockIdx.x * kBgWarps + w; it < nitems; it += gridDim.x * kBgWarps) {
-    GroupItem gi = items[it];
-    int64_t hb = g.off[gi.h];
-    int dh = (int)(g.off[gi.h + 1] - hb);
-    for (int j = lane; j < dh; j += 32) row[w][j] = g.cols[hb + j];
+  for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
+  __syncwarp();
+  unsigned long long total = 0;
+  int32_t* T = tab[w];
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(next, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const GroupItem gi = items[it];
+    const int64_t hb = g.off[gi.h];
+    const int dh = (int)(g.off[gi.h + 1] - hb);
+    int64_t cur = gi.b;
+    auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
+    unsigned cnt;
+    if (gi.mode == 0) {
+      for (int j = lane; j < dh; j += 32) T[j] = __ldg(g.cols + hb + j);
+      __syncwarp();
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+        int lo = 0, n = dh;
+        while (n > 1) {  // branch-free lower bound over the sorted copy
+          int half = n >> 1;
+          lo = T[lo + half - 1] < x ? lo + half : lo;
+          n -= half;
+        }
+        return T[lo] == x;
+      });
+      __syncwarp();
+      for (int j = lane; j < dh; j += 32) T[j] = -1;
+    } else {
+      uint32_t cap = 64;
+      while (cap < 4u * (uint32_t)dh) cap <<= 1;
+      const uint32_t mask = cap - 1;
+      for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
+      __syncwarp();
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
+                            [&](int32_t x) -> unsigned { return hash_has(T, mask, x); });
+      __syncwarp();
+      for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
+    }
     __syncwarp();
-    const int32_t* r = row[w];
-    cnt += stream_partners(g, plist, gi.b, gi.e, 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
-      int lo = 0, hi = dh;
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (r[mid] < x) lo = mid + 1; else hi = mid;
-      }
-      return lo < dh && r[lo] == x;
-    });
-    __syncwarp();
+    total += cnt;
   }
-  warp_add_count(cnt, out);
+  warp_add_count(total, out);
 }
 
-__global__ void __launch_bounds__(kBgWarps * 32) bisson_heavy_kernel(CsrView g, const int32_t* plist,
+__global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                    const GroupItem* items, int nitems, int* next,
-                                                                   unsigned long long* out) {
-  extern __shared__ int32_t tab[];  // kTabWords
+                                                                   uint32_t tab_words, unsigned long long* out) {
+  extern __shared__ int32_t tab[];  // tab_words
   __shared__ int sx[kBgWarps][32];
   __shared__ int64_t sp[kBgWarps][32];
   __shared__ int cur_item;
+  __shared__ unsigned long long bnext;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned long long cnt = 0;
+  for (uint32_t j = threadIdx.x; j < tab_words; j += blockDim.x) tab[j] = -1;
+  unsigned long long total = 0;
   for (;;) {
-    if (threadIdx.x == 0) cur_item = atomicAdd(next, 1);
+    if (threadIdx.x == 0) {
+      cur_item = atomicAdd(next, 1);
+      bnext = 0;
+    }
     __syncthreads();
-    int it = cur_item;
+    const int it = cur_item;
     if (it >= nitems) break;
-    GroupItem gi = items[it];
-    int64_t hb = g.off[gi.h];
-    int64_t dh = g.off[gi.h + 1] - hb;
+    const GroupItem gi = items[it];
+    const int64_t hb = g.off[gi.h];
+    const int64_t dh = g.off[gi.h + 1] - hb;
     const int32_t* Nh = g.cols + hb;
+    // partner batches of 32 handed out to the warps as they finish
+    auto nb = [&]() {
+      unsigned long long r = 0;
+      if (lane == 0) r = atomicAdd(&bnext, 32ull);
+      return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
+    };
+    unsigned cnt = 0;
     if (gi.mode == 0) {
       uint32_t cap = 64;
-      while (cap < 4 * (uint32_t)dh) cap <<= 1;
+      while (cap < 4u * (uint32_t)dh) cap <<= 1;
       const uint32_t mask = cap - 1;
-      for (uint32_t j = threadIdx.x; j < cap; j += blockDim.x) tab[j] = -1;
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
       __syncthreads();
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) {
-        int32_t x = Nh[j];
-        uint32_t s = hash_slot(x, mask);
-        for (uint32_t n = 0; n < cap; ++n) {
-          if (atomicCAS(&tab[s], -1, x) == -1) break;
-          s = (s + 1) & mask;
-        }
-      }
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
+                            [&](int32_t x) -> unsigned { return hash_has(tab, mask, x); });
       __syncthreads();
-      cnt += stream_partners(g, plist, gi.b + w * 32, gi.e, kBgWarps * 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
-        uint32_t s = hash_slot(x, mask);
-        for (uint32_t n = 0; n < cap; ++n) {
-          int32_t y = tab[s];
-          if (y == x) return 1u;
-          if (y == -1) return 0u;
-          s = (s + 1) & mask;
-        }
-        return 0u;
-      });
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
     } else if (gi.mode == 1) {
       const int32_t lo = Nh[0], hi = Nh[dh - 1];
       const int words = ((hi - lo) >> 5) + 1;
@@ -485,13 +552,15 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_heavy_kernel(CsrView g, 
         atomicOr(&bits[x >> 5], 1u << (x & 31));
       }
       __syncthreads();
-      cnt += stream_partners(g, plist, gi.b + w * 32, gi.e, kBgWarps * 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
         if (x < lo || x > hi) return 0u;
         x -= lo;
         return (bits[x >> 5] >> (x & 31)) & 1u;
       });
+      __syncthreads();
+      for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0xffffffffu;  // back to empty slots (-1)
     } else {
-      cnt += stream_partners(g, plist, gi.b + w * 32, gi.e, kBgWarps * 32, lane, sx[w], sp[w], [&](int32_t x) -> unsigned {
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
         int64_t lo = 0, hi = dh;
         while (lo < hi) {
           int64_t mid = (lo + hi) >> 1;
@@ -501,8 +570,9 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_heavy_kernel(CsrView g, 
       });
     }
     __syncthreads();
+    total += cnt;
   }
-  warp_add_count(cnt, out);
+  warp_add_count(total, out);
 }
 
 int blocks_per_sm(const void* kernel, int block, size_t smem) {
@@ -635,52 +705,56 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
 
 static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                              int* launches) {
-  int light_max = t && t->bisson_cutover > 0 ? std::min(t->bisson_cutover, kLightMax) : 32;
+  int cutover = t && t->bisson_cutover > 0 ? std::min(t->bisson_cutover, kWarpMax) : 32;
   DevBuf<int32_t> cnt, cur, plist;
   DevBuf<int64_t> gstart;
-  DevBuf<int> counters;  // nlight, nheavy, next
+  DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
   ATC_TRY(cnt.alloc(g.n + 1, s));
   ATC_TRY(cur.alloc(g.n, s));
   ATC_TRY(gstart.alloc(g.n + 1, s));
-  ATC_TRY(counters.alloc(3, s));
+  ATC_TRY(counters.alloc(8, s));
   ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (g.n + 1), s));
   ATC_CK(cudaMemsetAsync(cur.p, 0, sizeof(int32_t) * g.n, s));
-  ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 3, s));
+  ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
   group_count_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, cnt.p);
   ATC_CK(cudaGetLastError());
   ATC_TRY(exclusive_scan_i32_to_i64(cnt.p, gstart.p, g.n + 1, s));
   int64_t total = 0;
   ATC_CK(cudaMemcpyAsync(&total, gstart.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
-  ATC_TRY(plist.alloc(total + 1, s));
+  ATC_TRY(plist.alloc(total + 32, s));
   group_scatter_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, gstart.p, cur.p, plist.p);
   ATC_CK(cudaGetLastError());
   // items: at most one per group plus one per chunk boundary
-  int64_t max_items = g.n + total / kLightChunk + 1;
-  DevBuf<GroupItem> light, heavy;
-  ATC_TRY(light.alloc(max_items, s));
-  ATC_TRY(heavy.alloc(max_items, s));
-  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, light.p, counters.p, heavy.p, counters.p + 1,
-                                                        light_max);
+  int64_t max_items = g.n + total / kWarpChunk + 1;
+  DevBuf<GroupItem> witems, bitems;
+  ATC_TRY(witems.alloc(max_items, s));
+  ATC_TRY(bitems.alloc(max_items, s));
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p, cutover);
   ATC_CK(cudaGetLastError());
-  int hc[2];
+  int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   *launches += 4;
   if (hc[1]) {
-    size_t smem = sizeof(int32_t) * kTabWords;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_heavy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    // block table: enough slots for the longest hashed list at load factor 1/4, or the
+    // full bitmap when some list needs it
+    uint32_t words = 64;
+    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
+    if (words > (uint32_t)kTabWords) words = kTabWords;
+    size_t smem = sizeof(int32_t) * words;
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_heavy_kernel, kBgWarps * 32, smem);
+    int bps = blocks_per_sm((const void*)bisson_block_kernel, kBgWarps * 32, smem);
     int grid = std::min(hc[1], sm_count() * bps);
-    bisson_heavy_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, heavy.p, hc[1], counters.p + 2, ctr);
+    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, bitems.p, hc[1], counters.p + 5, words, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
   if (hc[0]) {
-    int bps = blocks_per_sm((const void*)bisson_light_kernel, kBgWarps * 32, 0);
-    unsigned grid = (unsigned)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
-    bisson_light_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist.p, light.p, hc[0], ctr);
+    int bps = blocks_per_sm((const void*)bisson_warp_kernel, kBgWarps * 32, 0);
+    int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
+    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist.p, witems.p, hc[0], counters.p + 4, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
