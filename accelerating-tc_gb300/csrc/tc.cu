@@ -372,14 +372,17 @@ __global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* 
 __device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
 
 // Linear-probing lookup; the table always has empty slots, and `cap` bounds the walk.
+// Most lookups end at the first slot (load factor <= 1/4).
 __device__ __forceinline__ unsigned hash_has(const int32_t* tab, uint32_t mask, int32_t x) {
   uint32_t s = hash_slot(x, mask);
   int32_t y = tab[s];
   if (y == x) return 1u;
-  for (uint32_t n = 0; y != -1 && n <= mask; ++n) {
+  if (y == -1) return 0u;
+  for (uint32_t n = 0; n < mask; ++n) {
     s = (s + 1) & mask;
     y = tab[s];
     if (y == x) return 1u;
+    if (y == -1) return 0u;
   }
   return 0u;
 }
@@ -403,10 +406,13 @@ __device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t 
   }
 }
 
-// Streams the lists of partners plist[i0, i0+32), then the batch `next_batch()` gives,
-// through `probe`.  A warp prefix sum over the 32 lengths spreads the elements over
-// the lanes, so short lists do not leave lanes idle; each lane keeps the current
-// partner's start in registers.  sx/sp: the warp's 32-entry shared scratch.
+// Streams the lists of the partners plist[base, base+32) for every batch start `base`
+// that `next_batch()` hands out (until it reaches i1) through `probe`, and returns the
+// hits.  Lists of 32 or more elements are walked by the whole warp, one list at a
+// time, four coalesced loads in flight per lane.  Shorter lists are spread over the
+// lanes by a warp prefix sum of their lengths, so they do not leave lanes idle; each
+// lane follows the list it is in with a cursor kept in registers.  sx/sp: the warp's
+// 32-entry shared scratch.
 template <class NextBatch, class Probe>
 __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
                                                     int lane, int* sx, int64_t* sp, NextBatch next_batch,
@@ -421,16 +427,32 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
       pb = __ldg(g.off + p);
       len = (int)(__ldg(g.off + p + 1) - pb);
     }
-    int incl = len;
+    unsigned longm = __ballot_sync(0xffffffffu, len >= 32);
+    while (longm) {
+      const int k = __ffs(longm) - 1;
+      longm &= longm - 1;
+      const int32_t* P = g.cols + __shfl_sync(0xffffffffu, pb, k);
+      const int ln = __shfl_sync(0xffffffffu, len, k);
+      int j = lane;
+      for (; j + 96 < ln; j += 128) {
+        int32_t x0 = __ldg(P + j), x1 = __ldg(P + j + 32), x2 = __ldg(P + j + 64), x3 = __ldg(P + j + 96);
+        cnt += probe(x0) + probe(x1) + probe(x2) + probe(x3);
+      }
+      for (; j < ln; j += 32) cnt += probe(__ldg(P + j));
+    }
+    const int slen = len < 32 ? len : 0;
+    int incl = slen;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    sx[lane] = incl - len;
+    if (total == 0) continue;
+    sx[lane] = incl - slen;
     sp[lane] = pb;
     __syncwarp();
+    // k = the last lane whose start is <= t: always a lane with a non-empty short list
     int k = 0;
     int kx = sx[0], knext = sx[1];
     int64_t kp = sp[0];
