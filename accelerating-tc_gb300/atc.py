@@ -126,6 +126,7 @@ _SIGS = {
     "atc_adirection": (C.c_int, [_P, C.c_uint64, _P, C.POINTER(C.c_uint64), _P, _P]),
     "atc_aorder": (C.c_int, [_P, C.c_uint64, _P, _P, _P, _P]),
     "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
+    "atc_tc_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_uint64), _P]),
     "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_costfunc": (C.c_int, [_P, C.c_uint64, C.c_int32, _P, _P]),
     "atc_verification": (C.c_int, [_P, C.c_uint64, _P, _P]),
@@ -296,6 +297,13 @@ def tc(csr: CSR, kernel=Kernel.AUTO, tuning=None, stream=None):
     st = StatsStruct()
     _check(lib().atc_tc(C.byref(csr.struct), int(kernel), _tuning(tuning), C.byref(cnt), C.byref(st), stream))
     return cnt.value, _stats(st)
+
+
+def tc_noalloc(offsets_dev_ptr, cols_dev_ptr, n, m, stream=None):
+    """atc_tc_noalloc on plain device arrays (no device allocation inside the call)."""
+    cnt = C.c_uint64(0)
+    _check(lib().atc_tc_noalloc(C.c_void_p(offsets_dev_ptr), C.c_void_p(cols_dev_ptr), n, m, C.byref(cnt), stream))
+    return cnt.value
 
 
 def kcl(csr: CSR, k, stream=None):

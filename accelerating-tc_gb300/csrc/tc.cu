@@ -20,6 +20,7 @@
 //                                        shorter list, then a binary search inside the
 //                                        bracket.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "internal.cuh"
@@ -783,6 +784,174 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   return ATC_OK;
 }
 
+// ---- counting without device allocation ------------------------------------------
+// Some callers cannot call cudaMalloc: code recording into a CUDA graph whose capture
+// mode forbids allocation, hosts whose device memory is owned by another allocator or
+// runtime, or real-time loops that must not block in the driver.  atc_tc_noalloc runs
+// the Bisson-style count above with every scratch buffer (edge sources, group counts,
+// grouped partner list, work items, counters) carved out of one file-scope device array
+// of kNoAllocBytes, fixed in size, which every GPU that loads this library keeps until
+// the process exits.  Graphs above kNoAllocMaxN vertices or kNoAllocMaxM edges are
+// refused.  All calls share the one array: calls that overlap on the GPU (concurrent
+// streams or host threads on one device) race and must be serialised by the caller.
+constexpr int64_t kNoAllocMaxN = 1 << 17;  // 131072 vertices
+constexpr int64_t kNoAllocMaxM = 1 << 20;  // 1048576 oriented edges
+constexpr int64_t kNoAllocItems = kNoAllocMaxN + kNoAllocMaxM / kWarpChunk + 1;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kNaEsrc = 0;
+constexpr size_t kNaCnt = kNaEsrc + align256(sizeof(int32_t) * (kNoAllocMaxM + 32));
+constexpr size_t kNaCur = kNaCnt + align256(sizeof(int32_t) * (kNoAllocMaxN + 1));
+constexpr size_t kNaGstart = kNaCur + align256(sizeof(int32_t) * kNoAllocMaxN);
+constexpr size_t kNaPlist = kNaGstart + align256(sizeof(int64_t) * (kNoAllocMaxN + 1));
+constexpr size_t kNaWitems = kNaPlist + align256(sizeof(int32_t) * (kNoAllocMaxM + 32));
+constexpr size_t kNaBitems = kNaWitems + align256(sizeof(GroupItem) * kNoAllocItems);
+constexpr size_t kNaCounters = kNaBitems + align256(sizeof(GroupItem) * kNoAllocItems);
+constexpr size_t kNaCount = kNaCounters + align256(sizeof(int) * 8);
+constexpr size_t kNoAllocBytes = kNaCount + align256(sizeof(unsigned long long));
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+// Device address of g_noalloc_scratch for each device, looked up once per device.
+atc_status noalloc_scratch(unsigned char** out) {
+  static std::mutex mu;
+  static unsigned char* addr[64] = {};
+  int dev = 0;
+  ATC_CK(cudaGetDevice(&dev));
+  ATC_CHECK_ARG(dev >= 0 && dev < 64, "device index above 63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      set_error("cudaGetSymbolAddress(g_noalloc_scratch): %s", cudaGetErrorString(e));
+      return ATC_ERR_CUDA;
+    }
+    addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = addr[dev];
+  return ATC_OK;
+}
+
+// Checks a caller's CSR before any kernel indexes with it: offsets start at 0, end at m
+// and never decrease; every row is strictly increasing with ids in [0, n).  Sets
+// *bad = 1 on the first violation found by each warp.
+__global__ void csr_check_kernel(const int64_t* off, const int32_t* cols, int64_t n, int64_t m, int* bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[n] != m)) *bad = 1;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+    int64_t b = off[u], e = off[u + 1];
+    bool ok = b <= e && b >= 0 && e <= m;
+    if (ok) {
+      for (int64_t j = b + lane; j < e; j += 32) {
+        int32_t x = cols[j];
+        if (x < 0 || x >= n || (j + 1 < e && cols[j + 1] <= x)) ok = false;
+      }
+    }
+    if (__any_sync(0xffffffffu, !ok) && lane == 0) *bad = 1;
+  }
+}
+
+__global__ void esrc_fill_kernel(const int64_t* off, int64_t n, int32_t* esrc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < n; u += warps)
+    for (int64_t j = off[u] + lane; j < off[u + 1]; j += 32) esrc[j] = (int32_t)u;
+}
+
+// Exclusive scan of cnt[0, len) into out (int64), one block of 1024 threads, no
+// temporary storage: each thread scans a contiguous slice, slices are combined in
+// shared memory.
+__global__ void __launch_bounds__(1024) scan_one_block_kernel(const int32_t* cnt, int64_t len, int64_t* out) {
+  __shared__ int64_t part[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (len + 1023) / 1024;
+  const int64_t b = t * per, e = b + per < len ? b + per : len;
+  int64_t s = 0;
+  for (int64_t i = b; i < e; ++i) s += cnt[i];
+  part[t] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int64_t y = t >= o ? part[t - o] : 0;
+    __syncthreads();
+    part[t] += y;
+    __syncthreads();
+  }
+  int64_t run = part[t] - s;
+  for (int64_t i = b; i < e; ++i) {
+    out[i] = run;
+    run += cnt[i];
+  }
+}
+
+}  // namespace
+
+static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64_t n, int64_t m, uint64_t* count,
+                                  cudaStream_t s) {
+  unsigned char* base = nullptr;
+  ATC_TRY(noalloc_scratch(&base));
+  int32_t* esrc = reinterpret_cast<int32_t*>(base + kNaEsrc);
+  int32_t* cnt = reinterpret_cast<int32_t*>(base + kNaCnt);
+  int32_t* cur = reinterpret_cast<int32_t*>(base + kNaCur);
+  int64_t* gstart = reinterpret_cast<int64_t*>(base + kNaGstart);
+  int32_t* plist = reinterpret_cast<int32_t*>(base + kNaPlist);
+  GroupItem* witems = reinterpret_cast<GroupItem*>(base + kNaWitems);
+  GroupItem* bitems = reinterpret_cast<GroupItem*>(base + kNaBitems);
+  int* counters = reinterpret_cast<int*>(base + kNaCounters);
+  unsigned long long* total_ctr = reinterpret_cast<unsigned long long*>(base + kNaCount);
+  // what the kernels accumulate into starts at zero; the rest is overwritten
+  ATC_CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (n + 1), s));
+  ATC_CK(cudaMemsetAsync(cur, 0, sizeof(int32_t) * n, s));
+  ATC_CK(cudaMemsetAsync(counters, 0, sizeof(int) * 8, s));
+  ATC_CK(cudaMemsetAsync(total_ctr, 0, sizeof(unsigned long long), s));
+  csr_check_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(off, cols, n, m, counters + 6);
+  ATC_CK(cudaGetLastError());
+  int bad = 0;
+  ATC_CK(cudaMemcpyAsync(&bad, counters + 6, sizeof(int), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (bad) {
+    set_error("atc_tc_noalloc: offsets/cols are not an oriented CSR with sorted rows of ids in [0, n)");
+    return ATC_ERR_INVALID;
+  }
+  esrc_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(off, n, esrc);
+  ATC_CK(cudaGetLastError());
+  CsrView g{off, cols, esrc, n, m};
+  group_count_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, cnt);
+  scan_one_block_kernel<<<1, 1024, 0, s>>>(cnt, n + 1, gstart);
+  group_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, gstart, cur, plist);
+  group_items_kernel<<<grid_for(n, 256), 256, 0, s>>>(g, gstart, witems, bitems, counters, 32);
+  ATC_CK(cudaGetLastError());
+  int hc[4];
+  ATC_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (hc[1]) {
+    uint32_t words = 64;
+    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
+    if (words > (uint32_t)kTabWords) words = kTabWords;
+    size_t smem = sizeof(int32_t) * words;
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    int bps = blocks_per_sm((const void*)bisson_block_kernel, kBgWarps * 32, smem);
+    int grid = std::min(hc[1], sm_count() * bps);
+    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist, bitems, hc[1], counters + 5, words, total_ctr);
+    ATC_CK(cudaGetLastError());
+  }
+  if (hc[0]) {
+    int bps = blocks_per_sm((const void*)bisson_warp_kernel, kBgWarps * 32, 0);
+    int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
+    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist, witems, hc[0], counters + 4, total_ctr);
+    ATC_CK(cudaGetLastError());
+  }
+  unsigned long long h = 0;
+  ATC_CK(cudaMemcpyAsync(&h, total_ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  *count = h;
+  return ATC_OK;
+}
+
 }  // namespace atc
 
 using namespace atc;
@@ -826,4 +995,19 @@ extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tu
     stats->launches = launches;
   }
   return ATC_OK;
+}
+
+extern "C" atc_status atc_tc_noalloc(const int64_t* offsets, const int32_t* cols, int64_t n, int64_t m,
+                                     uint64_t* count, atc_stream st) {
+  ATC_CHECK_ARG(count != nullptr, "count is NULL");
+  ATC_CHECK_ARG(n >= 0 && m >= 0, "negative size");
+  if (n > kNoAllocMaxN || m > kNoAllocMaxM) {
+    set_error("graph too large for atc_tc_noalloc: n=%lld m=%lld, limits n<=%lld m<=%lld (scratch %zu bytes)",
+              (long long)n, (long long)m, (long long)kNoAllocMaxN, (long long)kNoAllocMaxM, kNoAllocBytes);
+    return ATC_ERR_INVALID;
+  }
+  *count = 0;
+  if (m == 0 || n == 0) return ATC_OK;
+  ATC_CHECK_ARG(offsets != nullptr && cols != nullptr, "NULL CSR array");
+  return tc_noalloc_impl(offsets, cols, n, m, count, as_stream(st));
 }

@@ -166,6 +166,19 @@ atc_status atc_aorder(const int32_t* pairs, uint64_t n_pairs, int32_t* lookup, i
    Bisson/tc.cu:198-204, Fox/tc.cu:334-384, tricount_gpu.cu:337-408. */
 atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning,
                   uint64_t* count, atc_stats* stats, atc_stream s);
+/* Triangle count of an oriented CSR given as plain device arrays, computed without
+   allocating any device memory.  No counterpart in the reference: it is for callers
+   that cannot call cudaMalloc (capture of a CUDA graph in a mode that forbids
+   allocation, device memory owned by another allocator, real-time loops).  Runs the
+   ATC_KERNEL_BISSON count with all scratch in one fixed device array of the library
+   (about 17 MiB, held by every device that loads the library until exit).  Limits:
+   n <= 131072 vertices and m <= 1048576 edges, else ATC_ERR_INVALID; offsets (n+1,
+   int64) and cols (m) must form a CSR whose rows are strictly increasing ids in
+   [0, n) (checked on the device first; ATC_ERR_INVALID otherwise).  The first call on
+   a device looks up the array's device address, so make it before any stream capture.
+   All calls share the array: calls that overlap on the GPU race. */
+atc_status atc_tc_noalloc(const int64_t* offsets_dev, const int32_t* cols_dev, int64_t n, int64_t m,
+                          uint64_t* count, atc_stream s);
 /* k-clique count (k >= 3) of the oriented CSR, exact in uint64.  Replaces
    kcl_gpu_solver(std::string, unsigned k, AccType& total, size_t) (k-clique/kcl.h:6-7). */
 atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream s);
