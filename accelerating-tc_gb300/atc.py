@@ -118,6 +118,8 @@ _SIGS = {
     "atc_init": (C.c_int, [C.c_int]),
     "atc_gen_rmat_host": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, C.c_int]),
     "atc_gen_rmat_device": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P]),
+    "atc_gen_rgg_host": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, _P, C.c_uint64, C.POINTER(C.c_uint64), C.c_int]),
+    "atc_gen_rgg_device": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, _P, C.c_uint64, C.POINTER(C.c_uint64), _P]),
     "atc_simplify_host": (C.c_int, [_P, C.c_uint64, C.c_int, _P, C.POINTER(C.c_uint64)]),
     "atc_pretc": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
     "atc_pretc_device": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
@@ -185,6 +187,16 @@ def gen_rmat(scale, edge_factor=16, seed=1, abc=GRAPH500, nthreads=None):
     _check(lib().atc_gen_rmat_host(scale, edge_factor, abc[0], abc[1], abc[2], seed, _ptr(out),
                                     nthreads or os.cpu_count() or 1))
     return out
+
+
+def gen_rgg(n, mean_degree=32.0, seed=1, nthreads=None):
+    """2-D random geometric graph on the host: edges (i, j), i < j, sorted."""
+    cnt = C.c_uint64(0)
+    nt = nthreads or os.cpu_count() or 1
+    _check(lib().atc_gen_rgg_host(n, mean_degree, seed, None, 0, C.byref(cnt), nt))
+    out = np.empty((max(cnt.value, 1), 2), dtype=np.int32)
+    _check(lib().atc_gen_rgg_host(n, mean_degree, seed, _ptr(out), cnt.value, C.byref(cnt), nt))
+    return out[: cnt.value]
 
 
 def simplify(pairs, symmetric=True):

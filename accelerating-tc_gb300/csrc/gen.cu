@@ -2,10 +2,12 @@
 // and the host simplifier that turns raw samples into the symmetrised, loop-free,
 // duplicate-free edge lists the benchmarks feed to every program.
 #include <algorithm>
+#include <atomic>
+#include <cmath>
 #include <thread>
 #include <vector>
 
-#include "common.cuh"
+#include "internal.cuh"
 
 namespace atc {
 
@@ -28,9 +30,181 @@ __global__ void rmat_kernel(uint64_t s0, uint32_t scale, uint64_t count, uint32_
   }
 }
 
+// ---- 2-D random geometric graph ------------------------------------------------------
+// Point i has 31-bit fixed-point coordinates drawn from one splitmix64 value; vertices
+// i < j are adjacent iff (dx^2 + dy^2) <= R^2 in 64-bit integers, R = radius * 2^31.
+// Integer arithmetic only, so host and device (and x86 / Arm) give the same edge set.
+__host__ __device__ inline void rgg_point(uint64_t s0, uint64_t i, uint32_t* x, uint32_t* y) {
+  uint64_t r = mix64(s0 + (i + 1) * kGolden);
+  *x = (uint32_t)(r & 0x7fffffffu);
+  *y = (uint32_t)((r >> 32) & 0x7fffffffu);
+}
+
+struct RggGrid {
+  uint64_t R2;      // squared radius
+  uint32_t cell;    // cell side (>= R)
+  uint32_t G;       // cells per side
+};
+
+static bool rgg_grid(uint32_t n, double mean_degree, RggGrid* g) {
+  if (n < 2 || !(mean_degree > 0)) return false;
+  double r = std::sqrt(mean_degree / (3.141592653589793 * (double)n));
+  if (!(r < 0.5)) return false;
+  uint64_t R = (uint64_t)(r * 2147483648.0);
+  if (R < 1) R = 1;
+  g->R2 = R * R;
+  g->cell = (uint32_t)R;
+  g->G = (uint32_t)((2147483648ull + R - 1) / R);
+  return true;
+}
+
+__global__ void rgg_keys_kernel(uint64_t s0, uint32_t n, RggGrid gr, uint64_t* keys) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t x, y;
+    rgg_point(s0, i, &x, &y);
+    uint64_t c = (uint64_t)(y / gr.cell) * gr.G + x / gr.cell;
+    keys[i] = (c << 32) | i;
+  }
+}
+
+__global__ void rgg_cells_kernel(const uint64_t* keys, uint32_t n, uint64_t ncell, uint32_t* cstart) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c <= ncell; c += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+      uint64_t mid = (lo + hi) >> 1;
+      if ((keys[mid] >> 32) < c) lo = mid + 1; else hi = mid;
+    }
+    cstart[c] = (uint32_t)lo;
+  }
+}
+
+// One thread per point: scans the 3x3 cells around it and emits (i, j) for j > i.
+__global__ void rgg_edges_kernel(uint64_t s0, uint32_t n, RggGrid gr, const uint64_t* keys, const uint32_t* cstart,
+                                 int2* out, unsigned long long cap, unsigned long long* count) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t x, y;
+    rgg_point(s0, i, &x, &y);
+    int64_t cx = x / gr.cell, cy = y / gr.cell;
+    for (int64_t yy = cy - 1; yy <= cy + 1; ++yy) {
+      if (yy < 0 || yy >= gr.G) continue;
+      for (int64_t xx = cx - 1; xx <= cx + 1; ++xx) {
+        if (xx < 0 || xx >= gr.G) continue;
+        uint64_t c = (uint64_t)yy * gr.G + (uint64_t)xx;
+        for (uint32_t k = cstart[c]; k < cstart[c + 1]; ++k) {
+          uint32_t j = (uint32_t)(keys[k] & 0xffffffffu);
+          if (j <= i) continue;
+          uint32_t xj, yj;
+          rgg_point(s0, j, &xj, &yj);
+          int64_t dx = (int64_t)xj - (int64_t)x, dy = (int64_t)yj - (int64_t)y;
+          if ((uint64_t)(dx * dx) + (uint64_t)(dy * dy) <= gr.R2) {
+            unsigned long long at = atomicAdd(count, 1ull);
+            if (at < cap) out[at] = make_int2((int32_t)i, (int32_t)j);
+          }
+        }
+      }
+    }
+  }
+}
+
 }  // namespace atc
 
 using namespace atc;
+
+extern "C" atc_status atc_gen_rgg_host(uint32_t n, double mean_degree, uint64_t seed, int32_t* out,
+                                       uint64_t capacity, uint64_t* n_out, int nthreads) {
+  ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
+  RggGrid gr;
+  ATC_CHECK_ARG(rgg_grid(n, mean_degree, &gr), "need n >= 2 and 0 < mean degree with radius < 0.5");
+  uint64_t s0 = mix64(seed);
+  std::vector<uint32_t> xs(n), ys(n);
+  for (uint64_t i = 0; i < n; ++i) rgg_point(s0, i, &xs[i], &ys[i]);
+  uint64_t ncell = (uint64_t)gr.G * gr.G;
+  std::vector<uint32_t> cnt(ncell + 1, 0), order(n);
+  auto cell_of = [&](uint64_t i) { return (uint64_t)(ys[i] / gr.cell) * gr.G + xs[i] / gr.cell; };
+  for (uint64_t i = 0; i < n; ++i) cnt[cell_of(i) + 1]++;
+  for (uint64_t c = 0; c < ncell; ++c) cnt[c + 1] += cnt[c];
+  std::vector<uint32_t> cur(cnt.begin(), cnt.end() - 1);
+  for (uint64_t i = 0; i < n; ++i) order[cur[cell_of(i)]++] = (uint32_t)i;  // ids ascending within a cell
+  if (nthreads < 1) nthreads = 1;
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> part(nthreads);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t)
+    th.emplace_back([&, t] {
+      uint64_t b = (uint64_t)n * t / nthreads, e = (uint64_t)n * (t + 1) / nthreads;
+      for (uint64_t i = b; i < e; ++i) {
+        int64_t cx = xs[i] / gr.cell, cy = ys[i] / gr.cell;
+        for (int64_t yy = cy - 1; yy <= cy + 1; ++yy) {
+          if (yy < 0 || yy >= gr.G) continue;
+          for (int64_t xx = cx - 1; xx <= cx + 1; ++xx) {
+            if (xx < 0 || xx >= gr.G) continue;
+            uint64_t c = (uint64_t)yy * gr.G + (uint64_t)xx;
+            for (uint32_t k = cnt[c]; k < cnt[c + 1]; ++k) {
+              uint32_t j = order[k];
+              if (j <= i) continue;
+              int64_t dx = (int64_t)xs[j] - (int64_t)xs[i], dy = (int64_t)ys[j] - (int64_t)ys[i];
+              if ((uint64_t)(dx * dx) + (uint64_t)(dy * dy) <= gr.R2) part[t].emplace_back((int32_t)i, (int32_t)j);
+            }
+          }
+        }
+      }
+    });
+  for (auto& x : th) x.join();
+  uint64_t total = 0;
+  for (auto& p : part) total += p.size();
+  *n_out = total;
+  if (!out) return ATC_OK;
+  if (total > capacity) {
+    set_error("RGG has %llu edges, capacity %llu", (unsigned long long)total, (unsigned long long)capacity);
+    return ATC_ERR_INVALID;
+  }
+  std::vector<std::pair<int32_t, int32_t>> all;
+  all.reserve(total);
+  for (auto& p : part) all.insert(all.end(), p.begin(), p.end());
+  std::sort(all.begin(), all.end());
+  for (uint64_t k = 0; k < total; ++k) {
+    out[2 * k] = all[k].first;
+    out[2 * k + 1] = all[k].second;
+  }
+  return ATC_OK;
+}
+
+extern "C" atc_status atc_gen_rgg_device(uint32_t n, double mean_degree, uint64_t seed, int32_t* out_dev,
+                                         uint64_t capacity, uint64_t* n_out, atc_stream st) {
+  ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
+  RggGrid gr;
+  ATC_CHECK_ARG(rgg_grid(n, mean_degree, &gr), "need n >= 2 and 0 < mean degree with radius < 0.5");
+  cudaStream_t s = as_stream(st);
+  uint64_t s0 = mix64(seed);
+  uint64_t ncell = (uint64_t)gr.G * gr.G;
+  DevBuf<uint64_t> ka, kb;
+  DevBuf<uint32_t> cstart;
+  DevBuf<unsigned long long> cnt;
+  ATC_TRY(ka.alloc(n, s));
+  ATC_TRY(kb.alloc(n, s));
+  ATC_TRY(cstart.alloc(ncell + 1, s));
+  ATC_TRY(cnt.alloc(1, s));
+  ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), s));
+  rgg_keys_kernel<<<grid_for(n, 256), 256, 0, s>>>(s0, n, gr, ka.p);
+  ATC_CK(cudaGetLastError());
+  uint64_t* a = ka.p;
+  uint64_t* b = kb.p;
+  int cb = 1;
+  while ((1ull << cb) < ncell + 1) ++cb;
+  ATC_TRY(sort_keys_u64(a, b, n, 0, 32 + cb, s));
+  rgg_cells_kernel<<<grid_for(ncell + 1, 256), 256, 0, s>>>(a, n, ncell, cstart.p);
+  rgg_edges_kernel<<<grid_for(n, 256), 256, 0, s>>>(s0, n, gr, a, cstart.p, reinterpret_cast<int2*>(out_dev),
+                                                    out_dev ? capacity : 0, cnt.p);
+  ATC_CK(cudaGetLastError());
+  unsigned long long h = 0;
+  ATC_CK(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  *n_out = h;
+  if (out_dev && h > capacity) {
+    set_error("RGG has %llu edges, capacity %llu", h, (unsigned long long)capacity);
+    return ATC_ERR_INVALID;
+  }
+  return ATC_OK;
+}
 
 extern "C" atc_status atc_gen_rmat_host(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm,
                                         uint32_t c_ppm, uint64_t seed, int32_t* out, int nthreads) {

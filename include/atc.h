@@ -121,6 +121,15 @@ atc_status atc_gen_rmat_host(uint32_t scale, uint32_t edge_factor, uint32_t a_pp
                              uint32_t c_ppm, uint64_t seed, int32_t* out_pairs, int nthreads);
 atc_status atc_gen_rmat_device(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm,
                                uint32_t c_ppm, uint64_t seed, int32_t* out_pairs_dev, atc_stream s);
+/* 2-D random geometric graph: n points with 31-bit fixed-point coordinates in the unit
+   square, i and j adjacent iff their distance is <= sqrt(mean_degree / (pi n)) (integer
+   test).  Writes each edge once as (i, j), i < j: sorted on the host; in no particular
+   order on the device.  *n_out = the number of edges; with out == NULL only counts.
+   ATC_ERR_INVALID if it exceeds `capacity` (pairs). */
+atc_status atc_gen_rgg_host(uint32_t n, double mean_degree, uint64_t seed, int32_t* out_pairs, uint64_t capacity,
+                            uint64_t* n_out, int nthreads);
+atc_status atc_gen_rgg_device(uint32_t n, double mean_degree, uint64_t seed, int32_t* out_pairs_dev,
+                              uint64_t capacity, uint64_t* n_out, atc_stream s);
 /* Drops self-loops and repeats; writes each undirected edge once as (min,max) sorted,
    or, with symmetric != 0, both directions sorted by (src,dst).  Capacity of `out`:
    2*n_pairs pairs when symmetric, else n_pairs. */

@@ -513,6 +513,52 @@ uint64_t orc_kclique(const int32_t* pairs, uint64_t np, int k, int nthreads) {
   return r;
 }
 
+// k-clique count restricted to cliques whose smallest vertex u satisfies u % stride ==
+// phase: the bounded sample the CPU baseline times.  *edges_out = edges out of the
+// sampled u (in the id orientation the count walks).
+uint64_t orc_kclique_sample(const int32_t* pairs, uint64_t np, int k, int64_t stride, int64_t phase, int nthreads,
+                            int64_t* edges_out) {
+  Adj g = build_adj(pairs, np);
+  std::vector<int64_t> hi(g.n);
+  for (int64_t v = 0; v < g.n; ++v) {
+    const int32_t* b = g.nbr.data() + g.off[v];
+    const int32_t* e = g.nbr.data() + g.off[v + 1];
+    hi[v] = std::upper_bound(b, e, (int32_t)v) - b;
+  }
+  int64_t nsamp = phase < g.n ? (g.n - phase + stride - 1) / stride : 0;
+  std::vector<uint64_t> part(std::max(1, nthreads), 0);
+  std::vector<int64_t> epart(std::max(1, nthreads), 0);
+  parallel_for(nsamp, nthreads, 16, [&](int64_t i, int t) {
+    int64_t u = phase + i * stride;
+    std::vector<std::vector<int32_t>> lv(k);
+    lv[0].assign(g.nbr.begin() + g.off[u] + hi[u], g.nbr.begin() + g.off[u + 1]);
+    epart[t] += (int64_t)lv[0].size();
+    struct Rec {
+      const Adj& g; const std::vector<int64_t>& hi; std::vector<std::vector<int32_t>>& lv; int k;
+      uint64_t go(int depth) {
+        const auto& c = lv[depth - 1];
+        if (depth == k - 1) return c.size();
+        uint64_t s = 0;
+        for (int32_t v : c) {
+          auto& nxt = lv[depth];
+          nxt.clear();
+          const int32_t* b = g.nbr.data() + g.off[v] + hi[v];
+          const int32_t* e = g.nbr.data() + g.off[v + 1];
+          std::set_intersection(c.begin(), c.end(), b, e, std::back_inserter(nxt));
+          if ((int)nxt.size() >= k - 1 - depth) s += go(depth + 1);
+        }
+        return s;
+      }
+    } rec{g, hi, lv, k};
+    part[t] += k >= 3 ? rec.go(1) : 0;
+  });
+  uint64_t r = 0;
+  int64_t e = 0;
+  for (size_t t = 0; t < part.size(); ++t) { r += part[t]; e += epart[t]; }
+  *edges_out = e;
+  return r;
+}
+
 // costFuncCal (tools/costFuncCal.cpp:15-88): out = {idPartCost, degreePartCost, lpPartCost}.
 void orc_costfunc(const int32_t* pairs, uint64_t np, int k, float* out) {
   unsigned edgeNum = (unsigned)np;

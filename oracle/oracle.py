@@ -42,6 +42,8 @@ def lib():
         L.orc_aorder.argtypes = [_P, C.c_uint64, _P, _P, _P]
         L.orc_kclique.restype = C.c_uint64
         L.orc_kclique.argtypes = [_P, C.c_uint64, C.c_int, C.c_int]
+        L.orc_kclique_sample.restype = C.c_uint64
+        L.orc_kclique_sample.argtypes = [_P, C.c_uint64, C.c_int, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_int64)]
         L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
         L.orc_hu_csr.restype = C.c_int64
@@ -135,6 +137,14 @@ def aorder(pairs):
 def kclique(pairs, k, nthreads=None):
     p = _pairs(pairs)
     return lib().orc_kclique(_ptr(p), p.shape[0], k, nthreads or nthreads_default())
+
+
+def kclique_sample(pairs, k, stride, phase=0, nthreads=None):
+    """(k-cliques whose smallest vertex is phase, phase+stride, ..., edges out of those)."""
+    p = _pairs(pairs)
+    e = C.c_int64(0)
+    c = lib().orc_kclique_sample(_ptr(p), p.shape[0], k, stride, phase, nthreads or nthreads_default(), C.byref(e))
+    return c, e.value
 
 
 def costfunc(pairs, k):

@@ -64,3 +64,12 @@ def test_argument_checks_without_gpu():
 def test_csr_free_is_idempotent():
     st = atc.CSRStruct()
     assert atc.lib().atc_csr_free(C.byref(st)) == 0
+
+
+def test_rgg_host_deterministic_and_geometric():
+    a = atc.gen_rgg(4096, 16.0, seed=5, nthreads=1)
+    b = atc.gen_rgg(4096, 16.0, seed=5, nthreads=5)
+    assert np.array_equal(a, b)
+    assert np.all(a[:, 0] < a[:, 1])
+    mean_deg = 2 * a.shape[0] / 4096
+    assert 13.0 < mean_deg < 17.0

@@ -295,3 +295,23 @@ def test_cli_dropins(tmp_path):
     r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout
+
+
+def test_rgg_device_matches_host():
+    import ctypes as C
+    import torch
+    n = 1 << 14
+    host = atc.gen_rgg(n, 32.0, 3)
+    cnt = C.c_uint64(0)
+    buf = torch.empty((host.shape[0] + 100, 2), dtype=torch.int32, device="cuda")
+    assert atc.lib().atc_gen_rgg_device(n, 32.0, 3, buf.data_ptr(), buf.shape[0], C.byref(cnt), None) == 0
+    dev = buf[: cnt.value].cpu().numpy()
+    order = np.lexsort((dev[:, 1], dev[:, 0]))
+    assert np.array_equal(dev[order], host)
+
+
+@pytest.mark.parametrize("k", [3, 4, 5, 6, 7])
+def test_kcl_rgg_matches_oracle(k):
+    g = atc.gen_rgg(1 << 14, 32.0, 2)
+    csr = atc.pretc(g, atc.Dir.ADIRECTION)
+    assert atc.kcl(csr, k)[0] == oracle.kclique(g, k)
