@@ -10,6 +10,9 @@
 //   C0 = N+(u) ∩ N+(v);  C(l+1) = C(l) ∩ N+(w) for the w chosen from C(l);
 //   with k-1 vertices chosen, every element of the current candidate set completes a
 //   k-clique, so the last level is counted, never stored.
+// When |C0| <= 64 (every RGG edge, most R-MAT edges) the warp instead builds the 64-bit
+// successor masks of the DAG induced on C0 with one ballot per member, and each lane
+// counts the remaining (k-2)-cliques of its first member with AND / popc on registers.
 //
 // Orientation is acyclic, so every k-clique is found once, from its first two vertices
 // in orientation order — the same count kcl_gpu_solver accumulates.  Intersections:
@@ -50,6 +53,39 @@ __device__ __forceinline__ int warp_intersect(const int32_t* P, int np, const in
 
 constexpr int kKcWarps = 8;
 constexpr int kMaxK = 16;
+constexpr int kMaskMax = 64;  // candidate sets up to this size use the bitmask path
+
+// d-cliques inside `mask` of the DAG whose successor sets (within C0) are adj[]:
+// cliq(1, M) = |M|, cliq(d, M) = sum_{i in M} cliq(d-1, M & adj[i]).  Iterative, one
+// lane, an explicit stack of (remaining mask, candidate mask) per depth.
+__device__ __forceinline__ unsigned long long mask_cliques(const unsigned long long* adj, unsigned long long mask,
+                                                           int d) {
+  if (d <= 0) return 1ull;
+  if (d == 1) return (unsigned long long)__popcll(mask);
+  unsigned long long total = 0;
+  unsigned long long rem[kMaxK], cand[kMaxK];
+  int top = 0;
+  rem[0] = mask;
+  cand[0] = mask;
+  while (top >= 0) {
+    if (rem[top] == 0) {
+      --top;
+      continue;
+    }
+    int i = __ffsll(rem[top]) - 1;
+    rem[top] &= rem[top] - 1;
+    unsigned long long nm = cand[top] & adj[i];
+    int left = d - 1 - top;  // vertices still to choose after i
+    if (left == 1) {
+      total += (unsigned long long)__popcll(nm);
+    } else if (__popcll(nm) >= left) {
+      ++top;
+      rem[top] = nm;
+      cand[top] = nm;
+    }
+  }
+  return total;
+}
 
 __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, const int32_t* cols, const int32_t* esrc,
                                                           int64_t m, int k, int cap, int32_t* scratch,
@@ -59,6 +95,7 @@ __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, 
   const int64_t warps = (int64_t)gridDim.x * kKcWarps;
   const int levels = k - 2;
   int32_t* buf = scratch + gw * (int64_t)levels * cap;
+  __shared__ unsigned long long adjm[kKcWarps][kMaskMax];
   unsigned long long cnt = 0, bytes = 0;
   int size[kMaxK];
   int idx[kMaxK];
@@ -74,6 +111,26 @@ __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, 
       continue;
     }
     if (c0 < levels) continue;  // not enough candidates for k-2 more vertices
+    if (c0 <= kMaskMax) {
+      // bitmask path: adjm[w][i] = members of C0 that are successors of C0[i]
+      for (int i = 0; i < c0; ++i) {
+        int32_t x = buf[i];
+        int64_t xb = off[x], xd = off[x + 1] - xb;
+        bytes += 4ull * (unsigned long long)xd;
+        bool h0 = lane < c0 && kc_has(cols + xb, xd, buf[lane]);
+        bool h1 = lane + 32 < c0 && kc_has(cols + xb, xd, buf[lane + 32]);
+        unsigned lo = __ballot_sync(0xffffffffu, h0), hi = __ballot_sync(0xffffffffu, h1);
+        if (lane == 0) adjm[w][i] = ((unsigned long long)hi << 32) | lo;
+      }
+      __syncwarp();
+      // (k-2)-cliques of the DAG on C0: lane i takes the ones whose first vertex is C0[i]
+      unsigned long long part = 0;
+      for (int i = lane; i < c0; i += 32) part += mask_cliques(adjm[w], adjm[w][i], levels - 1);
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      cnt += part;
+      __syncwarp();
+      continue;
+    }
     size[0] = c0;
     idx[0] = 0;
     int l = 0;  // level whose candidates are being chosen from

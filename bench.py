@@ -53,10 +53,8 @@ def parse():
     ap.add_argument("--kernels", default="hu,bisson,fox,tricore", help="families timed besides the headline")
     ap.add_argument("--mode", default="tc", choices=["tc", "kcl"],
                     help="tc: the headline (BASELINE config 2); kcl: k-clique counts (config 3)")
-    ap.add_argument("--kcl-scale", type=int, default=20, help="R-MAT scale of the k-clique graph")
-    ap.add_argument("--rgg-log2n", type=int, default=20, help="log2 of the RGG point count")
-    ap.add_argument("--kmin", type=int, default=4)
-    ap.add_argument("--kmax", type=int, default=7)
+    ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-4,rmat:16:4-7",
+                    help="comma list of kind:log2size:kmin-kmax (kind rmat or rgg)")
     return ap.parse_args()
 
 
@@ -348,7 +346,8 @@ def run_ours(a):
 
 
 def run_kcl(a):
-    """k-clique counting (BASELINE config 3): R-MAT and RGG, A-direction, k = kmin..kmax."""
+    """k-clique counting (BASELINE config 3): R-MAT and 2-D RGG graphs, A-direction."""
+    import ctypes as C
     import torch
     import atc
     import oracle
@@ -356,43 +355,48 @@ def run_kcl(a):
     atc.init(0)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
-    graphs = []
-    # R-MAT scale s, edge factor 16
-    nraw = a.edge_factor << a.kcl_scale
-    raw = torch.empty((nraw, 2), dtype=torch.int32, device="cuda")
-    assert atc.lib().atc_gen_rmat_device(a.kcl_scale, a.edge_factor, *atc.GRAPH500, a.seed, raw.data_ptr(), sp) == 0
-    graphs.append(("R-MAT scale %d edge factor %d" % (a.kcl_scale, a.edge_factor), raw, nraw))
-    # RGG, n = 2^rgg_log2n, mean degree 32
-    import ctypes as C
-    n = 1 << a.rgg_log2n
-    cnt = C.c_uint64(0)
-    cap = n * 20
-    rg = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
-    assert atc.lib().atc_gen_rgg_device(n, 32.0, a.seed, rg.data_ptr(), cap, C.byref(cnt), sp) == 0
-    graphs.append(("RGG n=2^%d mean degree 32" % a.rgg_log2n, rg, int(cnt.value)))
     out = []
-    for name, dev, npairs in graphs:
+    for spec in a.kcl_graphs.split(","):
+        kind, lg, kr = spec.split(":")
+        lg = int(lg)
+        kmin, kmax = (int(x) for x in kr.split("-"))
+        if kind == "rmat":
+            npairs = a.edge_factor << lg
+            dev = torch.empty((npairs, 2), dtype=torch.int32, device="cuda")
+            assert atc.lib().atc_gen_rmat_device(lg, a.edge_factor, *atc.GRAPH500, a.seed, dev.data_ptr(), sp) == 0
+            name = "R-MAT scale %d edge factor %d" % (lg, a.edge_factor)
+        else:
+            n = 1 << lg
+            cnt = C.c_uint64(0)
+            cap = n * 20
+            dev = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+            assert atc.lib().atc_gen_rgg_device(n, 32.0, a.seed, dev.data_ptr(), cap, C.byref(cnt), sp) == 0
+            npairs = int(cnt.value)
+            name = "RGG n=2^%d mean degree 32" % lg
         csr = atc.pretc_device(dev.data_ptr(), npairs, atc.Dir.ADIRECTION, stream=sp)
         host_pairs = dev[:npairs].cpu().numpy()
+        del dev
         rec = {"graph": name, "n": csr.n, "m": csr.m, "max_outdeg": csr.max_outdeg, "k": {}}
-        for k in range(a.kmin, a.kmax + 1):
+        for k in range(kmin, kmax + 1):
             atc.kcl(csr, k, stream=sp)  # warm-up
             times = []
             for _ in range(max(1, a.steps)):
                 c, st = atc.kcl(csr, k, stream=sp)
                 times.append(st.kernel_ms)
             ms = statistics.mean(times)
-            # CPU baseline: oracle DFS over a strided sample of first vertices
-            stride = max(1, csr.n // 4096)
-            t0 = time.perf_counter()
-            cc, ce = oracle.kclique_sample(host_pairs, k, stride, 0)
-            dt = time.perf_counter() - t0
-            rec["k"][str(k)] = {"cliques": c, "ms": ms, "cliques_per_s": c / (ms * 1e-3),
-                                "edges_per_s": csr.m / (ms * 1e-3), "alg_bytes": st.alg_bytes,
-                                "achieved_gbs": st.alg_bytes / (ms * 1e-3) / 1e9,
-                                "cpu_sample": {"stride": stride, "edges": ce, "seconds": dt,
-                                               "edges_per_s": ce / dt if dt > 0 else None,
-                                               "cores": os.cpu_count()}}
+            entry = {"cliques": c, "ms": ms, "cliques_per_s": c / (ms * 1e-3), "edges_per_s": csr.m / (ms * 1e-3),
+                     "alg_bytes": st.alg_bytes, "achieved_gbs": st.alg_bytes / (ms * 1e-3) / 1e9}
+            if not a.no_cpu_baseline:
+                # CPU baseline: the oracle's DFS over a strided sample of first vertices
+                stride = max(1, csr.n // 2048)
+                t0 = time.perf_counter()
+                _, ce = oracle.kclique_sample(host_pairs, k, stride, 0)
+                dt = time.perf_counter() - t0
+                entry["cpu_sample"] = {"stride": stride, "edges": ce, "seconds": dt,
+                                       "edges_per_s": ce / dt if dt > 0 else None, "cores": os.cpu_count(),
+                                       "kind": "port"}
+            rec["k"][str(k)] = entry
+            print(json.dumps({"partial": name, "k": k, **entry}), file=sys.stderr, flush=True)
         out.append(rec)
         csr.free()
     peak, kind = measured_peak()

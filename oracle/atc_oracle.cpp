@@ -465,98 +465,105 @@ int orc_aorder(const int32_t* pairs, uint64_t np, int32_t* lookup, int32_t* norm
   return ORC_OK;
 }
 
-// k-clique count of the simple graph (k >= 3), the quantity kcl_gpu_solver
-// accumulates (k-clique/kcl.cu:147-215): embeddings of the DAG extended level by
-// level by vertices adjacent to every member (is_all_connected_dag), counted at
-// level k-2.  Restated as a depth-first intersection over N+(v) = {w > v}; the
-// count does not depend on the acyclic orientation.
+// k-cliques (k >= 3) of the simple graph, the quantity kcl_gpu_solver accumulates
+// (k-clique/kcl.cu:147-215): embeddings of a DAG extended level by level by vertices
+// adjacent to every member (is_all_connected_dag), counted at level k-2.  Restated as
+// a depth-first intersection over a degree-ranked DAG (rank by (degree, id); N+(r) =
+// higher-ranked neighbours), which keeps hub candidate sets small; the count does not
+// depend on the acyclic orientation.
+namespace {
+
+struct RankDag {
+  int64_t n = 0;
+  std::vector<int64_t> off;
+  std::vector<int32_t> nbr;  // per rank, higher ranks, sorted
+};
+
+RankDag rank_dag(const Adj& g, int nthreads) {
+  RankDag d;
+  d.n = g.n;
+  std::vector<int32_t> order(g.n), rank(g.n);
+  for (int64_t v = 0; v < g.n; ++v) order[v] = (int32_t)v;
+  std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    int64_t da = g.off[a + 1] - g.off[a], db = g.off[b + 1] - g.off[b];
+    return da < db || (da == db && a < b);
+  });
+  for (int64_t r = 0; r < g.n; ++r) rank[order[r]] = (int32_t)r;
+  std::vector<int64_t> len(g.n + 1, 0);
+  for (int64_t v = 0; v < g.n; ++v)
+    for (int64_t j = g.off[v]; j < g.off[v + 1]; ++j)
+      if (rank[g.nbr[j]] > rank[v]) len[rank[v] + 1]++;
+  d.off.assign(g.n + 1, 0);
+  for (int64_t r = 0; r < g.n; ++r) d.off[r + 1] = d.off[r] + len[r + 1];
+  d.nbr.resize(d.off[g.n]);
+  parallel_for(g.n, nthreads, 1024, [&](int64_t v, int) {
+    int32_t r = rank[v];
+    int64_t at = d.off[r];
+    for (int64_t j = g.off[v]; j < g.off[v + 1]; ++j)
+      if (rank[g.nbr[j]] > r) d.nbr[at++] = rank[g.nbr[j]];
+    std::sort(d.nbr.begin() + d.off[r], d.nbr.begin() + d.off[r + 1]);
+  });
+  return d;
+}
+
+// k-cliques whose lowest-ranked vertex is r.
+uint64_t cliques_from(const RankDag& d, int64_t r, int k) {
+  std::vector<std::vector<int32_t>> lv(k);
+  lv[0].assign(d.nbr.begin() + d.off[r], d.nbr.begin() + d.off[r + 1]);
+  struct Rec {
+    const RankDag& d; std::vector<std::vector<int32_t>>& lv; int k;
+    uint64_t go(int depth) {  // depth chosen vertices; candidates lv[depth-1]
+      const auto& c = lv[depth - 1];
+      if (depth == k - 1) return c.size();
+      uint64_t s = 0;
+      for (int32_t v : c) {
+        auto& nxt = lv[depth];
+        nxt.clear();
+        std::set_intersection(c.begin(), c.end(), d.nbr.begin() + d.off[v], d.nbr.begin() + d.off[v + 1],
+                              std::back_inserter(nxt));
+        if ((int)nxt.size() >= k - 1 - depth) s += go(depth + 1);
+      }
+      return s;
+    }
+  } rec{d, lv, k};
+  return rec.go(1);
+}
+
+}  // namespace
+
 uint64_t orc_kclique(const int32_t* pairs, uint64_t np, int k, int nthreads) {
   Adj g = build_adj(pairs, np);
   if (k < 1) return 0;
   if (k == 1) return (uint64_t)g.n;
   if (k == 2) return (uint64_t)g.nbr.size() / 2;
-  std::vector<int64_t> hi(g.n);
-  for (int64_t v = 0; v < g.n; ++v) {
-    const int32_t* b = g.nbr.data() + g.off[v];
-    const int32_t* e = g.nbr.data() + g.off[v + 1];
-    hi[v] = std::upper_bound(b, e, (int32_t)v) - b;   // start of N+(v)
-  }
+  RankDag d = rank_dag(g, nthreads);
   std::vector<uint64_t> part(std::max(1, nthreads), 0);
-  parallel_for(g.n, nthreads, 64, [&](int64_t u, int t) {
-    // levels[l] holds the candidate set after l+1 chosen vertices
-    std::vector<std::vector<int32_t>> lv(k);
-    lv[0].assign(g.nbr.begin() + g.off[u] + hi[u], g.nbr.begin() + g.off[u + 1]);
-    uint64_t cnt = 0;
-    // recursive lambda via explicit function object
-    struct Rec {
-      const Adj& g; const std::vector<int64_t>& hi; std::vector<std::vector<int32_t>>& lv; int k;
-      uint64_t go(int depth) {  // depth chosen vertices so far; candidates lv[depth-1]
-        const auto& c = lv[depth - 1];
-        if (depth == k - 1) return c.size();
-        uint64_t s = 0;
-        for (int32_t v : c) {
-          auto& nxt = lv[depth];
-          nxt.clear();
-          const int32_t* b = g.nbr.data() + g.off[v] + hi[v];
-          const int32_t* e = g.nbr.data() + g.off[v + 1];
-          std::set_intersection(c.begin(), c.end(), b, e, std::back_inserter(nxt));
-          if ((int)nxt.size() >= k - 1 - depth) s += go(depth + 1);
-        }
-        return s;
-      }
-    } rec{g, hi, lv, k};
-    cnt = rec.go(1);
-    part[t] += cnt;
-  });
-  uint64_t r = 0;
-  for (auto x : part) r += x;
-  return r;
+  parallel_for(d.n, nthreads, 64, [&](int64_t r, int t) { part[t] += cliques_from(d, r, k); });
+  uint64_t total = 0;
+  for (auto x : part) total += x;
+  return total;
 }
 
-// k-clique count restricted to cliques whose smallest vertex u satisfies u % stride ==
-// phase: the bounded sample the CPU baseline times.  *edges_out = edges out of the
-// sampled u (in the id orientation the count walks).
+// The same count restricted to cliques whose lowest-ranked vertex has rank r with
+// r % stride == phase: the bounded sample the CPU baseline times.  *edges_out = edges
+// out of the sampled ranks.
 uint64_t orc_kclique_sample(const int32_t* pairs, uint64_t np, int k, int64_t stride, int64_t phase, int nthreads,
                             int64_t* edges_out) {
   Adj g = build_adj(pairs, np);
-  std::vector<int64_t> hi(g.n);
-  for (int64_t v = 0; v < g.n; ++v) {
-    const int32_t* b = g.nbr.data() + g.off[v];
-    const int32_t* e = g.nbr.data() + g.off[v + 1];
-    hi[v] = std::upper_bound(b, e, (int32_t)v) - b;
-  }
-  int64_t nsamp = phase < g.n ? (g.n - phase + stride - 1) / stride : 0;
+  RankDag d = rank_dag(g, nthreads);
+  int64_t nsamp = phase < d.n ? (d.n - phase + stride - 1) / stride : 0;
   std::vector<uint64_t> part(std::max(1, nthreads), 0);
   std::vector<int64_t> epart(std::max(1, nthreads), 0);
   parallel_for(nsamp, nthreads, 16, [&](int64_t i, int t) {
-    int64_t u = phase + i * stride;
-    std::vector<std::vector<int32_t>> lv(k);
-    lv[0].assign(g.nbr.begin() + g.off[u] + hi[u], g.nbr.begin() + g.off[u + 1]);
-    epart[t] += (int64_t)lv[0].size();
-    struct Rec {
-      const Adj& g; const std::vector<int64_t>& hi; std::vector<std::vector<int32_t>>& lv; int k;
-      uint64_t go(int depth) {
-        const auto& c = lv[depth - 1];
-        if (depth == k - 1) return c.size();
-        uint64_t s = 0;
-        for (int32_t v : c) {
-          auto& nxt = lv[depth];
-          nxt.clear();
-          const int32_t* b = g.nbr.data() + g.off[v] + hi[v];
-          const int32_t* e = g.nbr.data() + g.off[v + 1];
-          std::set_intersection(c.begin(), c.end(), b, e, std::back_inserter(nxt));
-          if ((int)nxt.size() >= k - 1 - depth) s += go(depth + 1);
-        }
-        return s;
-      }
-    } rec{g, hi, lv, k};
-    part[t] += k >= 3 ? rec.go(1) : 0;
+    int64_t r = phase + i * stride;
+    epart[t] += d.off[r + 1] - d.off[r];
+    part[t] += k >= 3 ? cliques_from(d, r, k) : 0;
   });
-  uint64_t r = 0;
+  uint64_t total = 0;
   int64_t e = 0;
-  for (size_t t = 0; t < part.size(); ++t) { r += part[t]; e += epart[t]; }
+  for (size_t t = 0; t < part.size(); ++t) { total += part[t]; e += epart[t]; }
   *edges_out = e;
-  return r;
+  return total;
 }
 
 // costFuncCal (tools/costFuncCal.cpp:15-88): out = {idPartCost, degreePartCost, lpPartCost}.
