@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--kernels", default="hu,bisson,fox,tricore", help="families timed besides the headline")
     ap.add_argument("--mode", default="tc", choices=["tc", "kcl"],
                     help="tc: the headline (BASELINE config 2); kcl: k-clique counts (config 3)")
-    ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-4,rmat:16:4-7",
+    ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-5,rmat:14:6-7",
                     help="comma list of kind:log2size:kmin-kmax (kind rmat or rgg)")
     return ap.parse_args()
 
