@@ -63,7 +63,10 @@ class Tuning(C.Structure):
         ("fox_rearrange", C.c_int32),
         ("fox_work_per_thread", C.c_int32),
         ("tricore_blocks", C.c_int32),
-        ("reserved", C.c_int32 * 9),
+        ("bisson_warp_max", C.c_int32),
+        ("bisson_warp_chunk", C.c_int32),
+        ("bisson_block_chunk", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -120,6 +123,8 @@ _SIGS = {
     "atc_gen_rmat_device": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P]),
     "atc_gen_rgg_host": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, _P, C.c_uint64, C.POINTER(C.c_uint64), C.c_int]),
     "atc_gen_rgg_device": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, _P, C.c_uint64, C.POINTER(C.c_uint64), _P]),
+    "atc_gen_chunglu_device": (C.c_int, [C.c_uint32, C.c_double, C.c_double, C.c_uint64, _P, C.c_uint64,
+                                          C.POINTER(C.c_uint64), _P]),
     "atc_simplify_host": (C.c_int, [_P, C.c_uint64, C.c_int, _P, C.POINTER(C.c_uint64)]),
     "atc_pretc": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
     "atc_pretc_device": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
@@ -130,6 +135,13 @@ _SIGS = {
     "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_tc_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_uint64), _P]),
     "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
+    "atc_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "atc_batch_reserve": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _P]),
+    "atc_batch_add": (C.c_int, [C.c_void_p, C.POINTER(CSRStruct), C.POINTER(C.c_int32), _P]),
+    "atc_batch_run": (C.c_int, [C.c_void_p, C.POINTER(Tuning), _P, C.POINTER(StatsStruct), _P]),
+    "atc_batch_tune": (C.c_int, [C.c_void_p, _P, C.c_int32, C.POINTER(C.c_int32), _P, _P]),
+    "atc_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "atc_batch_destroy": (C.c_int, [C.c_void_p]),
     "atc_costfunc": (C.c_int, [_P, C.c_uint64, C.c_int32, _P, _P]),
     "atc_verification": (C.c_int, [_P, C.c_uint64, _P, _P]),
 }
@@ -323,6 +335,67 @@ def kcl(csr: CSR, k, stream=None):
     st = StatsStruct()
     _check(lib().atc_kcl(C.byref(csr.struct), k, C.byref(cnt), C.byref(st), stream))
     return cnt.value, _stats(st)
+
+
+class Batch:
+    """Many graphs counted in one CUDA-graph replay (atc_batch_*)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(lib().atc_batch_create(C.byref(h)))
+        self._h = h
+
+    def reserve(self, n, m, stream=None):
+        _check(lib().atc_batch_reserve(self._h, n, m, stream))
+
+    def add(self, csr: CSR, stream=None):
+        idx = C.c_int32(0)
+        _check(lib().atc_batch_add(self._h, C.byref(csr.struct), C.byref(idx), stream))
+        return idx.value
+
+    def info(self):
+        g, n, m = C.c_int32(0), C.c_int64(0), C.c_int64(0)
+        _check(lib().atc_batch_info(self._h, C.byref(g), C.byref(n), C.byref(m)))
+        return g.value, n.value, m.value
+
+    def run(self, tuning=None, stream=None):
+        g = self.info()[0]
+        counts = np.zeros(max(g, 1), dtype=np.uint64)
+        st = StatsStruct()
+        _check(lib().atc_batch_run(self._h, _tuning(tuning), _ptr(counts), C.byref(st), stream))
+        return counts[:g], _stats(st)
+
+    def tune(self, candidates, stream=None):
+        arr = (Tuning * len(candidates))()
+        for i, c in enumerate(candidates):
+            for k, v in c.items():
+                setattr(arr[i], k, v)
+        best = C.c_int32(0)
+        ms = np.zeros(len(candidates), dtype=np.float32)
+        _check(lib().atc_batch_tune(self._h, C.cast(arr, C.c_void_p), len(candidates), C.byref(best), _ptr(ms), stream))
+        return best.value, ms
+
+    def free(self):
+        if self._h:
+            lib().atc_batch_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def gen_chunglu_device(n, gamma, mean_degree, seed, stream=None):
+    """Chung-Lu graph generated on the device; returns a torch int32 (m, 2) cuda tensor."""
+    import torch
+    cnt = C.c_uint64(0)
+    _check(lib().atc_gen_chunglu_device(n, gamma, mean_degree, seed, None, 0, C.byref(cnt), stream))
+    out = torch.empty((max(cnt.value, 1), 2), dtype=torch.int32, device="cuda")
+    _check(lib().atc_gen_chunglu_device(n, gamma, mean_degree, seed, C.c_void_p(out.data_ptr()), cnt.value,
+                                        C.byref(cnt), stream))
+    return out[: cnt.value]
 
 
 def adirection(pairs, want_prio=False, stream=None):

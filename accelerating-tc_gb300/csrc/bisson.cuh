@@ -1,0 +1,518 @@
+// Bisson-style grouped counting kernels, shared by the single-graph count (tc.cu), the
+// allocation-free count (tc.cu) and the batched count (batch.cu).  Internal header:
+// every includer gets its own copy of the kernels.
+#pragma once
+
+#include "internal.cuh"
+
+namespace atc {
+
+struct CsrView {
+  const int64_t* off;
+  const int32_t* cols;
+  const int32_t* esrc;
+  int64_t n, m;
+};
+
+namespace {
+
+__device__ __forceinline__ void warp_add_count(unsigned long long c, unsigned long long* out) {
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+int blocks_per_sm(const void* kernel, int block, size_t smem) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, block, smem) != cudaSuccess || b < 1) b = 1;
+  return b;
+}
+
+// ============================== Bisson-style =======================================
+// The reference keeps a bitmap of N+(u) for rows longer than 32 and streams every N+(v),
+// v in N+(u), through it (Bisson/tc.cu:36-62): one bit test per directed wedge, W tests
+// in all.  Here every edge {u, v} is handed to its endpoint h with the longer list; N+(h)
+// becomes a set in shared memory and the shorter list of the partner is streamed
+// through it.  That tests sum_edges min(d+u, d+v) elements instead of W.
+//   warp items (d+h <= kWarpMax): a warp per chunk of partners, no block barriers; N+(h)
+//     either copied sorted into the warp's slot and binary-searched (d+h <= cutover, the
+//     reference's <=32 branch, Bisson/tc.cu:63-87) or inserted into a warp-private hash
+//     table of kWarpSlots slots (load factor <= 1/4);
+//   block items (d+h > kWarpMax): a CTA per chunk of partners; N+(h) as a block hash
+//     table sized to the largest such list, or a bitmap over [min, max] of the list, or
+//     (lists too long for both) binary search in global memory.
+// Chunks come from device work counters (one atomicAdd per chunk; nothing waits on them).
+constexpr int kBgWarps = 8;
+constexpr int kWarpMax = 256;       // longest N+(h) handled by one warp
+constexpr int kWarpSlots = 1024;    // warp-private hash slots (4 KB)
+constexpr int kWarpChunk = 512;     // partners per warp item
+constexpr int kBlockChunk = 2048;   // partners per block item
+constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
+constexpr int kHashMax = kTabWords / 4;
+
+struct GroupItem {
+  int32_t h;
+  int32_t mode;  // warp: 0 sorted copy, 1 hash; block: 0 hash, 1 bitmap, 2 global search
+  int64_t b, e;  // partner range in the grouped list
+};
+
+__device__ __forceinline__ bool longer_is_u(int32_t u, int32_t v, int64_t du, int64_t dv) {
+  return du > dv || (du == dv && u < v);
+}
+
+// Pass 1: partners per group, with warp-aggregated atomics (edges of one source are
+// contiguous, so runs of one h are common).
+__global__ void group_count_kernel(CsrView g, int32_t* cnt) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t m_pad = (g.m + 31) & ~31ll;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
+    int32_t h = -1;
+    if (e < g.m) {
+      int32_t u = g.esrc[e], v = g.cols[e];
+      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      if (du > 0 && dv > 0) h = longer_is_u(u, v, du, dv) ? u : v;
+    }
+    unsigned same = __match_any_sync(0xffffffffu, h);
+    int lead = __ffs(same) - 1;
+    if (h >= 0 && (int)(threadIdx.x & 31) == lead) atomicAdd(&cnt[h], __popc(same));
+  }
+}
+
+// Pass 2: scatter partners into their group (order inside a group is irrelevant).
+__global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t m_pad = (g.m + 31) & ~31ll;
+  const int lane = threadIdx.x & 31;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
+    int32_t h = -1, p = 0;
+    if (e < g.m) {
+      int32_t u = g.esrc[e], v = g.cols[e];
+      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      if (du > 0 && dv > 0) {
+        bool hu = longer_is_u(u, v, du, dv);
+        h = hu ? u : v;
+        p = hu ? v : u;
+      }
+    }
+    unsigned same = __match_any_sync(0xffffffffu, h);
+    int lead = __ffs(same) - 1;
+    int base = 0;
+    if (h >= 0 && lane == lead) base = atomicAdd(&cur[h], __popc(same));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    if (h >= 0) plist[gstart[h] + base + __popc(same & ((1u << lane) - 1))] = p;
+  }
+}
+
+// Pass 3: cut every group into work items; counters[0] = warp items, [1] = block items,
+// [3] = longest N+(h) among block items.
+// Runtime shape of the work items: lists up to warp_max (<= kWarpMax) go to warp
+// items of warp_chunk partners, longer ones to block items of block_chunk partners.
+struct ItemShape {
+  int cutover;      // warp items: sorted copy up to this length, hash above
+  int warp_max;
+  int warp_chunk;
+  int block_chunk;
+};
+
+__host__ __device__ inline ItemShape default_shape(int cutover) {
+  return ItemShape{cutover, kWarpMax, kWarpChunk, kBlockChunk};
+}
+
+// Upper bound on the items of either kind for a graph with n vertices, `partners`
+// grouped partners and chunks of at least min_chunk partners.
+__host__ __device__ inline int64_t max_items(int64_t n, int64_t partners, int min_chunk) {
+  return n + partners / min_chunk + 1;
+}
+
+__global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* witems, GroupItem* bitems,
+                                   int* counters, ItemShape sh) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
+    int64_t b = gstart[h], e = gstart[h + 1];
+    if (b == e) continue;
+    int64_t hb = g.off[h], dh = g.off[h + 1] - hb;
+    if (dh <= sh.warp_max) {
+      int32_t mode = dh <= sh.cutover ? 0 : 1;
+      int64_t k = (e - b + sh.warp_chunk - 1) / sh.warp_chunk;
+      int at = atomicAdd(&counters[0], (int)k);
+      for (int64_t c = 0; c < k; ++c)
+        witems[at + c] = GroupItem{(int32_t)h, mode, b + c * sh.warp_chunk, min(e, b + (c + 1) * sh.warp_chunk)};
+    } else {
+      int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
+      int32_t mode = dh <= kHashMax ? 0 : (span < kTabWords * 32 ? 1 : 2);
+      if (mode == 0) atomicMax(&counters[3], (int)dh);
+      else atomicMax(&counters[3], kHashMax);
+      int64_t k = (e - b + sh.block_chunk - 1) / sh.block_chunk;
+      int at = atomicAdd(&counters[1], (int)k);
+      for (int64_t c = 0; c < k; ++c)
+        bitems[at + c] = GroupItem{(int32_t)h, mode, b + c * sh.block_chunk, min(e, b + (c + 1) * sh.block_chunk)};
+    }
+  }
+}
+
+// Where the counting kernels read their work items from.  FullItems: the explicit
+// items of the single-graph path.  CompactItems (batches): 8-byte (h, chunk) pairs,
+// warp items from the front of one array and block items from its back, decoded with
+// the group starts and the item shape.
+struct FullItems {
+  const GroupItem* p;
+  __device__ __forceinline__ GroupItem get(const CsrView&, int i) const { return p[i]; }
+};
+
+struct CompactItems {
+  const int2* p;
+  const int64_t* gstart;
+  int64_t cap;
+  bool from_back;  // block items
+  ItemShape sh;
+  __device__ __forceinline__ GroupItem get(const CsrView& g, int i) const {
+    int2 c = from_back ? p[cap - 1 - i] : p[i];
+    int64_t b0 = gstart[c.x], e0 = gstart[c.x + 1];
+    int64_t chunk = from_back ? sh.block_chunk : sh.warp_chunk;
+    int64_t b = b0 + (int64_t)c.y * chunk, e = min(e0, b + chunk);
+    int64_t hb = g.off[c.x], dh = g.off[c.x + 1] - hb;
+    int32_t mode;
+    if (!from_back) {
+      mode = dh <= sh.cutover ? 0 : 1;
+    } else {
+      int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
+      mode = dh <= kHashMax ? 0 : (span < kTabWords * 32 ? 1 : 2);
+    }
+    return GroupItem{c.x, mode, b, e};
+  }
+};
+
+// Vertex-centric grouping passes for a CSR without the per-edge source array: a warp
+// per source vertex, lanes over its out-edges (same grouping rule as above).
+__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < g.n; u += warps) {
+    const int64_t ub = g.off[u], du = g.off[u + 1] - ub;
+    if (du == 0) continue;
+    for (int64_t base = 0; base < du; base += 32) {
+      int32_t h = -1;
+      if (base + lane < du) {
+        int32_t v = g.cols[ub + base + lane];
+        int64_t dv = g.off[v + 1] - g.off[v];
+        if (dv > 0) h = longer_is_u((int32_t)u, v, du, dv) ? (int32_t)u : v;
+      }
+      unsigned same = __match_any_sync(0xffffffffu, h);
+      int lead = __ffs(same) - 1;
+      if (h >= 0 && lane == lead) atomicAdd(&cnt[h], __popc(same));
+    }
+  }
+}
+
+__global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < g.n; u += warps) {
+    const int64_t ub = g.off[u], du = g.off[u + 1] - ub;
+    if (du == 0) continue;
+    for (int64_t base = 0; base < du; base += 32) {
+      int32_t h = -1, p = 0;
+      if (base + lane < du) {
+        int32_t v = g.cols[ub + base + lane];
+        int64_t dv = g.off[v + 1] - g.off[v];
+        if (dv > 0) {
+          bool hu = longer_is_u((int32_t)u, v, du, dv);
+          h = hu ? (int32_t)u : v;
+          p = hu ? v : (int32_t)u;
+        }
+      }
+      unsigned same = __match_any_sync(0xffffffffu, h);
+      int lead = __ffs(same) - 1;
+      int at = 0;
+      if (h >= 0 && lane == lead) at = atomicAdd(&cur[h], __popc(same));
+      at = __shfl_sync(0xffffffffu, at, lead);
+      if (h >= 0) plist[gstart[h] + at + __popc(same & ((1u << lane) - 1))] = p;
+    }
+  }
+}
+
+// Compact items: counters[0] warp items (front), counters[1] block items (back),
+// counters[3] longest list among block items.
+__global__ void group_items_compact_kernel(CsrView g, const int64_t* gstart, int2* items, int64_t cap, int* counters,
+                                           ItemShape sh) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
+    int64_t b = gstart[h], e = gstart[h + 1];
+    if (b == e) continue;
+    int64_t dh = g.off[h + 1] - g.off[h];
+    bool warp = dh <= sh.warp_max;
+    int64_t chunk = warp ? sh.warp_chunk : sh.block_chunk;
+    int k = (int)((e - b + chunk - 1) / chunk);
+    int at = atomicAdd(&counters[warp ? 0 : 1], k);
+    if (!warp) atomicMax(&counters[3], (int)min(dh, (int64_t)kHashMax));
+    for (int c = 0; c < k; ++c) {
+      int64_t slot = warp ? (int64_t)at + c : cap - 1 - ((int64_t)at + c);
+      items[slot] = make_int2((int32_t)h, c);
+    }
+  }
+}
+
+// Per-graph attribution for a batch of graphs stored as one disjoint union: vertex
+// ranges [vbase[g], vbase[g+1]) belong to graph g; counts[g] receives its triangles.
+// counts == nullptr: a single graph, everything goes to the kernel's `out` counter.
+struct GraphTags {
+  const int64_t* vbase;
+  int ngraphs;
+  unsigned long long* counts;
+};
+
+__device__ __forceinline__ int graph_of(const GraphTags& t, int64_t v) {
+  int lo = 0, hi = t.ngraphs;  // last g with vbase[g] <= v
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (t.vbase[mid] <= v) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Adds a warp's per-lane partial of one item to its graph (all 32 lanes call this).
+__device__ __forceinline__ void add_item_to_graph(const GraphTags& t, int64_t h, unsigned part) {
+  unsigned long long c = part;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&t.counts[graph_of(t, h)], c);
+}
+
+__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
+
+// Linear-probing lookup; the table always has empty slots, and `cap` bounds the walk.
+// Most lookups end at the first slot (load factor <= 1/4).
+__device__ __forceinline__ unsigned hash_has(const int32_t* tab, uint32_t mask, int32_t x) {
+  uint32_t s = hash_slot(x, mask);
+  int32_t y = tab[s];
+  if (y == x) return 1u;
+  if (y == -1) return 0u;
+  for (uint32_t n = 0; n < mask; ++n) {
+    s = (s + 1) & mask;
+    y = tab[s];
+    if (y == x) return 1u;
+    if (y == -1) return 0u;
+  }
+  return 0u;
+}
+
+// Inserts x (not yet present); concurrent inserters use atomicCAS.
+__device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t x) {
+  uint32_t s = hash_slot(x, mask);
+  for (uint32_t n = 0; n <= mask; ++n) {
+    if (atomicCAS(&tab[s], -1, x) == -1) return;
+    s = (s + 1) & mask;
+  }
+}
+
+// Empties the slot holding x (x present); keys are cleared only by the thread that
+// inserted them, so the walk always reaches x.
+__device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t x) {
+  uint32_t s = hash_slot(x, mask);
+  for (uint32_t n = 0; n <= mask; ++n) {
+    if (tab[s] == x) { tab[s] = -1; return; }
+    s = (s + 1) & mask;
+  }
+}
+
+// Streams the lists of the partners plist[base, base+32) for every batch start `base`
+// that `next_batch()` hands out (until it reaches i1) through `probe`, and returns the
+// hits.  Lists of 32 or more elements are walked by the whole warp, one list at a
+// time, four coalesced loads in flight per lane.  Shorter lists are spread over the
+// lanes by a warp prefix sum of their lengths, so they do not leave lanes idle; each
+// lane follows the list it is in with a cursor kept in registers.  sx/sp: the warp's
+// 32-entry shared scratch.
+template <class NextBatch, class Probe>
+__device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
+                                                    int lane, int* sx, int64_t* sp, NextBatch next_batch,
+                                                    Probe probe) {
+  unsigned cnt = 0;
+  for (int64_t base = next_batch(); base < i1; base = next_batch()) {
+    int64_t i = base + lane;
+    int len = 0;
+    int64_t pb = 0;
+    if (i < i1) {
+      int32_t p = __ldg(plist + i);
+      pb = __ldg(g.off + p);
+      len = (int)(__ldg(g.off + p + 1) - pb);
+    }
+    unsigned longm = __ballot_sync(0xffffffffu, len >= 32);
+    while (longm) {
+      const int k = __ffs(longm) - 1;
+      longm &= longm - 1;
+      const int32_t* P = g.cols + __shfl_sync(0xffffffffu, pb, k);
+      const int ln = __shfl_sync(0xffffffffu, len, k);
+      int j = lane;
+      for (; j + 96 < ln; j += 128) {
+        int32_t x0 = __ldg(P + j), x1 = __ldg(P + j + 32), x2 = __ldg(P + j + 64), x3 = __ldg(P + j + 96);
+        cnt += probe(x0) + probe(x1) + probe(x2) + probe(x3);
+      }
+      for (; j < ln; j += 32) cnt += probe(__ldg(P + j));
+    }
+    const int slen = len < 32 ? len : 0;
+    int incl = slen;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) continue;
+    sx[lane] = incl - slen;
+    sp[lane] = pb;
+    __syncwarp();
+    // k = the last lane whose start is <= t: always a lane with a non-empty short list
+    int k = 0;
+    int kx = sx[0], knext = sx[1];
+    int64_t kp = sp[0];
+    for (int t = lane; t < total; t += 32) {
+      while (k < 31 && knext <= t) {
+        ++k;
+        kx = knext;
+        kp = sp[k];
+        knext = k < 31 ? sx[k + 1] : total;
+      }
+      cnt += probe(__ldg(g.cols + kp + (t - kx)));
+    }
+    __syncwarp();
+  }
+  return cnt;
+}
+
+// nitems_dev (nullable): the item count read from device memory instead of `nitems`.
+template <class Items>
+__global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
+                                                                  Items items, int nitems,
+                                                                  const int* nitems_dev, int* next, GraphTags tags,
+                                                                  unsigned long long* out) {
+  __shared__ int32_t tab[kBgWarps][kWarpSlots];
+  __shared__ int sx[kBgWarps][32];
+  __shared__ int64_t sp[kBgWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
+  __syncwarp();
+  unsigned long long total = 0;
+  int32_t* T = tab[w];
+  if (nitems_dev) nitems = *nitems_dev;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(next, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const GroupItem gi = items.get(g, it);
+    const int64_t hb = g.off[gi.h];
+    const int dh = (int)(g.off[gi.h + 1] - hb);
+    int64_t cur = gi.b;
+    auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
+    unsigned cnt;
+    if (gi.mode == 0) {
+      for (int j = lane; j < dh; j += 32) T[j] = __ldg(g.cols + hb + j);
+      __syncwarp();
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+        int lo = 0, n = dh;
+        while (n > 1) {  // branch-free lower bound over the sorted copy
+          int half = n >> 1;
+          lo = T[lo + half - 1] < x ? lo + half : lo;
+          n -= half;
+        }
+        return T[lo] == x;
+      });
+      __syncwarp();
+      for (int j = lane; j < dh; j += 32) T[j] = -1;
+    } else {
+      uint32_t cap = 64;
+      while (cap < 4u * (uint32_t)dh) cap <<= 1;
+      const uint32_t mask = cap - 1;
+      for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
+      __syncwarp();
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
+                            [&](int32_t x) -> unsigned { return hash_has(T, mask, x); });
+      __syncwarp();
+      for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
+    }
+    __syncwarp();
+    if (tags.counts) add_item_to_graph(tags, gi.h, cnt);
+    else total += cnt;
+  }
+  warp_add_count(total, out);
+}
+
+template <class Items>
+__global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
+                                                                   Items items, int nitems,
+                                                                   const int* nitems_dev, int* next, uint32_t tab_words,
+                                                                   GraphTags tags, unsigned long long* out) {
+  extern __shared__ int32_t tab[];  // tab_words
+  __shared__ int sx[kBgWarps][32];
+  __shared__ int64_t sp[kBgWarps][32];
+  __shared__ int cur_item;
+  __shared__ unsigned long long bnext;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t j = threadIdx.x; j < tab_words; j += blockDim.x) tab[j] = -1;
+  unsigned long long total = 0;
+  if (nitems_dev) nitems = *nitems_dev;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      cur_item = atomicAdd(next, 1);
+      bnext = 0;
+    }
+    __syncthreads();
+    const int it = cur_item;
+    if (it >= nitems) break;
+    const GroupItem gi = items.get(g, it);
+    const int64_t hb = g.off[gi.h];
+    const int64_t dh = g.off[gi.h + 1] - hb;
+    const int32_t* Nh = g.cols + hb;
+    // partner batches of 32 handed out to the warps as they finish
+    auto nb = [&]() {
+      unsigned long long r = 0;
+      if (lane == 0) r = atomicAdd(&bnext, 32ull);
+      return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
+    };
+    unsigned cnt = 0;
+    if (gi.mode == 0) {
+      uint32_t cap = 64;
+      while (cap < 4u * (uint32_t)dh) cap <<= 1;
+      const uint32_t mask = cap - 1;
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
+      __syncthreads();
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
+                            [&](int32_t x) -> unsigned { return hash_has(tab, mask, x); });
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
+    } else if (gi.mode == 1) {
+      const int32_t lo = Nh[0], hi = Nh[dh - 1];
+      const int words = ((hi - lo) >> 5) + 1;
+      uint32_t* bits = reinterpret_cast<uint32_t*>(tab);
+      for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0u;
+      __syncthreads();
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) {
+        int32_t x = Nh[j] - lo;
+        atomicOr(&bits[x >> 5], 1u << (x & 31));
+      }
+      __syncthreads();
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+        if (x < lo || x > hi) return 0u;
+        x -= lo;
+        return (bits[x >> 5] >> (x & 31)) & 1u;
+      });
+      __syncthreads();
+      for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0xffffffffu;  // back to empty slots (-1)
+    } else {
+      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+        int64_t lo = 0, hi = dh;
+        while (lo < hi) {
+          int64_t mid = (lo + hi) >> 1;
+          if (Nh[mid] < x) lo = mid + 1; else hi = mid;
+        }
+        return lo < dh && Nh[lo] == x;
+      });
+    }
+    __syncthreads();
+    if (tags.counts) add_item_to_graph(tags, gi.h, cnt);
+    else total += cnt;
+  }
+  warp_add_count(total, out);
+}
+
+}  // namespace
+
+}  // namespace atc

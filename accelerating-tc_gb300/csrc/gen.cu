@@ -106,9 +106,121 @@ __global__ void rgg_edges_kernel(uint64_t s0, uint32_t n, RggGrid gr, const uint
   }
 }
 
+// ---- Chung-Lu graphs (expected-degree model) ------------------------------------------
+// Vertex i has weight w_i = C (i+1)^(-1/(gamma-1)), capped at sqrt(n d) so that every edge
+// probability min(1, w_u w_v / S) (S = sum of weights = n d) is a probability; C is set
+// from the integral approximation of sum_i (i+1)^(-alpha).  Edges are drawn with the
+// O(n + m) skip method of Miller & Hagberg (2011): weights decrease with the index, so
+// for each u the candidates v > u are visited by geometric skips at the current
+// probability bound and accepted with ratio q / p.  A thread per u; its uniform draws
+// come from a counter-based generator, so the counting pass and the writing pass see
+// the same sequence.
+struct ChungLu {
+  double C, alpha, cap, S;
+  uint64_t s0;
+  uint32_t n;
+};
+
+// Arithmetic through round-to-nearest intrinsics: the counting and the writing pass
+// must produce the same values, so no operation may be contracted differently.
+__device__ __forceinline__ double cl_weight(const ChungLu& c, uint32_t i) {
+  double w = __dmul_rn(c.C, pow(__dadd_rn((double)i, 1.0), -c.alpha));
+  return w < c.cap ? w : c.cap;
+}
+
+__device__ __forceinline__ double cl_uniform(const ChungLu& c, uint32_t u, uint32_t t) {
+  uint64_t r = mix64(c.s0 + (((uint64_t)u << 32) | t) * kGolden + 0x5851F42D4C957F2Dull);
+  return __dmul_rn(__dadd_rn((double)(r >> 11), 1.0), 1.0 / 9007199254740992.0);  // (0, 1]
+}
+
+__device__ __forceinline__ double cl_prob(const ChungLu& c, double wu, uint32_t v) {
+  return fmin(__ddiv_rn(__dmul_rn(wu, cl_weight(c, v)), c.S), 1.0);
+}
+
+// Edges (u, v > u) of row u; writes at most `limit` of them when out != nullptr.
+__device__ __forceinline__ uint32_t cl_row(const ChungLu& c, uint32_t u, int2* out, uint32_t limit) {
+  uint32_t found = 0, t = 0;
+  const double wu = cl_weight(c, u);
+  uint32_t v = u + 1;
+  if (v >= c.n) return 0;
+  double p = cl_prob(c, wu, v);
+  while (v < c.n && p > 0.0) {
+    if (p < 1.0) {
+      double r = cl_uniform(c, u, t++);
+      double skip = floor(__ddiv_rn(log(r), log1p(-p)));
+      if (skip >= (double)(c.n - v)) break;
+      v += (uint32_t)skip;
+    }
+    if (v >= c.n) break;
+    double q = cl_prob(c, wu, v);
+    double r = cl_uniform(c, u, t++);
+    if (__dmul_rn(r, p) < q || q >= 1.0) {
+      if (out && found < limit) out[found] = make_int2((int32_t)u, (int32_t)v);
+      ++found;
+    }
+    p = q;
+    ++v;
+  }
+  return found;
+}
+
+__global__ void cl_count_kernel(ChungLu c, uint32_t* rowcnt) {
+  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < c.n; u += (uint64_t)gridDim.x * blockDim.x)
+    rowcnt[u] = cl_row(c, (uint32_t)u, nullptr, 0);
+}
+
+__global__ void cl_write_kernel(ChungLu c, const int64_t* rowoff, const uint32_t* rowcnt, int2* out) {
+  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < c.n; u += (uint64_t)gridDim.x * blockDim.x)
+    cl_row(c, (uint32_t)u, out + rowoff[u], rowcnt[u]);
+}
+
+static bool chunglu_params(uint32_t n, double gamma, double mean_degree, uint64_t seed, ChungLu* c) {
+  if (n < 2 || !(gamma > 1.05) || !(mean_degree > 0) || mean_degree >= (double)n) return false;
+  c->alpha = 1.0 / (gamma - 1.0);
+  c->S = (double)n * mean_degree;
+  c->cap = std::sqrt(c->S);
+  // sum_{i=1..n} i^-alpha ~ integral_1^{n} x^-alpha dx + (1 + n^-alpha) / 2
+  double a = c->alpha, nn = (double)n;
+  double integral = std::fabs(a - 1.0) < 1e-12 ? std::log(nn) : (std::pow(nn, 1.0 - a) - 1.0) / (1.0 - a);
+  double h = integral + 0.5 * (1.0 + std::pow(nn, -a));
+  c->C = c->S / h;
+  c->s0 = mix64(seed);
+  c->n = n;
+  return true;
+}
+
 }  // namespace atc
 
 using namespace atc;
+
+extern "C" atc_status atc_gen_chunglu_device(uint32_t n, double gamma, double mean_degree, uint64_t seed,
+                                             int32_t* out_dev, uint64_t capacity, uint64_t* n_out, atc_stream st) {
+  ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
+  ChungLu c;
+  ATC_CHECK_ARG(chunglu_params(n, gamma, mean_degree, seed, &c), "need n >= 2, gamma > 1.05, 0 < mean degree < n");
+  cudaStream_t s = as_stream(st);
+  DevBuf<uint32_t> cnt;
+  DevBuf<int64_t> off;
+  ATC_TRY(cnt.alloc(n + 1, s));
+  ATC_TRY(off.alloc(n + 1, s));
+  ATC_CK(cudaMemsetAsync(cnt.p + n, 0, sizeof(uint32_t), s));
+  cl_count_kernel<<<grid_for(n, 128, 16), 128, 0, s>>>(c, cnt.p);
+  ATC_CK(cudaGetLastError());
+  ATC_TRY(exclusive_scan_i32_to_i64(reinterpret_cast<const int32_t*>(cnt.p), off.p, (size_t)n + 1, s));
+  int64_t total = 0;
+  ATC_CK(cudaMemcpyAsync(&total, off.p + n, sizeof(total), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  *n_out = (uint64_t)total;
+  if (!out_dev) return ATC_OK;
+  if ((uint64_t)total > capacity) {
+    set_error("Chung-Lu graph has %lld edges, capacity %llu", (long long)total, (unsigned long long)capacity);
+    return ATC_ERR_INVALID;
+  }
+  cl_write_kernel<<<grid_for(n, 128, 16), 128, 0, s>>>(c, off.p, cnt.p, reinterpret_cast<int2*>(out_dev));
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaStreamSynchronize(s));
+  return ATC_OK;
+}
 
 extern "C" atc_status atc_gen_rgg_host(uint32_t n, double mean_degree, uint64_t seed, int32_t* out,
                                        uint64_t capacity, uint64_t* n_out, int nthreads) {

@@ -14,6 +14,8 @@ atc_status unique_u64(const uint64_t* in, uint64_t* out, size_t n, size_t* n_out
 // out[i] = sum_{j<i} in[j], for n elements.
 atc_status exclusive_scan_i64(const int64_t* in, int64_t* out, size_t n, cudaStream_t s);
 atc_status exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, size_t n, cudaStream_t s);
+atc_status exclusive_scan_i32_to_i64_tmp(void* tmp, size_t* bytes, const int32_t* in, int64_t* out, size_t n,
+                                         cudaStream_t s);
 
 // Bits needed to hold ids in [0, n): at least 1.
 inline int id_bits(int64_t n) {

@@ -67,4 +67,13 @@ atc_status exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, size_t n, 
   return ATC_OK;
 }
 
+// The same scan with caller-provided temporary storage (no allocation, so it can be
+// recorded into a CUDA graph).  tmp == nullptr: *bytes receives the size needed.
+atc_status exclusive_scan_i32_to_i64_tmp(void* tmp, size_t* bytes, const int32_t* in, int64_t* out, size_t n,
+                                         cudaStream_t s) {
+  thrust::transform_iterator<I32ToI64, const int32_t*, int64_t> it(in, I32ToI64());
+  ATC_CK(cub::DeviceScan::ExclusiveSum(tmp, *bytes, it, out, (int64_t)n, s));
+  return ATC_OK;
+}
+
 }  // namespace atc

@@ -23,23 +23,13 @@
 #include <mutex>
 #include <vector>
 
-#include "internal.cuh"
+#include "bisson.cuh"
 
 namespace atc {
 
-struct CsrView {
-  const int64_t* off;
-  const int32_t* cols;
-  const int32_t* esrc;
-  int64_t n, m;
-};
 
 namespace {
 
-__device__ __forceinline__ void warp_add_count(unsigned long long c, unsigned long long* out) {
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
-}
 
 // Number of elements < x in a sorted list (lower bound), list in any address space.
 __device__ __forceinline__ bool bsearch_has(const int32_t* a, int64_t n, int32_t x) {
@@ -267,342 +257,6 @@ __global__ void __launch_bounds__(kHuWarps * 32) hu_kernel(CsrView g, const int3
   warp_add_count(cnt, out);
 }
 
-// ============================== Bisson-style =======================================
-// The reference keeps a bitmap of N+(u) for rows longer than 32 and streams every N+(v),
-// v in N+(u), through it (Bisson/tc.cu:36-62): one bit test per directed wedge, W tests
-// in all.  Here every edge {u, v} is handed to its endpoint h with the longer list; N+(h)
-// becomes a set in shared memory and the shorter list of the partner is streamed
-// through it.  That tests sum_edges min(d+u, d+v) elements instead of W.
-//   warp items (d+h <= kWarpMax): a warp per chunk of partners, no block barriers; N+(h)
-//     either copied sorted into the warp's slot and binary-searched (d+h <= cutover, the
-//     reference's <=32 branch, Bisson/tc.cu:63-87) or inserted into a warp-private hash
-//     table of kWarpSlots slots (load factor <= 1/4);
-//   block items (d+h > kWarpMax): a CTA per chunk of partners; N+(h) as a block hash
-//     table sized to the largest such list, or a bitmap over [min, max] of the list, or
-//     (lists too long for both) binary search in global memory.
-// Chunks come from device work counters (one atomicAdd per chunk; nothing waits on them).
-constexpr int kBgWarps = 8;
-constexpr int kWarpMax = 256;       // longest N+(h) handled by one warp
-constexpr int kWarpSlots = 1024;    // warp-private hash slots (4 KB)
-constexpr int kWarpChunk = 512;     // partners per warp item
-constexpr int kBlockChunk = 2048;   // partners per block item
-constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
-constexpr int kHashMax = kTabWords / 4;
-
-struct GroupItem {
-  int32_t h;
-  int32_t mode;  // warp: 0 sorted copy, 1 hash; block: 0 hash, 1 bitmap, 2 global search
-  int64_t b, e;  // partner range in the grouped list
-};
-
-__device__ __forceinline__ bool longer_is_u(int32_t u, int32_t v, int64_t du, int64_t dv) {
-  return du > dv || (du == dv && u < v);
-}
-
-// Pass 1: partners per group, with warp-aggregated atomics (edges of one source are
-// contiguous, so runs of one h are common).
-__global__ void group_count_kernel(CsrView g, int32_t* cnt) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t m_pad = (g.m + 31) & ~31ll;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
-    int32_t h = -1;
-    if (e < g.m) {
-      int32_t u = g.esrc[e], v = g.cols[e];
-      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
-      if (du > 0 && dv > 0) h = longer_is_u(u, v, du, dv) ? u : v;
-    }
-    unsigned same = __match_any_sync(0xffffffffu, h);
-    int lead = __ffs(same) - 1;
-    if (h >= 0 && (int)(threadIdx.x & 31) == lead) atomicAdd(&cnt[h], __popc(same));
-  }
-}
-
-// Pass 2: scatter partners into their group (order inside a group is irrelevant).
-__global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t m_pad = (g.m + 31) & ~31ll;
-  const int lane = threadIdx.x & 31;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
-    int32_t h = -1, p = 0;
-    if (e < g.m) {
-      int32_t u = g.esrc[e], v = g.cols[e];
-      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
-      if (du > 0 && dv > 0) {
-        bool hu = longer_is_u(u, v, du, dv);
-        h = hu ? u : v;
-        p = hu ? v : u;
-      }
-    }
-    unsigned same = __match_any_sync(0xffffffffu, h);
-    int lead = __ffs(same) - 1;
-    int base = 0;
-    if (h >= 0 && lane == lead) base = atomicAdd(&cur[h], __popc(same));
-    base = __shfl_sync(0xffffffffu, base, lead);
-    if (h >= 0) plist[gstart[h] + base + __popc(same & ((1u << lane) - 1))] = p;
-  }
-}
-
-// Pass 3: cut every group into work items; counters[0] = warp items, [1] = block items,
-// [3] = longest N+(h) among block items.
-__global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* witems, GroupItem* bitems,
-                                   int* counters, int cutover) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
-    int64_t b = gstart[h], e = gstart[h + 1];
-    if (b == e) continue;
-    int64_t hb = g.off[h], dh = g.off[h + 1] - hb;
-    if (dh <= kWarpMax) {
-      int32_t mode = dh <= cutover ? 0 : 1;
-      int64_t k = (e - b + kWarpChunk - 1) / kWarpChunk;
-      int at = atomicAdd(&counters[0], (int)k);
-      for (int64_t c = 0; c < k; ++c)
-        witems[at + c] = GroupItem{(int32_t)h, mode, b + c * kWarpChunk, min(e, b + (c + 1) * kWarpChunk)};
-    } else {
-      int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
-      int32_t mode = dh <= kHashMax ? 0 : (span < kTabWords * 32 ? 1 : 2);
-      if (mode == 0) atomicMax(&counters[3], (int)dh);
-      else atomicMax(&counters[3], kHashMax);
-      int64_t k = (e - b + kBlockChunk - 1) / kBlockChunk;
-      int at = atomicAdd(&counters[1], (int)k);
-      for (int64_t c = 0; c < k; ++c)
-        bitems[at + c] = GroupItem{(int32_t)h, mode, b + c * kBlockChunk, min(e, b + (c + 1) * kBlockChunk)};
-    }
-  }
-}
-
-__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
-
-// Linear-probing lookup; the table always has empty slots, and `cap` bounds the walk.
-// Most lookups end at the first slot (load factor <= 1/4).
-__device__ __forceinline__ unsigned hash_has(const int32_t* tab, uint32_t mask, int32_t x) {
-  uint32_t s = hash_slot(x, mask);
-  int32_t y = tab[s];
-  if (y == x) return 1u;
-  if (y == -1) return 0u;
-  for (uint32_t n = 0; n < mask; ++n) {
-    s = (s + 1) & mask;
-    y = tab[s];
-    if (y == x) return 1u;
-    if (y == -1) return 0u;
-  }
-  return 0u;
-}
-
-// Inserts x (not yet present); concurrent inserters use atomicCAS.
-__device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t x) {
-  uint32_t s = hash_slot(x, mask);
-  for (uint32_t n = 0; n <= mask; ++n) {
-    if (atomicCAS(&tab[s], -1, x) == -1) return;
-    s = (s + 1) & mask;
-  }
-}
-
-// Empties the slot holding x (x present); keys are cleared only by the thread that
-// inserted them, so the walk always reaches x.
-__device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t x) {
-  uint32_t s = hash_slot(x, mask);
-  for (uint32_t n = 0; n <= mask; ++n) {
-    if (tab[s] == x) { tab[s] = -1; return; }
-    s = (s + 1) & mask;
-  }
-}
-
-// Streams the lists of the partners plist[base, base+32) for every batch start `base`
-// that `next_batch()` hands out (until it reaches i1) through `probe`, and returns the
-// hits.  Lists of 32 or more elements are walked by the whole warp, one list at a
-// time, four coalesced loads in flight per lane.  Shorter lists are spread over the
-// lanes by a warp prefix sum of their lengths, so they do not leave lanes idle; each
-// lane follows the list it is in with a cursor kept in registers.  sx/sp: the warp's
-// 32-entry shared scratch.
-template <class NextBatch, class Probe>
-__device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
-                                                    int lane, int* sx, int64_t* sp, NextBatch next_batch,
-                                                    Probe probe) {
-  unsigned cnt = 0;
-  for (int64_t base = next_batch(); base < i1; base = next_batch()) {
-    int64_t i = base + lane;
-    int len = 0;
-    int64_t pb = 0;
-    if (i < i1) {
-      int32_t p = __ldg(plist + i);
-      pb = __ldg(g.off + p);
-      len = (int)(__ldg(g.off + p + 1) - pb);
-    }
-    unsigned longm = __ballot_sync(0xffffffffu, len >= 32);
-    while (longm) {
-      const int k = __ffs(longm) - 1;
-      longm &= longm - 1;
-      const int32_t* P = g.cols + __shfl_sync(0xffffffffu, pb, k);
-      const int ln = __shfl_sync(0xffffffffu, len, k);
-      int j = lane;
-      for (; j + 96 < ln; j += 128) {
-        int32_t x0 = __ldg(P + j), x1 = __ldg(P + j + 32), x2 = __ldg(P + j + 64), x3 = __ldg(P + j + 96);
-        cnt += probe(x0) + probe(x1) + probe(x2) + probe(x3);
-      }
-      for (; j < ln; j += 32) cnt += probe(__ldg(P + j));
-    }
-    const int slen = len < 32 ? len : 0;
-    int incl = slen;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) continue;
-    sx[lane] = incl - slen;
-    sp[lane] = pb;
-    __syncwarp();
-    // k = the last lane whose start is <= t: always a lane with a non-empty short list
-    int k = 0;
-    int kx = sx[0], knext = sx[1];
-    int64_t kp = sp[0];
-    for (int t = lane; t < total; t += 32) {
-      while (k < 31 && knext <= t) {
-        ++k;
-        kx = knext;
-        kp = sp[k];
-        knext = k < 31 ? sx[k + 1] : total;
-      }
-      cnt += probe(__ldg(g.cols + kp + (t - kx)));
-    }
-    __syncwarp();
-  }
-  return cnt;
-}
-
-__global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
-                                                                  const GroupItem* items, int nitems, int* next,
-                                                                  unsigned long long* out) {
-  __shared__ int32_t tab[kBgWarps][kWarpSlots];
-  __shared__ int sx[kBgWarps][32];
-  __shared__ int64_t sp[kBgWarps][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
-  __syncwarp();
-  unsigned long long total = 0;
-  int32_t* T = tab[w];
-  for (;;) {
-    int it = 0;
-    if (lane == 0) it = atomicAdd(next, 1);
-    it = __shfl_sync(0xffffffffu, it, 0);
-    if (it >= nitems) break;
-    const GroupItem gi = items[it];
-    const int64_t hb = g.off[gi.h];
-    const int dh = (int)(g.off[gi.h + 1] - hb);
-    int64_t cur = gi.b;
-    auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
-    unsigned cnt;
-    if (gi.mode == 0) {
-      for (int j = lane; j < dh; j += 32) T[j] = __ldg(g.cols + hb + j);
-      __syncwarp();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
-        int lo = 0, n = dh;
-        while (n > 1) {  // branch-free lower bound over the sorted copy
-          int half = n >> 1;
-          lo = T[lo + half - 1] < x ? lo + half : lo;
-          n -= half;
-        }
-        return T[lo] == x;
-      });
-      __syncwarp();
-      for (int j = lane; j < dh; j += 32) T[j] = -1;
-    } else {
-      uint32_t cap = 64;
-      while (cap < 4u * (uint32_t)dh) cap <<= 1;
-      const uint32_t mask = cap - 1;
-      for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
-      __syncwarp();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
-                            [&](int32_t x) -> unsigned { return hash_has(T, mask, x); });
-      __syncwarp();
-      for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
-    }
-    __syncwarp();
-    total += cnt;
-  }
-  warp_add_count(total, out);
-}
-
-__global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
-                                                                   const GroupItem* items, int nitems, int* next,
-                                                                   uint32_t tab_words, unsigned long long* out) {
-  extern __shared__ int32_t tab[];  // tab_words
-  __shared__ int sx[kBgWarps][32];
-  __shared__ int64_t sp[kBgWarps][32];
-  __shared__ int cur_item;
-  __shared__ unsigned long long bnext;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (uint32_t j = threadIdx.x; j < tab_words; j += blockDim.x) tab[j] = -1;
-  unsigned long long total = 0;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      cur_item = atomicAdd(next, 1);
-      bnext = 0;
-    }
-    __syncthreads();
-    const int it = cur_item;
-    if (it >= nitems) break;
-    const GroupItem gi = items[it];
-    const int64_t hb = g.off[gi.h];
-    const int64_t dh = g.off[gi.h + 1] - hb;
-    const int32_t* Nh = g.cols + hb;
-    // partner batches of 32 handed out to the warps as they finish
-    auto nb = [&]() {
-      unsigned long long r = 0;
-      if (lane == 0) r = atomicAdd(&bnext, 32ull);
-      return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
-    };
-    unsigned cnt = 0;
-    if (gi.mode == 0) {
-      uint32_t cap = 64;
-      while (cap < 4u * (uint32_t)dh) cap <<= 1;
-      const uint32_t mask = cap - 1;
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
-      __syncthreads();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
-                            [&](int32_t x) -> unsigned { return hash_has(tab, mask, x); });
-      __syncthreads();
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
-    } else if (gi.mode == 1) {
-      const int32_t lo = Nh[0], hi = Nh[dh - 1];
-      const int words = ((hi - lo) >> 5) + 1;
-      uint32_t* bits = reinterpret_cast<uint32_t*>(tab);
-      for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0u;
-      __syncthreads();
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) {
-        int32_t x = Nh[j] - lo;
-        atomicOr(&bits[x >> 5], 1u << (x & 31));
-      }
-      __syncthreads();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
-        if (x < lo || x > hi) return 0u;
-        x -= lo;
-        return (bits[x >> 5] >> (x & 31)) & 1u;
-      });
-      __syncthreads();
-      for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0xffffffffu;  // back to empty slots (-1)
-    } else {
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
-        int64_t lo = 0, hi = dh;
-        while (lo < hi) {
-          int64_t mid = (lo + hi) >> 1;
-          if (Nh[mid] < x) lo = mid + 1; else hi = mid;
-        }
-        return lo < dh && Nh[lo] == x;
-      });
-    }
-    __syncthreads();
-    total += cnt;
-  }
-  warp_add_count(total, out);
-}
-
-int blocks_per_sm(const void* kernel, int block, size_t smem) {
-  int b = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, block, smem) != cudaSuccess || b < 1) b = 1;
-  return b;
-}
 
 }  // namespace
 
@@ -753,7 +407,8 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   DevBuf<GroupItem> witems, bitems;
   ATC_TRY(witems.alloc(max_items, s));
   ATC_TRY(bitems.alloc(max_items, s));
-  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p, cutover);
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p,
+                                                        default_shape(cutover));
   ATC_CK(cudaGetLastError());
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
@@ -766,18 +421,20 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
     while (words < 4u * (uint32_t)hc[3]) words <<= 1;
     if (words > (uint32_t)kTabWords) words = kTabWords;
     size_t smem = sizeof(int32_t) * words;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_block_kernel, kBgWarps * 32, smem);
+    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems>, kBgWarps * 32, smem);
     int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, bitems.p, hc[1], counters.p + 5, words, ctr);
+    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, FullItems{bitems.p}, hc[1], nullptr, counters.p + 5, words,
+                                                          GraphTags{nullptr, 0, nullptr}, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
   if (hc[0]) {
-    int bps = blocks_per_sm((const void*)bisson_warp_kernel, kBgWarps * 32, 0);
+    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems>, kBgWarps * 32, 0);
     int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
-    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist.p, witems.p, hc[0], counters.p + 4, ctr);
+    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist.p, FullItems{witems.p}, hc[0], nullptr, counters.p + 4,
+                                                      GraphTags{nullptr, 0, nullptr}, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
@@ -922,7 +579,7 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
   group_count_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, cnt);
   scan_one_block_kernel<<<1, 1024, 0, s>>>(cnt, n + 1, gstart);
   group_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, gstart, cur, plist);
-  group_items_kernel<<<grid_for(n, 256), 256, 0, s>>>(g, gstart, witems, bitems, counters, 32);
+  group_items_kernel<<<grid_for(n, 256), 256, 0, s>>>(g, gstart, witems, bitems, counters, default_shape(32));
   ATC_CK(cudaGetLastError());
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
@@ -932,17 +589,19 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
     while (words < 4u * (uint32_t)hc[3]) words <<= 1;
     if (words > (uint32_t)kTabWords) words = kTabWords;
     size_t smem = sizeof(int32_t) * words;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_block_kernel, kBgWarps * 32, smem);
+    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems>, kBgWarps * 32, smem);
     int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist, bitems, hc[1], counters + 5, words, total_ctr);
+    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, words,
+                                                          GraphTags{nullptr, 0, nullptr}, total_ctr);
     ATC_CK(cudaGetLastError());
   }
   if (hc[0]) {
-    int bps = blocks_per_sm((const void*)bisson_warp_kernel, kBgWarps * 32, 0);
+    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems>, kBgWarps * 32, 0);
     int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
-    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist, witems, hc[0], counters + 4, total_ctr);
+    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist, FullItems{witems}, hc[0], nullptr, counters + 4,
+                                                      GraphTags{nullptr, 0, nullptr}, total_ctr);
     ATC_CK(cudaGetLastError());
   }
   unsigned long long h = 0;

@@ -76,7 +76,10 @@ typedef struct atc_tuning {
   int32_t fox_rearrange;     /* interleave each bin's edges (Fox/tc.cu:127-183) */
   int32_t fox_work_per_thread; /* bin base of the threads-per-edge bins (8) */
   int32_t tricore_blocks;    /* CTAs of the TriCore-style kernel (0: auto) */
-  int32_t reserved[9];
+  int32_t bisson_warp_max;   /* longest list a warp item handles, <= 256 (256) */
+  int32_t bisson_warp_chunk; /* partners per warp item (512) */
+  int32_t bisson_block_chunk; /* partners per block item (2048) */
+  int32_t reserved[6];
 } atc_tuning;
 
 /* Oriented CSR on the device (the reference's edgeOffset/edgeRow/adjLength globals,
@@ -130,6 +133,12 @@ atc_status atc_gen_rgg_host(uint32_t n, double mean_degree, uint64_t seed, int32
                             uint64_t* n_out, int nthreads);
 atc_status atc_gen_rgg_device(uint32_t n, double mean_degree, uint64_t seed, int32_t* out_pairs_dev,
                               uint64_t capacity, uint64_t* n_out, atc_stream s);
+/* Chung-Lu (expected-degree) graph on the device: n vertices, power-law weights with
+   exponent gamma (> 1.05) and mean degree mean_degree, each edge once as (u, v), u < v,
+   in row order.  *n_out = edges; with out == NULL only counts.  ATC_ERR_INVALID above
+   `capacity` pairs.  Deterministic for one device type (floating-point weights). */
+atc_status atc_gen_chunglu_device(uint32_t n, double gamma, double mean_degree, uint64_t seed, int32_t* out_pairs_dev,
+                                  uint64_t capacity, uint64_t* n_out, atc_stream s);
 /* Drops self-loops and repeats; writes each undirected edge once as (min,max) sorted,
    or, with symmetric != 0, both directions sorted by (src,dst).  Capacity of `out`:
    2*n_pairs pairs when symmetric, else n_pairs. */
@@ -191,6 +200,32 @@ atc_status atc_tc_noalloc(const int64_t* offsets_dev, const int32_t* cols_dev, i
 /* k-clique count (k >= 3) of the oriented CSR, exact in uint64.  Replaces
    kcl_gpu_solver(std::string, unsigned k, AccType& total, size_t) (k-clique/kcl.h:6-7). */
 atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream s);
+
+/* ---- batched counting --------------------------------------------------------------
+   Many graphs of uneven sizes counted together.  No counterpart in the reference, which
+   runs one program per graph.  The batch keeps the graphs as one disjoint union on the
+   device (vertex and edge ranges per graph); atc_batch_run counts every graph in one
+   replay of a CUDA graph that holds the whole Bisson-style pipeline (grouping passes and
+   the persistent, work-queue-driven counting kernels), with per-graph counters.  The
+   captured graph is rebuilt when the batch or the item shape changes. */
+typedef struct atc_batch atc_batch;
+atc_status atc_batch_create(atc_batch** out);
+/* Optional: preallocates room for `n` vertices and `m` edges in total, so that adding
+   graphs never regrows the union (regrowth briefly needs the old and the new arrays). */
+atc_status atc_batch_reserve(atc_batch* b, int64_t n, int64_t m, atc_stream s);
+/* Appends a copy of `csr` (device to device; the caller keeps and frees its csr).
+   *index (nullable) receives the graph's position in the batch. */
+atc_status atc_batch_add(atc_batch* b, const atc_csr* csr, int32_t* index, atc_stream s);
+/* Counts every graph; counts (host, one per graph).  `tuning` (nullable) sets the item
+   shape (bisson_cutover, bisson_warp_max, bisson_warp_chunk, bisson_block_chunk). */
+atc_status atc_batch_run(atc_batch* b, const atc_tuning* tuning, uint64_t* counts, atc_stats* stats, atc_stream s);
+/* Autotuner: runs each of `n` candidate tunings (two timed replays each), keeps the
+   fastest as the batch's shape.  *best = its index; ms (nullable, n floats) = times. */
+atc_status atc_batch_tune(atc_batch* b, const atc_tuning* candidates, int32_t n, int32_t* best, float* ms,
+                          atc_stream s);
+/* Graphs, vertices and edges held. */
+atc_status atc_batch_info(const atc_batch* b, int32_t* graphs, int64_t* n, int64_t* m);
+atc_status atc_batch_destroy(atc_batch* b);
 
 /* ---- orientation-cost figures ----------------------------------------------------- */
 /* costFuncCal <file> <k> (tools/costFuncCal.cpp:15-88): out = {idPartCost,

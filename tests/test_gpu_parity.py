@@ -315,3 +315,57 @@ def test_kcl_rgg_matches_oracle(k):
     g = atc.gen_rgg(1 << 14, 32.0, 2)
     csr = atc.pretc(g, atc.Dir.ADIRECTION)
     assert atc.kcl(csr, k)[0] == oracle.kclique(g, k)
+
+
+# ---- batched counting ---------------------------------------------------------------------------
+def _batch_graphs():
+    import torch
+    gs = [atc.rmat_graph(10, 16, 1), atc.gen_rgg(3000, 20.0, 4), np.zeros((0, 2), dtype=np.int32),
+          np.array([(a, b) for a in range(4) for b in range(4) if a != b], dtype=np.int32),
+          atc.rmat_graph(12, 8, 2)]
+    for n, gamma, d, seed in ((2000, 2.1, 16.0, 1), (50000, 2.5, 40.0, 2), (300, 3.0, 8.0, 3)):
+        gs.append(atc.gen_chunglu_device(n, gamma, d, seed).cpu().numpy())
+    hub = [(0, i) for i in range(1, 3001)] + [(a, b) for a in range(1, 61) for b in range(a + 1, 61)]
+    gs.append(np.array(hub, dtype=np.int32))
+    return gs
+
+
+def test_batch_counts_match_per_graph():
+    gs = _batch_graphs()
+    want = [oracle.tc_count(g) if g.size else 0 for g in gs]
+    b = atc.Batch()
+    for i, g in enumerate(gs):
+        d = (atc.Dir.ADIRECTION, atc.Dir.DEGREE, atc.Dir.ID)[i % 3]
+        assert b.add(atc.pretc(g, d)) == i
+    counts, st = b.run()
+    assert counts.tolist() == want
+    counts2, _ = b.run()  # a second replay of the same captured graph
+    assert counts2.tolist() == want
+    for t in ({"bisson_cutover": 8, "bisson_warp_max": 64}, {"bisson_warp_chunk": 32, "bisson_block_chunk": 64},
+              {"bisson_warp_max": 256, "bisson_cutover": 256}):
+        assert b.run(tuning=t)[0].tolist() == want, t
+    best, ms = b.tune([{}, {"bisson_warp_max": 128}, {"bisson_block_chunk": 256}])
+    assert 0 <= best < 3 and np.all(ms > 0)
+    assert b.run()[0].tolist() == want
+    # graphs added after a run rebuild the pipeline
+    extra = atc.rmat_graph(11, 16, 9)
+    b.add(atc.pretc(extra, atc.Dir.DEGREE))
+    assert b.run()[0].tolist() == want + [oracle.tc_count(extra)]
+
+
+def test_batch_reserve_and_empty():
+    b = atc.Batch()
+    assert b.run()[0].tolist() == []
+    b.reserve(10000, 100000)
+    g = atc.rmat_graph(9, 8, 3)
+    b.add(atc.pretc(g, atc.Dir.DEGREE))
+    assert b.run()[0].tolist() == [oracle.tc_count(g)]
+
+
+def test_chunglu_generator_shape():
+    g = atc.gen_chunglu_device(100000, 2.5, 20.0, 7).cpu().numpy()
+    assert np.all(g[:, 0] < g[:, 1]) and g.min() >= 0 and g.max() < 100000
+    mean_deg = 2 * g.shape[0] / 100000
+    assert 12.0 < mean_deg < 24.0, mean_deg
+    g2 = atc.gen_chunglu_device(100000, 2.5, 20.0, 7).cpu().numpy()
+    assert np.array_equal(g, g2)
