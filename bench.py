@@ -51,8 +51,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernels", default="hu,bisson,fox,tricore", help="families timed besides the headline")
-    ap.add_argument("--mode", default="tc", choices=["tc", "kcl"],
-                    help="tc: the headline (BASELINE config 2); kcl: k-clique counts (config 3)")
+    ap.add_argument("--mode", default="tc", choices=["tc", "kcl", "batch"],
+                    help="tc: the headline (BASELINE config 2); kcl: k-clique counts (config 3); "
+                         "batch: many Chung-Lu graphs, batched vs per-graph loop (config 4)")
+    ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--batch-select", action="store_true",
+                    help="batched path picks each graph's orientation (degree or A-direction) by its work estimate")
     ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-5,rmat:14:6-7",
                     help="comma list of kind:log2size:kmin-kmax (kind rmat or rgg)")
     return ap.parse_args()
@@ -405,8 +409,101 @@ def run_kcl(a):
                       "peak_source": kind, "graphs": out}), flush=True)
 
 
+def batch_params(count, seed):
+    """Seeded Chung-Lu parameters: gamma ~ U[2,3], n log-uniform in [1e3, 2e6], mean degree ~ U[4,64]."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(count):
+        gamma = rng.uniform(2.0, 3.0)
+        n = int(round(math.exp(rng.uniform(math.log(1e3), math.log(2e6)))))
+        d = rng.uniform(4.0, 64.0)
+        out.append((n, gamma, min(d, n / 4.0)))
+    return out
+
+
+def run_batch(a):
+    """Batched TC (BASELINE config 4): one CUDA-graph replay for all graphs vs a per-graph loop."""
+    import ctypes as C
+    import torch
+    import atc
+    torch.cuda.set_device(0)
+    atc.init(0)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    params = batch_params(a.batch_graphs, a.seed)
+    # sizes first, so the batch's union is allocated once
+    tot_n = tot_m = 0
+    for i, (n, gamma, d) in enumerate(params):
+        cnt = C.c_uint64(0)
+        assert atc.lib().atc_gen_chunglu_device(n, gamma, d, a.seed * 100003 + i, None, 0, C.byref(cnt), sp) == 0
+        tot_n += n
+        tot_m += int(cnt.value)
+    batch = atc.Batch()
+    batch.reserve(tot_n, tot_m, stream=sp)
+    plain_ms = []
+    plain_counts = []
+    dirs = []
+    kfixed = atc.Kernel.BISSON
+    t_setup = time.perf_counter()
+    for i, (n, gamma, d) in enumerate(params):
+        pairs = atc.gen_chunglu_device(n, gamma, d, a.seed * 100003 + i, stream=sp)
+        csr = atc.pretc_device(pairs.data_ptr(), pairs.shape[0], atc.Dir.ADIRECTION, stream=sp)
+        atc.tc(csr, kfixed, stream=sp)  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c, _ = atc.tc(csr, kfixed, stream=sp)
+        plain_ms.append((time.perf_counter() - t0) * 1e3)
+        plain_counts.append(c)
+        chosen = csr
+        dsel = "A-direction"
+        if a.batch_select:
+            alt = atc.pretc_device(pairs.data_ptr(), pairs.shape[0], atc.Dir.DEGREE, stream=sp)
+            if alt.wedges_min < csr.wedges_min:
+                chosen, dsel = alt, "degree"
+        dirs.append(dsel)
+        batch.add(chosen, stream=sp)
+        csr.free()
+        if chosen is not csr:
+            chosen.free()
+        del pairs
+    setup_s = time.perf_counter() - t_setup
+    ng, n_all, m_all = batch.info()
+    cands = [{}, {"bisson_warp_max": 128}, {"bisson_warp_max": 64, "bisson_cutover": 16},
+             {"bisson_warp_chunk": 256, "bisson_block_chunk": 1024}, {"bisson_warp_chunk": 2048, "bisson_block_chunk": 8192},
+             {"bisson_cutover": 64}]
+    best, tune_ms = batch.tune(cands, stream=sp)
+    counts, _ = batch.run(stream=sp)
+    assert counts.tolist() == plain_counts, "batched and per-graph counts differ"
+    times = []
+    for _ in range(max(1, a.steps)):
+        _, st = batch.run(stream=sp)
+        times.append(st.kernel_ms)
+    batch_ms = statistics.mean(times)
+    plain_total = sum(plain_ms)
+    line = {
+        "mode": "batch", "metric": "graphs/s, batched (one CUDA-graph replay, autotuned items) vs per-graph loop",
+        "unit": "graphs/s", "dtype": "int32", "data": "synthetic Chung-Lu graphs generated on the device",
+        "graphs": ng, "vertices": n_all, "edges": m_all, "triangles": int(sum(plain_counts)),
+        "plain": {"kernel": "bisson (atc_tc per graph, host-synchronised)", "direction": "A-direction",
+                  "ms_total": plain_total, "graphs_per_s": ng / (plain_total * 1e-3),
+                  "edges_per_s": m_all / (plain_total * 1e-3)},
+        "batched": {"ms_per_replay": batch_ms, "graphs_per_s": ng / (batch_ms * 1e-3),
+                    "edges_per_s": m_all / (batch_ms * 1e-3), "tuned": cands[best],
+                    "tune_ms": [float(x) for x in tune_ms], "selection": "work estimate" if a.batch_select else "none",
+                    "degree_chosen": dirs.count("degree")},
+        "speedup_graphs_per_s": plain_total / batch_ms,
+        "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.mode == "batch":
+        run_batch(a)
+        return
     if a.mode == "kcl":
         run_kcl(a)
         return
