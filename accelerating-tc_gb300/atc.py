@@ -142,6 +142,16 @@ _SIGS = {
     "atc_batch_tune": (C.c_int, [C.c_void_p, _P, C.c_int32, C.POINTER(C.c_int32), _P, _P]),
     "atc_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "atc_batch_destroy": (C.c_int, [C.c_void_p]),
+    "atc_mlp_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "atc_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "atc_mlp_params": (C.c_int, [C.c_void_p, _P, _P, C.POINTER(C.c_int64)]),
+    "atc_mlp_scaling": (C.c_int, [C.c_void_p, _P, _P, _P, _P]),
+    "atc_mlp_forward": (C.c_int, [C.c_void_p, _P, C.c_int32, _P, _P]),
+    "atc_mlp_gradients": (C.c_int, [C.c_void_p, _P, _P, _P, C.c_int32, _P, _P, _P]),
+    "atc_mlp_train": (C.c_int, [C.c_void_p, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                _P, _P]),
+    "atc_graph_features": (C.c_int, [_P, C.c_uint64, _P, _P]),
+    "atc_select": (C.c_int, [C.c_void_p, _P, C.POINTER(C.c_int32), _P, _P]),
     "atc_costfunc": (C.c_int, [_P, C.c_uint64, C.c_int32, _P, _P]),
     "atc_verification": (C.c_int, [_P, C.c_uint64, _P, _P]),
 }
@@ -385,6 +395,84 @@ class Batch:
             self.free()
         except Exception:
             pass
+
+
+class MLP:
+    """The selector network (atc_mlp_*): FP32, trained and run on the GPU."""
+
+    def __init__(self, n_in=6, hidden=64, n_out=24, seed=1):
+        h = C.c_void_p()
+        _check(lib().atc_mlp_create(n_in, hidden, n_out, seed, C.byref(h)))
+        self._h, self.n_in, self.hidden, self.n_out = h, n_in, hidden, n_out
+
+    def params(self, new=None):
+        cnt = C.c_int64(0)
+        _check(lib().atc_mlp_params(self._h, None, None, C.byref(cnt)))
+        if new is not None:
+            new = np.ascontiguousarray(new, dtype=np.float32)
+            assert new.size == cnt.value
+            _check(lib().atc_mlp_params(self._h, None, _ptr(new), C.byref(cnt)))
+        out = np.empty(cnt.value, dtype=np.float32)
+        _check(lib().atc_mlp_params(self._h, _ptr(out), None, C.byref(cnt)))
+        return out
+
+    def scaling(self, mean=None, std=None):
+        if mean is not None:
+            mean = np.ascontiguousarray(mean, dtype=np.float32)
+            std = np.ascontiguousarray(std, dtype=np.float32)
+            _check(lib().atc_mlp_scaling(self._h, None, None, _ptr(mean), _ptr(std)))
+        m = np.empty(self.n_in, dtype=np.float32)
+        s = np.empty(self.n_in, dtype=np.float32)
+        _check(lib().atc_mlp_scaling(self._h, _ptr(m), _ptr(s), None, None))
+        return m, s
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        y = np.empty((x.shape[0], self.n_out), dtype=np.float32)
+        _check(lib().atc_mlp_forward(self._h, _ptr(x), x.shape[0], _ptr(y), None))
+        return y
+
+    def gradients(self, x, t, mask=None):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, self.n_out)
+        mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        g = np.empty(self.params().size, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(lib().atc_mlp_gradients(self._h, _ptr(x), _ptr(t), _ptr(mask), x.shape[0], _ptr(g), _ptr(loss), None))
+        return float(loss[0]), g
+
+    def train(self, x, t, mask=None, epochs=200, batch=256, lr=3e-3, seed=1):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, self.n_out)
+        mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(lib().atc_mlp_train(self._h, _ptr(x), _ptr(t), _ptr(mask), x.shape[0], epochs, batch, lr, seed,
+                                   _ptr(loss), None))
+        return float(loss[0])
+
+    def select(self, features):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        ch = C.c_int32(0)
+        y = np.empty(self.n_out, dtype=np.float32)
+        _check(lib().atc_select(self._h, _ptr(f), C.byref(ch), _ptr(y), None))
+        return ch.value, y
+
+    def free(self):
+        if self._h:
+            lib().atc_mlp_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def graph_features(pairs_dev_ptr, n_pairs, stream=None):
+    out = np.zeros(6, dtype=np.float32)
+    _check(lib().atc_graph_features(C.c_void_p(pairs_dev_ptr), n_pairs, _ptr(out), stream))
+    return out
 
 
 def gen_chunglu_device(n, gamma, mean_degree, seed, stream=None):

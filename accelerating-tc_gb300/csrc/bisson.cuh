@@ -123,28 +123,56 @@ __host__ __device__ inline int64_t max_items(int64_t n, int64_t partners, int mi
   return n + partners / min_chunk + 1;
 }
 
+// Reserves k slots of counter `*ctr` for every lane of the warp with one atomic: returns
+// this lane's first slot.  All 32 lanes call it (k may be 0).
+__device__ __forceinline__ int warp_reserve(int* ctr, int k) {
+  const int lane = threadIdx.x & 31;
+  int incl = k;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  int total = __shfl_sync(0xffffffffu, incl, 31);
+  int base = 0;
+  if (lane == 31 && total) base = atomicAdd(ctr, total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return base + incl - k;
+}
+
+// One lane per vertex h; the loop bound is padded to whole warps so that every lane of a
+// warp takes part in warp_reserve.
 __global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* witems, GroupItem* bitems,
                                    int* counters, ItemShape sh) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
-    int64_t b = gstart[h], e = gstart[h + 1];
-    if (b == e) continue;
-    int64_t hb = g.off[h], dh = g.off[h + 1] - hb;
-    if (dh <= sh.warp_max) {
+  int64_t n_pad = (g.n + 31) & ~31ll;
+  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < n_pad; h += stride) {
+    int64_t b = 0, e = 0, hb = 0, dh = 0;
+    if (h < g.n) {
+      b = gstart[h];
+      e = gstart[h + 1];
+      hb = g.off[h];
+      dh = g.off[h + 1] - hb;
+    }
+    const bool any = e > b;
+    const bool warp = dh <= sh.warp_max;
+    const int kw = any && warp ? (int)((e - b + sh.warp_chunk - 1) / sh.warp_chunk) : 0;
+    const int kb = any && !warp ? (int)((e - b + sh.block_chunk - 1) / sh.block_chunk) : 0;
+    const int atw = warp_reserve(&counters[0], kw);
+    const int atb = warp_reserve(&counters[1], kb);
+    if (kw) {
       int32_t mode = dh <= sh.cutover ? 0 : 1;
-      int64_t k = (e - b + sh.warp_chunk - 1) / sh.warp_chunk;
-      int at = atomicAdd(&counters[0], (int)k);
-      for (int64_t c = 0; c < k; ++c)
-        witems[at + c] = GroupItem{(int32_t)h, mode, b + c * sh.warp_chunk, min(e, b + (c + 1) * sh.warp_chunk)};
-    } else {
+      for (int c = 0; c < kw; ++c)
+        witems[atw + c] = GroupItem{(int32_t)h, mode, b + c * (int64_t)sh.warp_chunk,
+                                    min(e, b + (c + 1) * (int64_t)sh.warp_chunk)};
+    }
+    if (kb) {
       int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
       int32_t mode = dh <= kHashMax ? 0 : (span < kTabWords * 32 ? 1 : 2);
-      if (mode == 0) atomicMax(&counters[3], (int)dh);
-      else atomicMax(&counters[3], kHashMax);
-      int64_t k = (e - b + sh.block_chunk - 1) / sh.block_chunk;
-      int at = atomicAdd(&counters[1], (int)k);
-      for (int64_t c = 0; c < k; ++c)
-        bitems[at + c] = GroupItem{(int32_t)h, mode, b + c * sh.block_chunk, min(e, b + (c + 1) * sh.block_chunk)};
+      atomicMax(&counters[3], mode == 0 ? (int)dh : kHashMax);
+      for (int c = 0; c < kb; ++c)
+        bitems[atb + c] = GroupItem{(int32_t)h, mode, b + c * (int64_t)sh.block_chunk,
+                                    min(e, b + (c + 1) * (int64_t)sh.block_chunk)};
     }
   }
 }
@@ -235,19 +263,23 @@ __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_
 __global__ void group_items_compact_kernel(CsrView g, const int64_t* gstart, int2* items, int64_t cap, int* counters,
                                            ItemShape sh) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < g.n; h += stride) {
-    int64_t b = gstart[h], e = gstart[h + 1];
-    if (b == e) continue;
-    int64_t dh = g.off[h + 1] - g.off[h];
-    bool warp = dh <= sh.warp_max;
-    int64_t chunk = warp ? sh.warp_chunk : sh.block_chunk;
-    int k = (int)((e - b + chunk - 1) / chunk);
-    int at = atomicAdd(&counters[warp ? 0 : 1], k);
-    if (!warp) atomicMax(&counters[3], (int)min(dh, (int64_t)kHashMax));
-    for (int c = 0; c < k; ++c) {
-      int64_t slot = warp ? (int64_t)at + c : cap - 1 - ((int64_t)at + c);
-      items[slot] = make_int2((int32_t)h, c);
+  int64_t n_pad = (g.n + 31) & ~31ll;
+  for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < n_pad; h += stride) {
+    int64_t b = 0, e = 0, dh = 0;
+    if (h < g.n) {
+      b = gstart[h];
+      e = gstart[h + 1];
+      dh = g.off[h + 1] - g.off[h];
     }
+    const bool any = e > b;
+    const bool warp = dh <= sh.warp_max;
+    const int kw = any && warp ? (int)((e - b + sh.warp_chunk - 1) / sh.warp_chunk) : 0;
+    const int kb = any && !warp ? (int)((e - b + sh.block_chunk - 1) / sh.block_chunk) : 0;
+    const int atw = warp_reserve(&counters[0], kw);
+    const int atb = warp_reserve(&counters[1], kb);
+    for (int c = 0; c < kw; ++c) items[(int64_t)atw + c] = make_int2((int32_t)h, c);
+    if (kb) atomicMax(&counters[3], (int)min(dh, (int64_t)kHashMax));
+    for (int c = 0; c < kb; ++c) items[cap - 1 - ((int64_t)atb + c)] = make_int2((int32_t)h, c);
   }
 }
 

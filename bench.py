@@ -51,10 +51,13 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernels", default="hu,bisson,fox,tricore", help="families timed besides the headline")
-    ap.add_argument("--mode", default="tc", choices=["tc", "kcl", "batch"],
+    ap.add_argument("--mode", default="tc", choices=["tc", "kcl", "batch", "select"],
                     help="tc: the headline (BASELINE config 2); kcl: k-clique counts (config 3); "
                          "batch: many Chung-Lu graphs, batched vs per-graph loop (config 4)")
     ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--select-train", type=int, default=2048, help="training graphs of the selector")
+    ap.add_argument("--select-eval", type=int, default=512, help="held-out graphs of the selector")
+    ap.add_argument("--select-out", default="", help="write features and timings (.npz) here")
     ap.add_argument("--batch-plain-kernels", default="bisson",
                     help="fixed kernels timed in the per-graph loop (the first is the reference line)")
     ap.add_argument("--batch-select", action="store_true",
@@ -511,8 +514,156 @@ def run_batch(a):
     print(json.dumps(line), flush=True)
 
 
+SEL_DIRS = ("ID", "DEGREE", "ADIRECTION")
+SEL_ORDERS = ("NONE", "AORDER")
+SEL_KERNELS = ("HU", "BISSON", "FOX", "TRICORE")
+
+
+def triple_name(i):
+    d, rest = divmod(i, len(SEL_ORDERS) * len(SEL_KERNELS))
+    o, k = divmod(rest, len(SEL_KERNELS))
+    return "%s/%s/%s" % (SEL_DIRS[d], SEL_ORDERS[o], SEL_KERNELS[k])
+
+
+def tail_cost(off, m):
+    """costFuncCal's tail cost (tools/costFuncCal.cpp:66-81, k = 1) of an orientation."""
+    n = off.size - 1
+    avg = m / max(n, 1)
+    dout = np.diff(off).astype(np.float64)
+    sel = dout - avg > avg
+    return float(np.abs(dout[sel] - avg).sum())
+
+
+def select_graphs(count, seed):
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for i in range(count):
+        if i % 2 == 0:
+            n = int(round(math.exp(rng.uniform(math.log(1e3), math.log(2e5)))))
+            out.append(("cl", n, rng.uniform(2.0, 3.0), min(rng.uniform(4.0, 64.0), n / 4.0)))
+        else:
+            out.append(("rmat", rng.randint(10, 17), rng.choice((8, 16, 32)), None))
+    return out
+
+
+def measure_graph(spec, gseed, sp):
+    """Features, preTC+count time of every triple (inf where undefined), costs, count."""
+    import atc
+    kind, p1, p2, p3 = spec
+    if kind == "cl":
+        pairs = atc.gen_chunglu_device(p1, p2, p3, gseed, stream=sp)
+    else:
+        import torch
+        pairs = torch.empty(((p2 << p1), 2), dtype=torch.int32, device="cuda")
+        assert atc.lib().atc_gen_rmat_device(p1, p2, *atc.GRAPH500, gseed, pairs.data_ptr(), sp) == 0
+    npairs = pairs.shape[0]
+    feats = atc.graph_features(pairs.data_ptr(), npairs, stream=sp)
+    T = len(SEL_DIRS) * len(SEL_ORDERS) * len(SEL_KERNELS)
+    times = np.full(T, np.inf)
+    costs = np.zeros(len(SEL_DIRS))
+    counts = set()
+    for di, d in enumerate(SEL_DIRS):
+        for oi, o in enumerate(SEL_ORDERS):
+            t0 = time.perf_counter()
+            try:
+                csr = atc.pretc_device(pairs.data_ptr(), npairs, atc.Dir[d], atc.Order[o], stream=sp)
+            except atc.ATCError as e:
+                if e.status == atc.Status.ERR_UNSUPPORTED:
+                    continue
+                raise
+            t_pre = time.perf_counter() - t0
+            if o == "NONE":
+                off, _ = csr.to_host()
+                costs[di] = tail_cost(off, csr.m)
+            for ki, k in enumerate(SEL_KERNELS):
+                t0 = time.perf_counter()
+                c, _ = atc.tc(csr, atc.Kernel[k], stream=sp)
+                times[(di * len(SEL_ORDERS) + oi) * len(SEL_KERNELS) + ki] = (t_pre + time.perf_counter() - t0) * 1e3
+                counts.add(c)
+            csr.free()
+    assert len(counts) == 1, ("triples disagree", spec, counts)
+    return feats, times, costs, counts.pop()
+
+
+def evaluate_policies(times, choices):
+    """Total time of each policy (dict name -> per-graph triple index) and its regret."""
+    best = times.min(axis=1)
+    out = {"oracle_best": {"ms": float(best.sum())}}
+    for name, ch in choices.items():
+        t = times[np.arange(times.shape[0]), ch]
+        out[name] = {"ms": float(t.sum()), "regret": float(t.sum() / best.sum()),
+                     "picked_best": float(np.mean(t <= best * 1.0000001))}
+    return out
+
+
+def selector_policies(train_t, eval_t, eval_costs, preds):
+    """Choices of the non-learned baselines and of the network on the held-out graphs."""
+    T = train_t.shape[1]
+    finite = np.where(np.isfinite(train_t), train_t, np.nan)
+    best_fixed = int(np.nanargmin(np.nansum(np.log(finite), axis=0) + np.isnan(finite).sum(axis=0) * 1e9))
+    default = (SEL_DIRS.index("ADIRECTION") * len(SEL_ORDERS) + SEL_ORDERS.index("NONE")) * len(SEL_KERNELS) + \
+        SEL_KERNELS.index("BISSON")
+    cost_dir = eval_costs.argmin(axis=1)
+    cost_choice = (cost_dir * len(SEL_ORDERS) + SEL_ORDERS.index("NONE")) * len(SEL_KERNELS) + SEL_KERNELS.index("BISSON")
+    learned = np.where(np.isfinite(eval_t), preds, np.inf).argmin(axis=1)
+    n = eval_t.shape[0]
+    return {"fixed_default": np.full(n, default), "best_fixed_on_train": np.full(n, best_fixed),
+            "cost_function": cost_choice, "learned": learned}, default, best_fixed
+
+
+def run_select(a):
+    """Learned (direction, ordering, kernel) selection (BASELINE config 5)."""
+    import torch
+    import atc
+    torch.cuda.set_device(0)
+    atc.init(0)
+    sp = torch.cuda.current_stream().cuda_stream
+    specs = select_graphs(a.select_train + a.select_eval, a.seed)
+    measure_graph(("rmat", 10, 8, None), 999, sp)  # warm-up: module load, pools
+    feats, times, costs = [], [], []
+    t0 = time.perf_counter()
+    for i, spec in enumerate(specs):
+        f, t, c, _ = measure_graph(spec, a.seed * 7919 + i, sp)
+        feats.append(f)
+        times.append(t)
+        costs.append(c)
+    gen_s = time.perf_counter() - t0
+    feats, times, costs = np.array(feats, np.float32), np.array(times), np.array(costs)
+    if a.select_out:
+        np.savez_compressed(a.select_out, features=feats, times_ms=times, costs=costs,
+                            triples=np.array([triple_name(i) for i in range(times.shape[1])]))
+    ntr = a.select_train
+    result = train_and_evaluate(feats, times, costs, ntr, seed=a.seed)
+    result.update({"mode": "select", "graphs_train": ntr, "graphs_eval": len(specs) - ntr,
+                   "measure_s": gen_s, "data": "seeded Chung-Lu (n log-uniform 1e3..2e5) and R-MAT (scale 10..17)"})
+    print(json.dumps(result), flush=True)
+
+
+def train_and_evaluate(feats, times, costs, ntr, seed=1, epochs=300):
+    """Trains the selector on the first ntr graphs, evaluates the policies on the rest."""
+    import atc
+    T = times.shape[1]
+    mask = np.isfinite(times).astype(np.float32)
+    target = np.where(mask > 0, np.log(np.where(mask > 0, times, 1.0)), 0.0).astype(np.float32)
+    net = atc.MLP(6, 64, T, seed=seed)
+    loss = net.train(feats[:ntr], target[:ntr], mask[:ntr], epochs=epochs, batch=256, lr=3e-3, seed=seed)
+    preds = net.forward(feats[ntr:])
+    choices, default, best_fixed = selector_policies(times[:ntr], times[ntr:], costs[ntr:], preds)
+    ev = evaluate_policies(times[ntr:], choices)
+    return {"metric": "total preTC+count time on held-out graphs by selection policy", "unit": "ms",
+            "final_train_loss": loss, "default_triple": triple_name(default),
+            "best_fixed_triple": triple_name(best_fixed), "policies": ev,
+            "learned_vs_cost_function": ev["cost_function"]["ms"] / ev["learned"]["ms"],
+            "learned_vs_default": ev["fixed_default"]["ms"] / ev["learned"]["ms"]}
+
+
 def main():
     a = parse()
+    if a.mode == "select":
+        run_select(a)
+        return
     if a.mode == "batch":
         run_batch(a)
         return

@@ -227,6 +227,36 @@ atc_status atc_batch_tune(atc_batch* b, const atc_tuning* candidates, int32_t n,
 atc_status atc_batch_info(const atc_batch* b, int32_t* graphs, int64_t* n, int64_t* m);
 atc_status atc_batch_destroy(atc_batch* b);
 
+/* ---- learned (direction, ordering, kernel) selection --------------------------------
+   No counterpart in the reference.  A small FP32 MLP (n_in -> hidden ReLU -> hidden ReLU
+   -> n_out), trained and evaluated on the GPU by the library's own kernels; the
+   selector reads graph statistics and predicts one log-time per candidate triple. */
+typedef struct atc_mlp atc_mlp;
+/* He-uniform weights from `seed`, zero biases. */
+atc_status atc_mlp_create(int32_t n_in, int32_t hidden, int32_t n_out, uint64_t seed, atc_mlp** out);
+atc_status atc_mlp_destroy(atc_mlp* net);
+/* Parameter vector (layout W1[in][h] b1 W2[h][h] b2 W3[h][out] b3): copied out to `get`
+   and / or in from `set` (each nullable); *count = its length. */
+atc_status atc_mlp_params(atc_mlp* net, float* get, const float* set, int64_t* count);
+/* Input standardisation (mean, std per input): read and / or set (each nullable). */
+atc_status atc_mlp_scaling(atc_mlp* net, float* get_mean, float* get_std, const float* set_mean, const float* set_std);
+/* y[rows][n_out] = net(x[rows][n_in]) (x raw; standardised inside). */
+atc_status atc_mlp_forward(atc_mlp* net, const float* x, int32_t rows, float* y, atc_stream s);
+/* Masked MSE loss  sum M (y - t)^2 / (2 sum M)  and its gradient w.r.t. every parameter
+   (mask nullable = all ones). */
+atc_status atc_mlp_gradients(atc_mlp* net, const float* x, const float* t, const float* mask, int32_t rows,
+                             float* grads, float* loss, atc_stream s);
+/* Adam training (fits the standardisation to x first); final mini-batch loss out. */
+atc_status atc_mlp_train(atc_mlp* net, const float* x, const float* t, const float* mask, int32_t rows, int32_t epochs,
+                         int32_t batch, float lr, uint64_t seed, float* final_loss, atc_stream s);
+/* Six graph statistics of device pairs, log1p-scaled: vertices, edges, mean, variance
+   and maximum degree, and the costFuncCal tail cost (tools/costFuncCal.cpp:66-81) of
+   the degree orientation (vertices whose out-degree exceeds twice the mean). */
+atc_status atc_graph_features(const int32_t* pairs_dev, uint64_t n_pairs, float* features, atc_stream s);
+/* The triple the network predicts fastest: *choice = argmin of its outputs;
+   predicted (nullable, n_out floats) = the outputs. */
+atc_status atc_select(atc_mlp* net, const float* features, int32_t* choice, float* predicted, atc_stream s);
+
 /* ---- orientation-cost figures ----------------------------------------------------- */
 /* costFuncCal <file> <k> (tools/costFuncCal.cpp:15-88): out = {idPartCost,
    degreePartCost, lpPartCost}, float sums in vertex order as the tool prints them. */

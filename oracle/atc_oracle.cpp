@@ -678,4 +678,75 @@ uint64_t orc_wedges(const int64_t* off, const int32_t* cols, int64_t n) {
   return w;
 }
 
+// Masked-MSE loss and gradients of the selector MLP in double precision: the checker for
+// the library's FP32 training kernels.  Same parameter layout (W1[I][H] b1 W2[H][H] b2
+// W3[H][O] b3), ReLU hidden layers, inputs standardised with (mean, std) first.
+void orc_mlp_grad(const float* params, int I, int H, int O, const float* mean, const float* stdv, const float* x,
+                  const float* t, const float* mask, int B, double* grads, double* loss) {
+  const float* W1 = params;
+  const float* b1 = W1 + (int64_t)I * H;
+  const float* W2 = b1 + H;
+  const float* b2 = W2 + (int64_t)H * H;
+  const float* W3 = b2 + H;
+  const float* b3 = W3 + (int64_t)H * O;
+  int64_t np = (int64_t)I * H + H + (int64_t)H * H + H + (int64_t)H * O + O;
+  std::fill(grads, grads + np, 0.0);
+  double* gW1 = grads;
+  double* gb1 = gW1 + (int64_t)I * H;
+  double* gW2 = gb1 + H;
+  double* gb2 = gW2 + (int64_t)H * H;
+  double* gW3 = gb2 + H;
+  double* gb3 = gW3 + (int64_t)H * O;
+  double msum = 0;
+  for (int64_t k = 0; k < (int64_t)B * O; ++k) msum += mask ? mask[k] : 1.0;
+  if (msum <= 0) msum = 1;
+  double L = 0;
+  std::vector<double> xs(I), a1(H), a2(H), y(O), dy(O), d2(H), d1(H);
+  for (int b = 0; b < B; ++b) {
+    for (int i = 0; i < I; ++i) xs[i] = ((double)x[(int64_t)b * I + i] - mean[i]) / (stdv[i] > 0 ? stdv[i] : 1.0);
+    for (int j = 0; j < H; ++j) {
+      double z = b1[j];
+      for (int i = 0; i < I; ++i) z += xs[i] * W1[(int64_t)i * H + j];
+      a1[j] = z > 0 ? z : 0;
+    }
+    for (int j = 0; j < H; ++j) {
+      double z = b2[j];
+      for (int i = 0; i < H; ++i) z += a1[i] * W2[(int64_t)i * H + j];
+      a2[j] = z > 0 ? z : 0;
+    }
+    for (int o = 0; o < O; ++o) {
+      double z = b3[o];
+      for (int i = 0; i < H; ++i) z += a2[i] * W3[(int64_t)i * O + o];
+      y[o] = z;
+      double mk = mask ? mask[(int64_t)b * O + o] : 1.0;
+      double d = z - t[(int64_t)b * O + o];
+      L += mk * d * d;
+      dy[o] = mk * d / msum;
+    }
+    for (int o = 0; o < O; ++o) {
+      gb3[o] += dy[o];
+      for (int i = 0; i < H; ++i) gW3[(int64_t)i * O + o] += a2[i] * dy[o];
+    }
+    for (int i = 0; i < H; ++i) {
+      double acc = 0;
+      for (int o = 0; o < O; ++o) acc += dy[o] * W3[(int64_t)i * O + o];
+      d2[i] = a2[i] > 0 ? acc : 0;
+    }
+    for (int j = 0; j < H; ++j) {
+      gb2[j] += d2[j];
+      for (int i = 0; i < H; ++i) gW2[(int64_t)i * H + j] += a1[i] * d2[j];
+    }
+    for (int i = 0; i < H; ++i) {
+      double acc = 0;
+      for (int j = 0; j < H; ++j) acc += d2[j] * W2[(int64_t)i * H + j];
+      d1[i] = a1[i] > 0 ? acc : 0;
+    }
+    for (int j = 0; j < H; ++j) {
+      gb1[j] += d1[j];
+      for (int i = 0; i < I; ++i) gW1[(int64_t)i * H + j] += xs[i] * d1[j];
+    }
+  }
+  *loss = 0.5 * L / msum;
+}
+
 }  // extern "C"

@@ -44,6 +44,8 @@ def lib():
         L.orc_kclique.argtypes = [_P, C.c_uint64, C.c_int, C.c_int]
         L.orc_kclique_sample.restype = C.c_uint64
         L.orc_kclique_sample.argtypes = [_P, C.c_uint64, C.c_int, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_int64)]
+        L.orc_mlp_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P,
+                                   C.POINTER(C.c_double)]
         L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
         L.orc_hu_csr.restype = C.c_int64
@@ -145,6 +147,18 @@ def kclique_sample(pairs, k, stride, phase=0, nthreads=None):
     e = C.c_int64(0)
     c = lib().orc_kclique_sample(_ptr(p), p.shape[0], k, stride, phase, nthreads or nthreads_default(), C.byref(e))
     return c, e.value
+
+
+def mlp_grad(params, I, H, O, mean, std, x, t, mask=None):
+    """(loss, gradient vector) of the selector MLP in double precision."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    params, mean, std, x, t = f(params), f(mean), f(std), f(x), f(t)
+    mask = None if mask is None else f(mask)
+    g = np.zeros(params.size, dtype=np.float64)
+    loss = C.c_double(0)
+    lib().orc_mlp_grad(_ptr(params), I, H, O, _ptr(mean), _ptr(std), _ptr(x), _ptr(t), _ptr(mask), x.shape[0],
+                       _ptr(g), C.byref(loss))
+    return loss.value, g
 
 
 def costfunc(pairs, k):

@@ -111,3 +111,25 @@ def test_hu_csr_matches_reference_rules():
     # orientation preserves the triangle count
     oriented = np.stack([np.repeat(np.arange(off.size - 1), np.diff(off)), cols], 1)
     assert oracle.tc_count(oriented) == oracle.tc_count(g)
+
+
+def test_oracle_mlp_gradient_by_finite_differences():
+    # pins the oracle's backward pass (the checker of the GPU training kernels)
+    rng = np.random.default_rng(0)
+    I, H, O, B = 3, 5, 4, 7
+    npar = I * H + H + H * H + H + H * O + O
+    p = rng.normal(size=npar).astype(np.float32) * 0.5
+    x = rng.normal(size=(B, I)).astype(np.float32)
+    t = rng.normal(size=(B, O)).astype(np.float32)
+    mean = np.zeros(I, np.float32)
+    std = np.ones(I, np.float32)
+    _, g = oracle.mlp_grad(p, I, H, O, mean, std, x, t)
+    h = 1e-3
+    for k in range(0, npar, 7):
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        lp, _ = oracle.mlp_grad(pp, I, H, O, mean, std, x, t)
+        lm, _ = oracle.mlp_grad(pm, I, H, O, mean, std, x, t)
+        num = (lp - lm) / (2 * h)
+        assert abs(num - g[k]) < 2e-3 * max(1.0, abs(g[k])), (k, num, g[k])
