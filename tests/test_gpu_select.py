@@ -76,7 +76,7 @@ def test_graph_features_known_values():
     pairs = np.array([[0, 1], [0, 2], [0, 3], [0, 4], [1, 2], [2, 3], [3, 1], [2, 2]], dtype=np.int32)
     d = torch.from_numpy(pairs).cuda()
     f = atc.graph_features(d.data_ptr(), pairs.shape[0])
-    deg = np.array([4, 3, 4, 3, 1], dtype=np.float64)
+    deg = np.array([4, 3, 3, 3, 1], dtype=np.float64)
     n, m = 5, 7
     assert np.allclose(f[:5], np.log1p([n, m, deg.mean(), deg.var(), deg.max()]), rtol=1e-6)
     # degree orientation (lower degree first, ties to the larger id): out-degrees
