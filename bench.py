@@ -155,6 +155,25 @@ def traffic_for(cfg, kernel_name):
     return rec.get("dram_bytes_per_launch") if rec else None
 
 
+def replica_throughput(units, ms, count, dist=None, device="cpu"):
+    """Whole-job throughput of independent replicas (one per rank, no data-path collective):
+    units are summed over ranks, the time is the slowest rank's.  Returns (total units,
+    max ms, units per second, whether every rank produced the same count)."""
+    if dist is None:
+        return units, ms, units / (ms * 1e-3), True
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    u = torch.tensor([int(units)], dtype=torch.int64, device=device)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    lo = torch.tensor([int(count)], dtype=torch.int64, device=device)
+    hi = lo.clone()
+    dist.all_reduce(lo, op=dist.ReduceOp.MIN)
+    dist.all_reduce(hi, op=dist.ReduceOp.MAX)
+    total, worst = int(u.item()), float(t.item())
+    return total, worst, total / (worst * 1e-3), int(lo.item()) == int(hi.item())
+
+
 # ---------------------------------------------------------------------------------------
 def cpu_baseline(g_lower_off, g_lower_cols, m_total, target_s):
     """Times the oracle's scalar-merge triangle count on a strided vertex sample."""
@@ -291,12 +310,9 @@ def run_ours(a):
         ev1.record(stream)
         torch.cuda.synchronize()
     total_ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    _, total_ms, value, same = replica_throughput(m * a.steps, total_ms, c, dist, "cuda")
+    assert same, "replicas counted different triangle totals"
     ms_step = total_ms / a.steps
-    value = m * a.steps * world / (total_ms * 1e-3)
     head_count = c
     assert all(v == head_count for v in counts.values()), (head_count, counts)
     alg = st.alg_bytes
