@@ -39,6 +39,7 @@ class Dir(enum.IntEnum):
     DEGREE = 1
     DEGREE_LOWID = 2
     ADIRECTION = 3
+    KCORE = 4
 
 
 class Order(enum.IntEnum):

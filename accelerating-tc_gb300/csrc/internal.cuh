@@ -43,6 +43,9 @@ atc_status simple_degrees(const SimpleEdges& e, int32_t* deg, cudaStream_t s);
 atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* prio, int* waves_out,
                            cudaStream_t s);
 
+// Core numbers (n_in ints, device) of the simple graph given by canonical keys.
+atc_status core_numbers(const SimpleEdges& e, const int32_t* deg, int32_t* core, cudaStream_t s);
+
 // A-order lookup (vertex_ordering/A-order/A-order.cpp:62-210) of an edge list with
 // repeats counted.  Edges come either as int2 pairs or as canonical keys (exactly one
 // non-null).  n_v = max id + 1 over the edges.  lookup: n_v ints (device).  If

@@ -11,6 +11,7 @@
 // therefore one parallel pass: atomicSub(rt[y], 2) on each unpeeled neighbour; the one
 // subtraction that takes rt from above the threshold to at or below it admits y.  The
 // float threshold arithmetic runs on the host exactly as in the reference (:37, :77, :127).
+#include <climits>
 #include <vector>
 
 #include "internal.cuh"
@@ -146,6 +147,115 @@ atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* pr
     threshold = grown;
   }
   *waves_out = waves;
+  return ATC_OK;
+}
+
+// ---- k-core numbers (for the k-core direction, edge_directing/kcore_direction.cpp:91-146) ----
+// Level-synchronous peeling: at level k every vertex whose remaining degree is <= k
+// leaves with core number k, each leaving vertex lowers its remaining neighbours by 1,
+// and the level repeats until nothing more leaves; k then jumps to the smallest
+// remaining degree.  Which vertices leave at a level does not depend on the order, so
+// the core numbers equal the sequential Batagelj-Zaversnik result.  (The reference tool
+// counts degrees over the first node_num edges only, :35-38; this uses the true degrees.)
+namespace {
+
+__global__ void core_scan_kernel(const int32_t* rt, int32_t* core, int64_t n, int32_t k, int32_t* frontier, int* count) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride)
+    if (core[v] == -1 && rt[v] <= k) {
+      core[v] = k;
+      frontier[atomicAdd(count, 1)] = (int32_t)v;
+    }
+}
+
+__global__ void core_wave_kernel(const int32_t* frontier, int nf, const int64_t* off, const int32_t* adj, int32_t* rt,
+                                 int32_t* core, int32_t k, int32_t* next, int* count) {
+  int lane = threadIdx.x & 31;
+  int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; f < nf; f += warps) {
+    int32_t x = frontier[f];
+    for (int64_t j = off[x] + lane; j < off[x + 1]; j += 32) {
+      int32_t y = adj[j];
+      if (*(volatile int32_t*)&core[y] != -1) continue;
+      int32_t old = atomicSub(&rt[y], 1);
+      if (old == k + 1) {  // the one decrement that takes rt from k+1 to k
+        core[y] = k;
+        next[atomicAdd(count, 1)] = y;
+      }
+    }
+  }
+}
+
+__global__ void core_min_kernel(const int32_t* rt, const int32_t* core, int64_t n, int* mn) {
+  int best = INT_MAX;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride)
+    if (core[v] == -1) best = min(best, rt[v]);
+  for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMin(mn, best);
+}
+
+}  // namespace
+
+atc_status core_numbers(const SimpleEdges& e, const int32_t* deg, int32_t* core, cudaStream_t s) {
+  const int64_t n = e.n_in, m = e.m;
+  if (n == 0) return ATC_OK;
+  DevBuf<int64_t> off;
+  DevBuf<unsigned long long> cur;
+  DevBuf<int32_t> adj, rt, fa, fb;
+  DevBuf<int> cnt;
+  ATC_TRY(off.alloc(n + 1, s));
+  ATC_TRY(exclusive_scan_i32_to_i64(deg, off.p, n, s));
+  int64_t total = 2 * m;
+  ATC_CK(cudaMemcpyAsync(off.p + n, &total, sizeof(total), cudaMemcpyHostToDevice, s));
+  ATC_TRY(cur.alloc(n, s));
+  ATC_CK(cudaMemcpyAsync(cur.p, off.p, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s));
+  ATC_TRY(adj.alloc(total, s));
+  if (m) sym_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(e.keys.p, m, e.bits, cur.p, adj.p);
+  ATC_CK(cudaGetLastError());
+  cur.release();
+  ATC_TRY(rt.alloc(n, s));
+  ATC_TRY(fa.alloc(n, s));
+  ATC_TRY(fb.alloc(n, s));
+  ATC_TRY(cnt.alloc(1, s));
+  ATC_CK(cudaMemcpyAsync(rt.p, deg, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+  ATC_CK(cudaMemsetAsync(core, 0xff, sizeof(int32_t) * n, s));
+  int32_t k = 0;
+  int64_t removed = 0;
+  int hcnt = 0;
+  int32_t* F = fa.p;
+  int32_t* N = fb.p;
+  for (;;) {
+    ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int), s));
+    core_scan_kernel<<<grid_for(n, 256), 256, 0, s>>>(rt.p, core, n, k, F, cnt.p);
+    ATC_CK(cudaGetLastError());
+    ATC_CK(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    int nf = hcnt;
+    removed += nf;
+    while (nf > 0) {
+      ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int), s));
+      core_wave_kernel<<<grid_for((int64_t)nf * 32, 256), 256, 0, s>>>(F, nf, off.p, adj.p, rt.p, core, k, N, cnt.p);
+      ATC_CK(cudaGetLastError());
+      ATC_CK(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      ATC_CK(cudaStreamSynchronize(s));
+      std::swap(F, N);
+      nf = hcnt;
+      removed += nf;
+    }
+    if (removed >= n) break;
+    int init = INT_MAX;
+    ATC_CK(cudaMemcpyAsync(cnt.p, &init, sizeof(int), cudaMemcpyHostToDevice, s));
+    core_min_kernel<<<grid_for(n, 256), 256, 0, s>>>(rt.p, core, n, cnt.p);
+    ATC_CK(cudaGetLastError());
+    ATC_CK(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    if (hcnt <= k) {  // cannot happen: every remaining degree is above k
+      set_error("k-core peel made no progress at level %d", k);
+      return ATC_ERR_CUDA;
+    }
+    k = hcnt;
+  }
   return ATC_OK;
 }
 

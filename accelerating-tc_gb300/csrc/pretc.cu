@@ -74,6 +74,7 @@ struct OrientArgs {
 //   DEGREE        lower degree; tie -> larger id        Hu/preTC.cu:125-133, A-order.cpp:91-96
 //   DEGREE_LOWID  lower degree; tie -> smaller id       tricount_gpu.cu:76-78
 //   ADIRECTION    lower priority; tie -> smaller id     A-direction-seri.cpp:259-261
+//   KCORE         lower core number; tie -> smaller id  kcore_direction.cpp:137-143
 __global__ void orient_kernel(const uint64_t* ek, int64_t m, OrientArgs a, uint64_t* out,
                               unsigned long long* dropped) {
   uint64_t mask = (1ull << a.bin) - 1;
@@ -94,6 +95,11 @@ __global__ void orient_kernel(const uint64_t* ek, int64_t m, OrientArgs a, uint6
       case ATC_DIR_ID: x_src = xn > yn; break;
       case ATC_DIR_DEGREE: x_src = dx < dy || (dx == dy && xn > yn); break;
       case ATC_DIR_DEGREE_LOWID: x_src = dx < dy || (dx == dy && xn < yn); break;
+      case ATC_DIR_KCORE: {
+        int32_t cx = a.prio[x], cy = a.prio[y];
+        x_src = cx < cy || (cx == cy && xn < yn);
+        break;
+      }
       default: {
         int32_t px = a.prio[x], py = a.prio[y];
         x_src = py > px || (py == px && xn < yn);
@@ -272,7 +278,7 @@ atc_status simple_degrees(const SimpleEdges& e, int32_t* deg, cudaStream_t s) {
 static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_order order, const atc_tuning* t,
                              atc_csr* out, int32_t* perm_out, cudaStream_t s) {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
-  ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION, "unknown atc_dir");
+  ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_KCORE, "unknown atc_dir");
   ATC_CHECK_ARG(order == ATC_ORDER_NONE || order == ATC_ORDER_AORDER, "unknown atc_order");
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
@@ -306,6 +312,9 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
     ATC_TRY(prio.alloc(n_in, s));
     int waves = 0;
     ATC_TRY(peel_priorities(e, deg.p, prio.p, &waves, s));
+  } else if (dir == ATC_DIR_KCORE) {
+    ATC_TRY(prio.alloc(n_in, s));
+    ATC_TRY(core_numbers(e, deg.p, prio.p, s));
   }
   int64_t n = n_in;
   if (prune) {

@@ -49,7 +49,10 @@ typedef enum atc_dir {
   ATC_DIR_DEGREE_LOWID = 2,
   /* A-direction: peel priorities, u -> v iff prio[v] > prio[u] or (equal and u < v)
      (edge_directing/A-direction-seri.cpp:35-153, 254-273). */
-  ATC_DIR_ADIRECTION = 3
+  ATC_DIR_ADIRECTION = 3,
+  /* k-core: lower core number first; equal cores: the smaller id is the source
+     (edge_directing/kcore_direction.cpp:91-146, with true degrees; see atc_pretc). */
+  ATC_DIR_KCORE = 4
 } atc_dir;
 
 typedef enum atc_order {

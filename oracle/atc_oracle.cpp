@@ -678,6 +678,37 @@ uint64_t orc_wedges(const int64_t* off, const int32_t* cols, int64_t n) {
   return w;
 }
 
+// Core numbers of the simple graph by the Batagelj-Zaversnik bucket algorithm, the
+// intent of edge_directing/kcore_direction.cpp:91-146 (which counts degrees over only
+// the first node_num edges, :35-38).  core (n ints).
+void orc_core_numbers(const int32_t* pairs, uint64_t np, int32_t* core) {
+  Adj g = build_adj(pairs, np);
+  int64_t n = g.n;
+  std::vector<int64_t> deg(n), pos(n), vert(n);
+  int64_t md = 0;
+  for (int64_t v = 0; v < n; ++v) { deg[v] = g.off[v + 1] - g.off[v]; md = std::max(md, deg[v]); }
+  std::vector<int64_t> bin(md + 2, 0);
+  for (int64_t v = 0; v < n; ++v) bin[deg[v]]++;
+  int64_t start = 0;
+  for (int64_t d = 0; d <= md; ++d) { int64_t c = bin[d]; bin[d] = start; start += c; }
+  for (int64_t v = 0; v < n; ++v) { pos[v] = bin[deg[v]]++; vert[pos[v]] = v; }
+  for (int64_t d = md; d >= 1; --d) bin[d] = bin[d - 1];
+  bin[0] = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t v = vert[i];
+    for (int64_t j = g.off[v]; j < g.off[v + 1]; ++j) {
+      int64_t u = g.nbr[j];
+      if (deg[u] > deg[v]) {
+        int64_t du = deg[u], pu = pos[u], pw = bin[du], w = vert[pw];
+        if (u != w) { pos[u] = pw; vert[pu] = w; pos[w] = pu; vert[pw] = u; }
+        bin[du]++;
+        deg[u]--;
+      }
+    }
+  }
+  for (int64_t v = 0; v < n; ++v) core[v] = (int32_t)deg[v];
+}
+
 // Masked-MSE loss and gradients of the selector MLP in double precision: the checker for
 // the library's FP32 training kernels.  Same parameter layout (W1[I][H] b1 W2[H][H] b2
 // W3[H][O] b3), ReLU hidden layers, inputs standardised with (mean, std) first.

@@ -46,6 +46,7 @@ def lib():
         L.orc_kclique_sample.argtypes = [_P, C.c_uint64, C.c_int, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_int64)]
         L.orc_mlp_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P,
                                    C.POINTER(C.c_double)]
+        L.orc_core_numbers.argtypes = [_P, C.c_uint64, _P]
         L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
         L.orc_hu_csr.restype = C.c_int64
@@ -159,6 +160,14 @@ def mlp_grad(params, I, H, O, mean, std, x, t, mask=None):
     lib().orc_mlp_grad(_ptr(params), I, H, O, _ptr(mean), _ptr(std), _ptr(x), _ptr(t), _ptr(mask), x.shape[0],
                        _ptr(g), C.byref(loss))
     return loss.value, g
+
+
+def core_numbers(pairs):
+    p = _pairs(pairs)
+    n = (int(p.max()) + 1) if p.size else 0
+    out = np.empty(max(n, 1), dtype=np.int32)
+    lib().orc_core_numbers(_ptr(p), p.shape[0], _ptr(out))
+    return out[:n]
 
 
 def costfunc(pairs, k):

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = sorted(load_golden()["cases"])
 KERNELS = [atc.Kernel.HU, atc.Kernel.BISSON, atc.Kernel.FOX, atc.Kernel.TRICORE]
-DIRS = [atc.Dir.ID, atc.Dir.DEGREE, atc.Dir.DEGREE_LOWID, atc.Dir.ADIRECTION]
+DIRS = [atc.Dir.ID, atc.Dir.DEGREE, atc.Dir.DEGREE_LOWID, atc.Dir.ADIRECTION, atc.Dir.KCORE]
 
 
 def sha(a):
@@ -369,3 +369,13 @@ def test_chunglu_generator_shape():
     assert 12.0 < mean_deg < 24.0, mean_deg
     g2 = atc.gen_chunglu_device(100000, 2.5, 20.0, 7).cpu().numpy()
     assert np.array_equal(g, g2)
+
+
+def test_kcore_orientation_matches_oracle_core_numbers():
+    g = atc.rmat_graph(12, 16, 4)
+    core = oracle.core_numbers(g)
+    off, cols = atc.pretc(g, atc.Dir.KCORE).to_host()
+    src = np.repeat(np.arange(off.size - 1), np.diff(off))
+    cs, cd = core[src], core[cols]
+    assert np.all((cs < cd) | ((cs == cd) & (src < cols)))
+    assert off[-1] == oracle.simple_stats(g)[1]

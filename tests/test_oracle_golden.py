@@ -133,3 +133,16 @@ def test_oracle_mlp_gradient_by_finite_differences():
         lm, _ = oracle.mlp_grad(pm, I, H, O, mean, std, x, t)
         num = (lp - lm) / (2 * h)
         assert abs(num - g[k]) < 2e-3 * max(1.0, abs(g[k])), (k, num, g[k])
+
+
+def test_oracle_core_numbers_match_networkx():
+    nx = pytest.importorskip("networkx")
+    import atc
+    for scale, seed in ((9, 1), (11, 2)):
+        g = atc.rmat_graph(scale, 8, seed, symmetric=False)
+        G = nx.Graph()
+        G.add_nodes_from(range(int(g.max()) + 1))
+        G.add_edges_from(map(tuple, g))
+        want = nx.core_number(G)
+        got = oracle.core_numbers(g)
+        assert all(got[v] == want[v] for v in G.nodes)
