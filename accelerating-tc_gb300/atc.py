@@ -131,6 +131,9 @@ _SIGS = {
     "atc_pretc_device": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
     "atc_csr_to_host": (C.c_int, [C.POINTER(CSRStruct), _P, _P, _P]),
     "atc_csr_free": (C.c_int, [C.POINTER(CSRStruct)]),
+    "atc_read_edges": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "atc_csr_save": (C.c_int, [C.POINTER(CSRStruct), C.c_char_p, _P]),
+    "atc_csr_load": (C.c_int, [C.c_char_p, C.POINTER(CSRStruct), _P]),
     "atc_adirection": (C.c_int, [_P, C.c_uint64, _P, C.POINTER(C.c_uint64), _P, _P]),
     "atc_aorder": (C.c_int, [_P, C.c_uint64, _P, _P, _P, _P]),
     "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
@@ -231,6 +234,16 @@ def simplify(pairs, symmetric=True):
     return out[: n.value].copy()
 
 
+def read_edges(path):
+    """Edge pairs from a Galois .gr file (by suffix) or an int32 pair file (host only)."""
+    n = C.c_uint64(0)
+    p = os.fsencode(path)
+    _check(lib().atc_read_edges(p, None, 0, C.byref(n)))
+    out = np.empty((max(n.value, 1), 2), dtype=np.int32)
+    _check(lib().atc_read_edges(p, _ptr(out), n.value, C.byref(n)))
+    return out[: n.value]
+
+
 def rmat_graph(scale, edge_factor=16, seed=1, symmetric=True):
     """The benchmarks' input: seeded R-MAT, symmetrised, loops and repeats removed."""
     return simplify(gen_rmat(scale, edge_factor, seed), symmetric=symmetric)
@@ -272,6 +285,15 @@ class CSR:
         cols = np.empty(self.m, dtype=np.int32)
         _check(lib().atc_csr_to_host(C.byref(self._st), _ptr(off), _ptr(cols), stream))
         return off, cols
+
+    def save(self, path, stream=None):
+        _check(lib().atc_csr_save(C.byref(self._st), os.fsencode(path), stream))
+
+    @staticmethod
+    def load(path, stream=None):
+        st = CSRStruct()
+        _check(lib().atc_csr_load(os.fsencode(path), C.byref(st), stream))
+        return CSR(st)
 
     def free(self):
         if self._st is not None and self._st.offsets is not None:

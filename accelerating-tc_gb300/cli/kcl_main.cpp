@@ -1,11 +1,11 @@
 // Drop-in for the k-clique program (k-clique/kcl_gpu.cpp:13-32, kcl.cu:147-215):
-//   kcl <edges.bin> -k=K
-// The reference reads a Galois .gr file through Galois/Pangolin (not part of the
-// reference tree); this program reads the int32 pair files of the other tools, orients
-// by A-direction and prints the reference's result line "total_num_cliques = N".
+//   kcl [-symmetricGraph] [-simpleGraph] <graph.gr | edges.bin> -k=K
+// Reads a Galois .gr file (the reference's input) or an int32 pair file, orients by
+// A-direction and prints the reference's result line "total_num_cliques = N".
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "atc.h"
@@ -17,20 +17,25 @@ int main(int argc, char** argv) {
     if (strncmp(argv[i], "-k=", 3) == 0) k = (unsigned)atoi(argv[i] + 3);
     else if (argv[i][0] != '-') path = argv[i];
   }
-  if (!path) { fprintf(stderr, "usage: %s <edges.bin> -k=K\n", argv[0]); return 2; }
-  FILE* f = fopen(path, "rb");
-  if (!f) { fprintf(stderr, "cannot read %s\n", path); return 1; }
-  fseek(f, 0, SEEK_END);
-  long sz = ftell(f);
-  fseek(f, 0, SEEK_SET);
-  size_t n = sz > 0 ? (size_t)sz / 8 : 0;
-  std::vector<int32_t> pairs(2 * n);
-  size_t got = n ? fread(pairs.data(), 8, n, f) : 0;
-  fclose(f);
-  if (got != n) return 1;
-  atc_status s = atc_init(0);
+  if (!path) {
+    fprintf(stderr, "usage: %s <graph.gr | edges.bin> -k=K\n", argv[0]);
+    return 2;
+  }
+  uint64_t np = 0;
+  std::vector<int32_t> pairs;
+  atc_status s = atc_read_edges(path, nullptr, 0, &np);
+  if (s == ATC_OK) {
+    pairs.resize(2 * np);
+    s = atc_read_edges(path, pairs.data(), np, &np);
+  }
+  if (s != ATC_OK) {
+    fprintf(stderr, "%s\n", atc_last_error());
+    return 1;
+  }
+  s = atc_init(0);
   atc_csr csr;
-  if (s == ATC_OK) s = atc_pretc(pairs.data(), n, ATC_DIR_ADIRECTION, ATC_ORDER_NONE, nullptr, &csr, nullptr, nullptr);
+  if (s == ATC_OK)
+    s = atc_pretc(pairs.data(), pairs.size() / 2, ATC_DIR_ADIRECTION, ATC_ORDER_NONE, nullptr, &csr, nullptr, nullptr);
   uint64_t total = 0;
   atc_stats st;
   if (s == ATC_OK) {

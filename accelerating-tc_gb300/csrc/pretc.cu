@@ -8,6 +8,8 @@
 // 64-bit (src << B | dst) keys are radix-sorted once and the CSR offsets are read off
 // the sorted keys.
 #include <climits>
+#include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "internal.cuh"
@@ -490,5 +492,109 @@ extern "C" atc_status atc_adirection(const int32_t* pairs, uint64_t np, int32_t*
   if (prio_out) ATC_CK(cudaMemcpyAsync(prio_out, prio.p, sizeof(int32_t) * e.n_in, cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   *n_out = (uint64_t)e.m;
+  return ATC_OK;
+}
+
+// ---- binary CSR cache -----------------------------------------------------------------
+// File: "ATCCSR01", then int64 n, m, n_input, wedges, wedges_min, int32 dir, order,
+// pruned, max_outdeg, then offsets (n+1 int64) and cols (m int32), little-endian.
+namespace atc {
+__global__ void csr_fill_esrc_kernel(const int64_t* off, int64_t n, int32_t* esrc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < n; u += warps)
+    for (int64_t j = off[u] + lane; j < off[u + 1]; j += 32) esrc[j] = (int32_t)u;
+}
+static const char kCsrMagic[8] = {'A', 'T', 'C', 'C', 'S', 'R', '0', '1'};
+}  // namespace atc
+
+extern "C" atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && path != nullptr, "NULL argument");
+  std::vector<int64_t> off(csr->n + 1);
+  std::vector<int32_t> cols(csr->m);
+  ATC_TRY(atc_csr_to_host(csr, off.data(), cols.data(), st));
+  FILE* f = fopen(path, "wb");
+  if (!f) {
+    set_error("cannot open %s for writing", path);
+    return ATC_ERR_INVALID;
+  }
+  int64_t h64[5] = {csr->n, csr->m, csr->n_input, csr->wedges, csr->wedges_min};
+  int32_t h32[4] = {csr->dir, csr->order, csr->pruned, csr->max_outdeg};
+  bool ok = fwrite(atc::kCsrMagic, 1, 8, f) == 8 && fwrite(h64, 8, 5, f) == 5 && fwrite(h32, 4, 4, f) == 4 &&
+            fwrite(off.data(), 8, off.size(), f) == off.size() &&
+            (cols.empty() || fwrite(cols.data(), 4, cols.size(), f) == cols.size());
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) {
+    set_error("short write to %s", path);
+    return ATC_ERR_INVALID;
+  }
+  return ATC_OK;
+}
+
+extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st) {
+  ATC_CHECK_ARG(path != nullptr && out != nullptr, "NULL argument");
+  cudaStream_t s = as_stream(st);
+  *out = atc_csr{};
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    set_error("cannot open %s", path);
+    return ATC_ERR_INVALID;
+  }
+  char magic[8];
+  int64_t h64[5];
+  int32_t h32[4];
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, atc::kCsrMagic, 8) == 0 && fread(h64, 8, 5, f) == 5 &&
+            fread(h32, 4, 4, f) == 4 && h64[0] >= 0 && h64[1] >= 0 && h64[0] < (int64_t)INT32_MAX;
+  std::vector<int64_t> off;
+  std::vector<int32_t> cols;
+  if (ok) {
+    off.resize(h64[0] + 1);
+    cols.resize(h64[1]);
+    ok = fread(off.data(), 8, off.size(), f) == off.size() &&
+         (cols.empty() || fread(cols.data(), 4, cols.size(), f) == cols.size());
+  }
+  fclose(f);
+  // the arrays must form a CSR: offsets from 0 to m, non-decreasing, rows strictly
+  // increasing ids in [0, n)
+  const int64_t n = ok ? h64[0] : 0, m = ok ? h64[1] : 0;
+  if (ok) ok = off[0] == 0 && off[n] == m;
+  for (int64_t u = 0; ok && u < n; ++u) {
+    if (off[u + 1] < off[u]) ok = false;
+    for (int64_t j = off[u]; ok && j < off[u + 1]; ++j)
+      if (cols[j] < 0 || cols[j] >= n || (j > off[u] && cols[j] <= cols[j - 1])) ok = false;
+  }
+  if (!ok) {
+    set_error("%s is not an ATCCSR01 file holding a valid CSR", path);
+    return ATC_ERR_INVALID;
+  }
+  DevBuf<int64_t> doff;
+  DevBuf<int32_t> dcols, desrc;
+  DevBuf<unsigned long long> counter;
+  ATC_TRY(doff.alloc(n + 1, s));
+  ATC_TRY(dcols.alloc(m + 16, s));
+  ATC_TRY(desrc.alloc(m + 16, s));
+  ATC_TRY(counter.alloc(4, s));
+  ATC_CK(cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s));
+  ATC_CK(cudaMemsetAsync(dcols.p + m, 0, sizeof(int32_t) * 16, s));
+  if (m) ATC_CK(cudaMemcpyAsync(dcols.p, cols.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
+  if (n) atc::csr_fill_esrc_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(doff.p, n, desrc.p);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaStreamSynchronize(s));
+  CsrPriv* pv = new CsrPriv();
+  pv->esrc = desrc.detach();
+  pv->counter = counter.detach();
+  pv->bits = id_bits(n);
+  out->n = n;
+  out->m = m;
+  out->offsets = doff.detach();
+  out->cols = dcols.detach();
+  out->n_input = h64[2];
+  out->wedges = h64[3];
+  out->wedges_min = h64[4];
+  out->dir = h32[0];
+  out->order = h32[1];
+  out->pruned = h32[2];
+  out->max_outdeg = h32[3];
+  out->priv = pv;
   return ATC_OK;
 }

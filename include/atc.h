@@ -165,6 +165,19 @@ atc_status atc_pretc_device(const int32_t* pairs_dev, uint64_t n_pairs, atc_dir 
 /* Copies the CSR to host arrays (n+1 int64, m int32). */
 atc_status atc_csr_to_host(const atc_csr* csr, int64_t* offsets, int32_t* cols, atc_stream s);
 atc_status atc_csr_free(atc_csr* csr);
+/* Edge-file reader (host only, no GPU): "*.gr" is read as a Galois binary graph
+   (versions 1 and 2; the k-clique program's input, k-clique/README.md:12-15), any
+   other name as {int32 src, int32 dst} pairs (Hu/preTC.cu:29-32,84).  Two-call
+   pattern: with pairs == NULL only *n_out (edge count) is written; then pass a
+   buffer of cap >= *n_out pairs.  ATC_ERR_INVALID for an unreadable or malformed file. */
+atc_status atc_read_edges(const char* path, int32_t* pairs, uint64_t cap, uint64_t* n_out);
+
+/* Binary CSR cache (no counterpart in the reference, whose programs hand over
+   intermediate edge files): writes / reads the oriented CSR with its statistics
+   ("ATCCSR01", little-endian), so a graph's preTC can be done once and reloaded.
+   atc_csr_load validates the arrays (ATC_ERR_INVALID for a file that is not a CSR). */
+atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_stream s);
+atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream s);
 
 /* ---- orientation and ordering as drop-ins for the reference programs ------------ */
 /* A-direction-seri <file> (edge_directing/A-direction-seri.cpp:170-288): writes the

@@ -45,3 +45,16 @@ def gpu_ready():
     import atc
     atc.init(0)
     return True
+
+
+def write_gr(path, n, adj, version):
+    """A Galois .gr file: header, u64 end offsets, targets (u32 padded to 8 or u64)."""
+    ends = np.cumsum([len(a) for a in adj]).astype(np.uint64)
+    dst = np.array([v for a in adj for v in a], dtype=np.uint32 if version == 1 else np.uint64)
+    with open(path, "wb") as f:
+        f.write(np.array([version, 0, n, len(dst)], dtype=np.uint64).tobytes())
+        f.write(ends.tobytes())
+        f.write(dst.tobytes())
+        if version == 1 and len(dst) % 2:
+            f.write(b"\0" * 4)
+

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import atc
+from conftest import write_gr
 
 
 def test_exports_every_declared_symbol():
@@ -73,3 +74,36 @@ def test_rgg_host_deterministic_and_geometric():
     assert np.all(a[:, 0] < a[:, 1])
     mean_deg = 2 * a.shape[0] / 4096
     assert 13.0 < mean_deg < 17.0
+
+
+@pytest.mark.parametrize("version", [1, 2])
+def test_read_edges_galois_gr(tmp_path, version):
+    rng = np.random.default_rng(version)
+    n = 50
+    pairs = atc.simplify(rng.integers(0, n, size=(300, 2)).astype(np.int32))
+    adj = [sorted(int(v) for v in pairs[pairs[:, 0] == u][:, 1]) for u in range(n)]
+    path = tmp_path / "g.gr"
+    write_gr(path, n, adj, version)
+    got = atc.read_edges(path)
+    assert np.array_equal(got, pairs)
+
+
+def test_read_edges_pair_file_and_errors(tmp_path):
+    pairs = np.array([[0, 1], [2, 3], [5, 4]], dtype=np.int32)
+    p = tmp_path / "e.bin"
+    p.write_bytes(pairs.tobytes() + b"\1\2\3")          # trailing partial pair ignored
+    assert np.array_equal(atc.read_edges(p), pairs)
+    empty = tmp_path / "empty.bin"
+    empty.write_bytes(b"")
+    assert atc.read_edges(empty).shape == (0, 2)
+    bad = tmp_path / "bad.gr"
+    write_gr(bad, 3, [[1], [5], []], 1)                  # target beyond n
+    with pytest.raises(atc.ATCError):
+        atc.read_edges(bad)
+    trunc = tmp_path / "trunc.gr"
+    write_gr(trunc, 3, [[1, 2], [0], [0]], 2)
+    trunc.write_bytes(trunc.read_bytes()[:-8])
+    with pytest.raises(atc.ATCError):
+        atc.read_edges(trunc)
+    with pytest.raises(atc.ATCError):
+        atc.read_edges(tmp_path / "missing.bin")

@@ -13,7 +13,7 @@ import pytest
 
 import atc
 import oracle
-from conftest import golden_input, load_golden
+from conftest import golden_input, load_golden, write_gr
 
 pytestmark = pytest.mark.gpu
 
@@ -295,6 +295,39 @@ def test_cli_dropins(tmp_path):
     r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout
+    n = int(g.max()) + 1
+    adj = [[] for _ in range(n)]
+    for u, v in g:
+        adj[u].append(int(v))
+    for version in (1, 2):
+        gr = tmp_path / ("G%d.gr" % version)
+        write_gr(gr, n, adj, version)
+        r = subprocess.run([os.path.join(bindir, "kcl"), "-symmetricGraph", "-simpleGraph", str(gr), "-k=5"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        assert "total_num_cliques = %d" % oracle.kclique(g, 5) in r.stdout
+
+
+@pytest.mark.parametrize("d", [atc.Dir.ADIRECTION, atc.Dir.DEGREE])
+def test_csr_save_load_round_trip(tmp_path, d):
+    g = atc.rmat_graph(12, 16, 5)
+    csr = atc.pretc(g, d, tuning={"prune_deg1": 1 if d == atc.Dir.DEGREE else 0})
+    path = tmp_path / "g.csr"
+    csr.save(path)
+    back = atc.CSR.load(path)
+    a, b = csr.to_host(), back.to_host()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for f in ("n", "m", "n_input", "wedges", "wedges_min", "max_outdeg", "dir", "order", "pruned"):
+        assert getattr(back._st, f) == getattr(csr._st, f), f
+    want = oracle.tc_count(g)
+    for k in KERNELS:
+        assert atc.tc(back, k)[0] == want
+    assert atc.kcl(back, 4)[0] == oracle.kclique(g, 4)
+    raw = path.read_bytes()
+    bad = tmp_path / "bad.csr"
+    bad.write_bytes(raw[:-4])
+    with pytest.raises(atc.ATCError):
+        atc.CSR.load(bad)
 
 
 def test_rgg_device_matches_host():
