@@ -131,6 +131,7 @@ _SIGS = {
     "atc_pretc_device": (C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(CSRStruct), _P, _P]),
     "atc_csr_to_host": (C.c_int, [C.POINTER(CSRStruct), _P, _P, _P]),
     "atc_csr_free": (C.c_int, [C.POINTER(CSRStruct)]),
+    "atc_kcore_direction": (C.c_int, [_P, C.c_uint64, _P, _P, C.POINTER(C.c_uint64), _P]),
     "atc_read_edges": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "atc_csr_save": (C.c_int, [C.POINTER(CSRStruct), C.c_char_p, _P]),
     "atc_csr_load": (C.c_int, [C.c_char_p, C.POINTER(CSRStruct), _P]),
@@ -519,6 +520,22 @@ def adirection(pairs, want_prio=False, stream=None):
     _check(lib().atc_adirection(_ptr(p), p.shape[0], _ptr(out), C.byref(n), _ptr(prio), stream))
     res = out[: n.value].copy()
     return (res, prio) if want_prio else res
+
+
+def kcore_direction(edges_u64, want_core=False, stream=None):
+    """The kcore_direction program on packed uint64 edges (src = x >> 32): the oriented
+    packed edges in input order, and optionally the core numbers."""
+    e = np.ascontiguousarray(edges_u64, dtype=np.uint64)
+    out = np.empty(max(e.size, 1), dtype=np.uint64)
+    nv = C.c_uint64(0)
+    core = None
+    if want_core:
+        hi = (e >> np.uint64(32)).max() if e.size else 0
+        lo = (e & np.uint64(0xFFFFFFFF)).max() if e.size else 0
+        core = np.empty(int(max(hi, lo)) + 1 if e.size else 1, dtype=np.int32)
+    _check(lib().atc_kcore_direction(_ptr(e), e.size, _ptr(out), _ptr(core), C.byref(nv), stream))
+    res = out[: e.size].copy()
+    return (res, core[: nv.value]) if want_core else res
 
 
 def aorder(pairs, stream=None):

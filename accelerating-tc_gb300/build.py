@@ -41,6 +41,7 @@ CLI_PROGRAMS = {
     "a_order": "order_main.cpp",
     "kcl": "kcl_main.cpp",
     "cost_func_cal": "order_main.cpp",
+    "kcore_direction": "order_main.cpp",
 }
 
 

@@ -5,6 +5,8 @@
 //   a_order <edges.bin>              vertex_ordering/A-order/A-order.cpp:62-247
 //        writes normal and reordered in the working directory
 //   cost_func_cal <edges.bin> <k>    tools/costFuncCal.cpp:15-95 (prints the three costs)
+//   kcore_direction <in> <out>       edge_directing/kcore_direction.cpp:12-146 (uint64 edges,
+//        src = x >> 32; writes the oriented uint64 edges to <out>)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -72,6 +74,17 @@ int main(int argc, char** argv) {
   std::cout << "idPartCost: " << c[0] << std::endl;
   std::cout << "degreePartCost: " << c[1] << std::endl;
   std::cout << "lpPartCost: " << c[2] << std::endl;
+#elif defined(ATC_PROGRAM_KCORE_DIRECTION)
+  if (argc < 3) { fprintf(stderr, "usage: %s <in> <out>\n", argv[0]); return 2; }
+  // the file's bytes read as little-endian uint64 edges
+  std::vector<uint64_t> packed(np), out(np ? np : 1);
+  if (np) memcpy(packed.data(), pairs.data(), 8 * np);
+  uint64_t nv = 0;
+  s = atc_kcore_direction(packed.data(), np, out.data(), nullptr, &nv, nullptr);
+  if (s != ATC_OK) return fail("atc_kcore_direction", s);
+  std::cout << "the edge num is " << np << std::endl;
+  std::cout << "the node num is " << nv << std::endl;
+  if (!write_pairs(argv[2], reinterpret_cast<const int32_t*>(out.data()), np)) return 1;
 #else
 #error "define one ATC_PROGRAM_*"
 #endif

@@ -495,6 +495,58 @@ extern "C" atc_status atc_adirection(const int32_t* pairs, uint64_t np, int32_t*
   return ATC_OK;
 }
 
+// ---- k-core direction (edge_directing/kcore_direction.cpp:12-146) -------------------
+namespace atc {
+__global__ void unpack_u64_pairs_kernel(const uint64_t* e, int64_t ne, int2* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ne; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_int2((int32_t)(uint32_t)(e[i] >> 32), (int32_t)(uint32_t)e[i]);
+}
+// One output per input edge, in input order: src = the endpoint of smaller core number,
+// the smaller id on a tie (kcore_direction.cpp:133-141).
+__global__ void kcore_orient_kernel(const int2* p, int64_t ne, const int32_t* core, uint64_t* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ne; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t a = p[i].x, b = p[i].y;
+    const int32_t ca = core[a], cb = core[b];
+    if (ca > cb || (ca == cb && a > b)) {
+      const int32_t t = a;
+      a = b;
+      b = t;
+    }
+    out[i] = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+  }
+}
+}  // namespace atc
+
+extern "C" atc_status atc_kcore_direction(const uint64_t* edges, uint64_t ne, uint64_t* oriented_out,
+                                          int32_t* core_out, uint64_t* n_vertices, atc_stream st) {
+  ATC_CHECK_ARG(ne == 0 || (edges != nullptr && oriented_out != nullptr), "NULL array");
+  cudaStream_t s = as_stream(st);
+  keep_pool();
+  if (n_vertices) *n_vertices = 0;
+  if (ne == 0) return ATC_OK;
+  DevBuf<uint64_t> de;
+  DevBuf<int2> d;
+  ATC_TRY(de.alloc(ne, s));
+  ATC_TRY(d.alloc(ne, s));
+  ATC_CK(cudaMemcpyAsync(de.p, edges, sizeof(uint64_t) * ne, cudaMemcpyHostToDevice, s));
+  atc::unpack_u64_pairs_kernel<<<grid_for(ne, 256), 256, 0, s>>>(de.p, ne, d.p);
+  ATC_CK(cudaGetLastError());
+  SimpleEdges e;
+  ATC_TRY(build_simple_edges(d.p, ne, &e, s));
+  DevBuf<int32_t> deg, core;
+  ATC_TRY(deg.alloc(e.n_in, s));
+  ATC_TRY(core.alloc(e.n_in, s));
+  ATC_TRY(simple_degrees(e, deg.p, s));
+  ATC_TRY(core_numbers(e, deg.p, core.p, s));
+  atc::kcore_orient_kernel<<<grid_for(ne, 256), 256, 0, s>>>(d.p, ne, core.p, de.p);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaMemcpyAsync(oriented_out, de.p, sizeof(uint64_t) * ne, cudaMemcpyDeviceToHost, s));
+  if (core_out) ATC_CK(cudaMemcpyAsync(core_out, core.p, sizeof(int32_t) * e.n_in, cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (n_vertices) *n_vertices = (uint64_t)e.n_in;
+  return ATC_OK;
+}
+
 // ---- binary CSR cache -----------------------------------------------------------------
 // File: "ATCCSR01", then int64 n, m, n_input, wedges, wedges_min, int32 dir, order,
 // pruned, max_outdeg, then offsets (n+1 int64) and cols (m int32), little-endian.

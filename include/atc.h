@@ -185,6 +185,16 @@ atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream s);
    if non-NULL, the peel priorities (max id + 1 ints). */
 atc_status atc_adirection(const int32_t* pairs, uint64_t n_pairs, int32_t* oriented_out,
                           uint64_t* n_out, int32_t* prio_out, atc_stream s);
+/* kcore_direction <in> <out> (edge_directing/kcore_direction.cpp:12-146): edges packed
+   as uint64 (src = x >> 32, dst = low 32 bits, the program's byte order); writes one
+   packed edge per input edge, in input order, directed from the smaller core number to
+   the larger, the smaller id first on a tie.  Core numbers are those of the simple graph
+   (repeats and loops dropped); `core_out` (nullable) receives them, *n_vertices (nullable)
+   = max id + 1.  Ids must be < 2^31 (ATC_ERR_INVALID otherwise).  The reference counts
+   degrees over the first node_num edges (:35-38) instead of all edges; this function
+   counts all of them. */
+atc_status atc_kcore_direction(const uint64_t* edges, uint64_t n_edges, uint64_t* oriented_out,
+                               int32_t* core_out, uint64_t* n_vertices, atc_stream s);
 /* A-order <file> (vertex_ordering/A-order/A-order.cpp:62-247) on the raw pairs,
    repeats included: `lookup` (max id + 1 ints) = new id of every id (badLookUpTable);
    `normal` / `reordered` (n_pairs pairs each, nullable) = the two output files.

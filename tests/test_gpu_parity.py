@@ -295,6 +295,10 @@ def test_cli_dropins(tmp_path):
     r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout
+    r = subprocess.run([os.path.join(bindir, "kcore_direction"), str(tmp_path / "E.u64"), str(tmp_path / "K.u64")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(np.fromfile(tmp_path / "K.u64", dtype=np.uint64), atc.kcore_direction(u64))
     n = int(g.max()) + 1
     adj = [[] for _ in range(n)]
     for u, v in g:
@@ -412,3 +416,23 @@ def test_kcore_orientation_matches_oracle_core_numbers():
     cs, cd = core[src], core[cols]
     assert np.all((cs < cd) | ((cs == cd) & (src < cols)))
     assert off[-1] == oracle.simple_stats(g)[1]
+
+
+def test_kcore_direction_program_matches_oracle():
+    """kcore_direction.cpp:133-141 on a simple edge list given once per undirected edge."""
+    rng = np.random.default_rng(11)
+    for g in (atc.simplify(atc.gen_rmat(11, 8, 3), symmetric=False),
+              atc.simplify(rng.integers(0, 300, size=(3000, 2)).astype(np.int32), symmetric=False)):
+        g = g[rng.permutation(g.shape[0])]
+        flip = rng.random(g.shape[0]) < 0.5
+        g[flip] = g[flip][:, ::-1]                        # either endpoint first
+        packed = (g[:, 0].astype(np.uint64) << np.uint64(32)) | g[:, 1].astype(np.uint64)
+        out, core = atc.kcore_direction(packed, want_core=True)
+        want_core = oracle.core_numbers(g)
+        assert np.array_equal(core, want_core)
+        src = (out >> np.uint64(32)).astype(np.int64)
+        dst = (out & np.uint64(0xFFFFFFFF)).astype(np.int64)
+        a, b = g[:, 0].astype(np.int64), g[:, 1].astype(np.int64)
+        swap = (want_core[a] > want_core[b]) | ((want_core[a] == want_core[b]) & (a > b))
+        assert np.array_equal(src, np.where(swap, b, a)) and np.array_equal(dst, np.where(swap, a, b))
+    assert atc.kcore_direction(np.zeros(0, dtype=np.uint64)).size == 0
