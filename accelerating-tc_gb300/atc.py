@@ -40,6 +40,7 @@ class Dir(enum.IntEnum):
     DEGREE_LOWID = 2
     ADIRECTION = 3
     KCORE = 4
+    ADIRECTION_PAR = 5
 
 
 class Order(enum.IntEnum):
@@ -132,6 +133,7 @@ _SIGS = {
     "atc_csr_to_host": (C.c_int, [C.POINTER(CSRStruct), _P, _P, _P]),
     "atc_csr_free": (C.c_int, [C.POINTER(CSRStruct)]),
     "atc_kcore_direction": (C.c_int, [_P, C.c_uint64, _P, _P, C.POINTER(C.c_uint64), _P]),
+    "atc_adirection_par": (C.c_int, [_P, C.c_uint64, C.c_int, _P, _P, _P, C.POINTER(C.c_uint64), _P, _P]),
     "atc_read_edges": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "atc_csr_save": (C.c_int, [C.POINTER(CSRStruct), C.c_char_p, _P]),
     "atc_csr_load": (C.c_int, [C.c_char_p, C.POINTER(CSRStruct), _P]),
@@ -536,6 +538,22 @@ def kcore_direction(edges_u64, want_core=False, stream=None):
     _check(lib().atc_kcore_direction(_ptr(e), e.size, _ptr(out), _ptr(core), C.byref(nv), stream))
     res = out[: e.size].copy()
     return (res, core[: nv.value]) if want_core else res
+
+
+def adirection_par(edges_u64, compat=False, stream=None):
+    """The Peel program on packed uint64 edges: (oriented edges, flags, minor, iterations)."""
+    e = np.ascontiguousarray(edges_u64, dtype=np.uint64)
+    hi = (e >> np.uint64(32)).max() if e.size else 0
+    lo = (e & np.uint64(0xFFFFFFFF)).max() if e.size else 0
+    n = int(max(hi, lo)) + 1 if e.size else 0
+    out = np.empty(max(e.size, 1), dtype=np.uint64)
+    flags = np.empty(max(n, 1), dtype=np.uint32)
+    minor = np.empty(max(n, 1), dtype=np.uint32)
+    nv = C.c_uint64(0)
+    it = C.c_int32(0)
+    _check(lib().atc_adirection_par(_ptr(e), e.size, 1 if compat else 0, _ptr(out), _ptr(flags), _ptr(minor),
+                                    C.byref(nv), C.byref(it), stream))
+    return out[: e.size].copy(), flags[: nv.value].copy(), minor[: nv.value].copy(), it.value
 
 
 def aorder(pairs, stream=None):

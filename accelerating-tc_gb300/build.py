@@ -42,6 +42,7 @@ CLI_PROGRAMS = {
     "kcl": "kcl_main.cpp",
     "cost_func_cal": "order_main.cpp",
     "kcore_direction": "order_main.cpp",
+    "Peel": "order_main.cpp",
 }
 
 

@@ -5,6 +5,8 @@
 //   a_order <edges.bin>              vertex_ordering/A-order/A-order.cpp:62-247
 //        writes normal and reordered in the working directory
 //   cost_func_cal <edges.bin> <k>    tools/costFuncCal.cpp:15-95 (prints the three costs)
+//   Peel <in> <out> [--compat]       edge_directing/A-direction-parallel/peel.cu:130-317 (uint64
+//        edges, src = x >> 32; --compat keeps the program's minor-priority term, peel.cu:49)
 //   kcore_direction <in> <out>       edge_directing/kcore_direction.cpp:12-146 (uint64 edges,
 //        src = x >> 32; writes the oriented uint64 edges to <out>)
 #include <cstdio>
@@ -74,6 +76,18 @@ int main(int argc, char** argv) {
   std::cout << "idPartCost: " << c[0] << std::endl;
   std::cout << "degreePartCost: " << c[1] << std::endl;
   std::cout << "lpPartCost: " << c[2] << std::endl;
+#elif defined(ATC_PROGRAM_PEEL)
+  if (argc < 3) { fprintf(stderr, "Usage: ./Peel inputFileName outFileName [--compat]\n"); return 2; }
+  const int compat = argc > 3 && strcmp(argv[3], "--compat") == 0;
+  std::vector<uint64_t> packed(np), out(np ? np : 1);
+  if (np) memcpy(packed.data(), pairs.data(), 8 * np);
+  uint64_t nv = 0;
+  int32_t iters = 0;
+  s = atc_adirection_par(packed.data(), np, compat, out.data(), nullptr, nullptr, &nv, &iters, nullptr);
+  if (s != ATC_OK) return fail("atc_adirection_par", s);
+  std::cout << "the node num is " << nv << ", and the edgeNum is " << np << std::endl;
+  std::cout << "iterations " << iters << std::endl;
+  if (!write_pairs(argv[2], reinterpret_cast<const int32_t*>(out.data()), np)) return 1;
 #elif defined(ATC_PROGRAM_KCORE_DIRECTION)
   if (argc < 3) { fprintf(stderr, "usage: %s <in> <out>\n", argv[0]); return 2; }
   // the file's bytes read as little-endian uint64 edges

@@ -46,6 +46,12 @@ atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* pr
 // Core numbers (n_in ints, device) of the simple graph given by canonical keys.
 atc_status core_numbers(const SimpleEdges& e, const int32_t* deg, int32_t* core, cudaStream_t s);
 
+// Approximate parallel A-direction peel (edge_directing/A-direction-parallel/peel.cu:130-262)
+// of the simple graph: flags (major priority, 0xFFFFFFFF = never peeled) and minor
+// priority (n_in each, device).  iters_out: the reference's itera_times at exit.
+atc_status approx_peel(const SimpleEdges& e, const int32_t* deg, uint32_t* flags, uint32_t* minor, int* iters_out,
+                       cudaStream_t s);
+
 // A-order lookup (vertex_ordering/A-order/A-order.cpp:62-210) of an edge list with
 // repeats counted.  Edges come either as int2 pairs or as canonical keys (exactly one
 // non-null).  n_v = max id + 1 over the edges.  lookup: n_v ints (device).  If

@@ -259,4 +259,132 @@ atc_status core_numbers(const SimpleEdges& e, const int32_t* deg, int32_t* core,
   return ATC_OK;
 }
 
+// ---- approximate parallel peel (edge_directing/A-direction-parallel/peel.cu:130-317) ----
+// Frontier-synchronous: a frontier is every unpeeled vertex whose runtime degree (simple
+// degree minus peeled neighbours, uint32) is <= a limit; it gets the iteration number as
+// its major priority and its runtime degree as minor priority.  The limit starts at
+// (uint32)(m / n) and grows by that step when a frontier comes out empty or small
+// (peel.cu:239-246, 255); the loop stops at 90 % of the vertices, depth 255 or 50
+// iterations (:217), and the vertices left keep flag 0xFFFFFFFF and their simple degree.
+// Which vertices join a frontier depends only on the set of the previous frontier, so
+// the atomic order inside a pass does not matter.
+namespace {
+
+constexpr uint32_t kUnpeeled = 0xFFFFFFFFu;
+
+__global__ void apeel_init_kernel(const int32_t* deg, int64_t n, uint32_t* rd, uint32_t* flags, uint32_t* minor) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    rd[v] = (uint32_t)deg[v];
+    minor[v] = (uint32_t)deg[v];
+    flags[v] = kUnpeeled;
+  }
+}
+
+// peel.cu:95-117 (advance + back_nbr_count): every unpeeled neighbour w of a frontier
+// vertex loses one runtime degree per frontier neighbour.  The lists are symmetric and
+// duplicate-free, so counting from the frontier side gives the same sums.
+__global__ void apeel_lower_kernel(const int32_t* frontier, int nf, const int64_t* off, const int32_t* adj,
+                                   const uint32_t* flags, uint32_t* rd) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < nf; i += warps) {
+    const int32_t u = frontier[i];
+    for (int64_t j = off[u] + lane; j < off[u + 1]; j += 32) {
+      const int32_t w = adj[j];
+      if (flags[w] == kUnpeeled) atomicSub(&rd[w], 1u);
+    }
+  }
+}
+
+// peel.cu:239-262: frontier = {v : rd[v] <= limit} (peeled vertices hold rd = 0xFFFFFFFF);
+// each member takes flag `it`, minor = rd, rd = 0xFFFFFFFF.  Counts only when `assign` is 0.
+// Whole warps step through the ids together so the ballot covers all 32 lanes.
+__global__ void apeel_select_kernel(uint32_t* rd, uint32_t* flags, uint32_t* minor, int64_t n, uint32_t limit,
+                                    uint32_t it, int assign, int32_t* frontier, int* count) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; v0 < n; v0 += stride) {
+    const int64_t v = v0 + lane;
+    const uint32_t r = v < n ? rd[v] : 0u;
+    const bool in = v < n && r <= limit;
+    const unsigned ballot = __ballot_sync(0xffffffffu, in);
+    if (!ballot) continue;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(count, __popc(ballot));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (in && assign) {
+      frontier[base + __popc(ballot & ((1u << lane) - 1))] = (int32_t)v;
+      flags[v] = it;
+      minor[v] = r;
+      rd[v] = kUnpeeled;
+    }
+  }
+}
+
+}  // namespace
+
+atc_status approx_peel(const SimpleEdges& e, const int32_t* deg, uint32_t* flags, uint32_t* minor, int* iters_out,
+                       cudaStream_t s) {
+  const int64_t n = e.n_in, m = e.m;
+  if (iters_out) *iters_out = 0;
+  if (n == 0) return ATC_OK;
+  DevBuf<int64_t> off;
+  DevBuf<unsigned long long> cur;
+  DevBuf<int32_t> adj, fr;
+  DevBuf<uint32_t> rd;
+  DevBuf<int> cnt;
+  ATC_TRY(off.alloc(n + 1, s));
+  ATC_TRY(exclusive_scan_i32_to_i64(deg, off.p, n, s));
+  int64_t total = 2 * m;
+  ATC_CK(cudaMemcpyAsync(off.p + n, &total, sizeof(total), cudaMemcpyHostToDevice, s));
+  ATC_TRY(cur.alloc(n, s));
+  ATC_CK(cudaMemcpyAsync(cur.p, off.p, sizeof(int64_t) * n, cudaMemcpyDeviceToDevice, s));
+  ATC_TRY(adj.alloc(total, s));
+  if (m) sym_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(e.keys.p, m, e.bits, cur.p, adj.p);
+  ATC_CK(cudaGetLastError());
+  cur.release();
+  ATC_TRY(rd.alloc(n, s));
+  ATC_TRY(fr.alloc(n, s));
+  ATC_TRY(cnt.alloc(1, s));
+  apeel_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(deg, n, rd.p, flags, minor);
+  ATC_CK(cudaGetLastError());
+
+  // host arithmetic in the reference's types: float threshold, uint32 limits and counts
+  const uint32_t node_num = (uint32_t)n, edge_num = (uint32_t)(2 * m);
+  const float deg_thre = (float)edge_num / 2 / node_num;
+  const uint32_t step = (uint32_t)deg_thre;
+  const uint32_t stop_at = node_num * 9 / 10;
+  int hcnt = 0;
+  auto select = [&](uint32_t limit, uint32_t it, int assign, int* nf) -> atc_status {
+    ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int), s));
+    apeel_select_kernel<<<grid_for(n, 256), 256, 0, s>>>(rd.p, flags, minor, n, limit, it, assign, fr.p, cnt.p);
+    ATC_CK(cudaGetLastError());
+    ATC_CK(cudaMemcpyAsync(&hcnt, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    *nf = hcnt;
+    return ATC_OK;
+  };
+  int f_size = 0;
+  ATC_TRY(select(step, 1, 1, &f_size));
+  uint32_t visited = (uint32_t)f_size;
+  uint32_t depth = 1, it = 1;
+  while (visited < stop_at && depth < 0xFF && it < 50) {
+    ++it;
+    if (f_size)
+      apeel_lower_kernel<<<grid_for((int64_t)f_size * 32, 256), 256, 0, s>>>(fr.p, f_size, off.p, adj.p, flags, rd.p);
+    ATC_CK(cudaGetLastError());
+    int cand = 0;
+    ATC_TRY(select(step * depth, it, 0, &cand));
+    while (cand == 0 && depth < 0xFF && visited < stop_at) {
+      ++depth;
+      ATC_TRY(select(step * depth, it, 0, &cand));
+    }
+    ATC_TRY(select(step * depth, it, 1, &f_size));
+    visited += (uint32_t)f_size;
+    if ((uint32_t)f_size <= node_num / 500) ++depth;
+  }
+  if (iters_out) *iters_out = (int)it;
+  return ATC_OK;
+}
+
 }  // namespace atc

@@ -63,7 +63,8 @@ __global__ void degree_kernel(const uint64_t* keys, int64_t m, int B, int32_t* d
 
 struct OrientArgs {
   const int32_t* deg;   // simple degree, by input id
-  const int32_t* prio;  // A-direction priority, by input id (ADIRECTION only)
+  const int32_t* prio;  // A-direction priority / core number / peel flag, by input id
+  const uint32_t* minor;  // approximate peel's minor priority (ADIRECTION_PAR only)
   const int32_t* perm;  // new id of every input id (A-order), or null
   const int32_t* cmap;  // compacted id of every (new) id when pruning, or null
   int dir;
@@ -100,6 +101,12 @@ __global__ void orient_kernel(const uint64_t* ek, int64_t m, OrientArgs a, uint6
       case ATC_DIR_KCORE: {
         int32_t cx = a.prio[x], cy = a.prio[y];
         x_src = cx < cy || (cx == cy && xn < yn);
+        break;
+      }
+      case ATC_DIR_ADIRECTION_PAR: {  // flags compare as int32 (0xFFFFFFFF = -1)
+        int32_t fx = a.prio[x], fy = a.prio[y];
+        int32_t mx = (int32_t)a.minor[x], my = (int32_t)a.minor[y];
+        x_src = fx < fy || (fx == fy && (mx < my || (mx == my && xn < yn)));
         break;
       }
       default: {
@@ -280,7 +287,7 @@ atc_status simple_degrees(const SimpleEdges& e, int32_t* deg, cudaStream_t s) {
 static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_order order, const atc_tuning* t,
                              atc_csr* out, int32_t* perm_out, cudaStream_t s) {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
-  ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_KCORE, "unknown atc_dir");
+  ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION_PAR, "unknown atc_dir");
   ATC_CHECK_ARG(order == ATC_ORDER_NONE || order == ATC_ORDER_AORDER, "unknown atc_order");
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
@@ -288,6 +295,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   ATC_TRY(build_simple_edges(pairs, np, &e, s));
   int64_t n_in = e.n_in;
   DevBuf<int32_t> deg, prio, perm, cmap;
+  DevBuf<uint32_t> minor;
   ATC_TRY(deg.alloc(n_in, s));
   ATC_TRY(simple_degrees(e, deg.p, s));
   if (order == ATC_ORDER_AORDER) {
@@ -317,6 +325,10 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   } else if (dir == ATC_DIR_KCORE) {
     ATC_TRY(prio.alloc(n_in, s));
     ATC_TRY(core_numbers(e, deg.p, prio.p, s));
+  } else if (dir == ATC_DIR_ADIRECTION_PAR) {
+    ATC_TRY(prio.alloc(n_in, s));
+    ATC_TRY(minor.alloc(n_in, s));
+    ATC_TRY(approx_peel(e, deg.p, reinterpret_cast<uint32_t*>(prio.p), minor.p, nullptr, s));
   }
   int64_t n = n_in;
   if (prune) {
@@ -343,7 +355,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   ATC_TRY(k2.alloc(e.m, s));
   ATC_TRY(dropped.alloc(1, s));
   ATC_CK(cudaMemsetAsync(dropped.p, 0, sizeof(unsigned long long), s));
-  OrientArgs oa{deg.p, prio.p, perm.p, cmap.p, (int)dir, e.bits, bout};
+  OrientArgs oa{deg.p, prio.p, minor.p, perm.p, cmap.p, (int)dir, e.bits, bout};
   if (e.m) orient_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, oa, k1.p, dropped.p);
   ATC_CK(cudaGetLastError());
   e.keys.release();
@@ -478,7 +490,7 @@ extern "C" atc_status atc_adirection(const int32_t* pairs, uint64_t np, int32_t*
   ATC_TRY(k1.alloc(e.m, s));
   ATC_TRY(k2.alloc(e.m, s));
   ATC_TRY(dropped.alloc(1, s));
-  OrientArgs oa{deg.p, prio.p, nullptr, nullptr, ATC_DIR_ADIRECTION, e.bits, e.bits};
+  OrientArgs oa{deg.p, prio.p, nullptr, nullptr, nullptr, ATC_DIR_ADIRECTION, e.bits, e.bits};
   if (e.m) orient_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, oa, k1.p, dropped.p);
   ATC_CK(cudaGetLastError());
   uint64_t* ka = k1.p;
@@ -544,6 +556,64 @@ extern "C" atc_status atc_kcore_direction(const uint64_t* edges, uint64_t ne, ui
   if (core_out) ATC_CK(cudaMemcpyAsync(core_out, core.p, sizeof(int32_t) * e.n_in, cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   if (n_vertices) *n_vertices = (uint64_t)e.n_in;
+  return ATC_OK;
+}
+
+// ---- approximate parallel A-direction (edge_directing/A-direction-parallel/peel.cu) -----
+namespace atc {
+// peel.cu:44-59: swap iff flag_d > 0, or flag_d == 0 and minor_d > 0, or both 0 and
+// src > dst, with flag_d = (int)(flag[src] - flag[dst]) and minor_d = (int)(minor[src] -
+// (compat ? flag[dst] : minor[dst])) in wrapping 32-bit arithmetic.
+__global__ void apeel_orient_kernel(const int2* p, int64_t ne, const uint32_t* flags, const uint32_t* minor,
+                                    int compat, uint64_t* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ne; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t a = (uint32_t)p[i].x, b = (uint32_t)p[i].y;
+    const int32_t flag_d = (int32_t)(flags[a] - flags[b]);
+    const int32_t minor_d = (int32_t)(minor[a] - (compat ? flags[b] : minor[b]));
+    if (flag_d > 0 || (flag_d == 0 && minor_d > 0) || (flag_d == 0 && minor_d == 0 && a > b)) {
+      const uint32_t t = a;
+      a = b;
+      b = t;
+    }
+    out[i] = ((uint64_t)a << 32) | b;
+  }
+}
+}  // namespace atc
+
+extern "C" atc_status atc_adirection_par(const uint64_t* edges, uint64_t ne, int compat, uint64_t* oriented_out,
+                                         uint32_t* flags_out, uint32_t* minor_out, uint64_t* n_vertices,
+                                         int32_t* iterations, atc_stream st) {
+  ATC_CHECK_ARG(ne == 0 || (edges != nullptr && oriented_out != nullptr), "NULL array");
+  cudaStream_t s = as_stream(st);
+  keep_pool();
+  if (n_vertices) *n_vertices = 0;
+  if (iterations) *iterations = 0;
+  if (ne == 0) return ATC_OK;
+  DevBuf<uint64_t> de;
+  DevBuf<int2> d;
+  ATC_TRY(de.alloc(ne, s));
+  ATC_TRY(d.alloc(ne, s));
+  ATC_CK(cudaMemcpyAsync(de.p, edges, sizeof(uint64_t) * ne, cudaMemcpyHostToDevice, s));
+  atc::unpack_u64_pairs_kernel<<<grid_for(ne, 256), 256, 0, s>>>(de.p, ne, d.p);
+  ATC_CK(cudaGetLastError());
+  SimpleEdges e;
+  ATC_TRY(build_simple_edges(d.p, ne, &e, s));
+  DevBuf<int32_t> deg;
+  DevBuf<uint32_t> flags, minor;
+  ATC_TRY(deg.alloc(e.n_in, s));
+  ATC_TRY(flags.alloc(e.n_in, s));
+  ATC_TRY(minor.alloc(e.n_in, s));
+  ATC_TRY(simple_degrees(e, deg.p, s));
+  int iters = 0;
+  ATC_TRY(approx_peel(e, deg.p, flags.p, minor.p, &iters, s));
+  atc::apeel_orient_kernel<<<grid_for(ne, 256), 256, 0, s>>>(d.p, ne, flags.p, minor.p, compat, de.p);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaMemcpyAsync(oriented_out, de.p, sizeof(uint64_t) * ne, cudaMemcpyDeviceToHost, s));
+  if (flags_out) ATC_CK(cudaMemcpyAsync(flags_out, flags.p, sizeof(uint32_t) * e.n_in, cudaMemcpyDeviceToHost, s));
+  if (minor_out) ATC_CK(cudaMemcpyAsync(minor_out, minor.p, sizeof(uint32_t) * e.n_in, cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (n_vertices) *n_vertices = (uint64_t)e.n_in;
+  if (iterations) *iterations = iters;
   return ATC_OK;
 }
 

@@ -52,7 +52,12 @@ typedef enum atc_dir {
   ATC_DIR_ADIRECTION = 3,
   /* k-core: lower core number first; equal cores: the smaller id is the source
      (edge_directing/kcore_direction.cpp:91-146, with true degrees; see atc_pretc). */
-  ATC_DIR_KCORE = 4
+  ATC_DIR_KCORE = 4,
+  /* approximate parallel A-direction: per vertex a peel iteration `flag` (0xFFFFFFFF for
+     vertices never peeled, which compare as -1, i.e. first) and a minor priority; the
+     source is the endpoint with the smaller (flag, minor, id)
+     (edge_directing/A-direction-parallel/peel.cu:44-59, 130-262; see atc_adirection_par). */
+  ATC_DIR_ADIRECTION_PAR = 5
 } atc_dir;
 
 typedef enum atc_order {
@@ -195,6 +200,17 @@ atc_status atc_adirection(const int32_t* pairs, uint64_t n_pairs, int32_t* orien
    counts all of them. */
 atc_status atc_kcore_direction(const uint64_t* edges, uint64_t n_edges, uint64_t* oriented_out,
                                int32_t* core_out, uint64_t* n_vertices, atc_stream s);
+/* Peel <in> <out> (edge_directing/A-direction-parallel/peel.cu:130-317): edges packed as
+   uint64 (src = x >> 32); writes one packed edge per input edge, in input order, directed
+   by the approximate parallel peel's (flag, minor, id) ranking.  compat != 0 reproduces
+   the program's comparison exactly, including its minor term minor[src] - flag[dst]
+   (peel.cu:49, where minor[dst] is meant); compat == 0 compares minor[src] - minor[dst].
+   flags_out / minor_out (nullable, max id + 1 entries each) receive the two priorities,
+   *n_vertices (nullable) = max id + 1, *iterations (nullable) the program's final
+   itera_times.  Ids must be < 2^31. */
+atc_status atc_adirection_par(const uint64_t* edges, uint64_t n_edges, int compat, uint64_t* oriented_out,
+                              uint32_t* flags_out, uint32_t* minor_out, uint64_t* n_vertices, int32_t* iterations,
+                              atc_stream s);
 /* A-order <file> (vertex_ordering/A-order/A-order.cpp:62-247) on the raw pairs,
    repeats included: `lookup` (max id + 1 ints) = new id of every id (badLookUpTable);
    `normal` / `reordered` (n_pairs pairs each, nullable) = the two output files.

@@ -709,6 +709,79 @@ void orc_core_numbers(const int32_t* pairs, uint64_t np, int32_t* core) {
   for (int64_t v = 0; v < n; ++v) core[v] = (int32_t)deg[v];
 }
 
+// The approximate parallel A-direction program, step for step
+// (edge_directing/A-direction-parallel/peel.cu:130-317, buildCSR.cu:75-201): the simple
+// symmetric CSR of the input (loops and repeats dropped), the float threshold
+// (float)edgeNum/2/nodeNum over directed entries, frontiers collected in id order
+// (thrust::copy_if), advance marking unpeeled neighbours (:77-95), back_nbr_count from the
+// reached side (:96-117), the depth / 90 % / 50-iteration stopping rules (:217-262) and the
+// per-edge output comparison (:44-59).  Input: packed uint64 edges (src = x >> 32).
+// Outputs: flags, minor (n each), oriented (ne), iterations.
+void orc_adirection_par(const uint64_t* edges, uint64_t ne, int compat, uint64_t* oriented, uint32_t* flags_out,
+                        uint32_t* minor_out, int32_t* iterations) {
+  std::vector<int32_t> pairs(2 * ne);
+  for (uint64_t i = 0; i < ne; ++i) {
+    pairs[2 * i] = (int32_t)(uint32_t)(edges[i] >> 32);
+    pairs[2 * i + 1] = (int32_t)(uint32_t)edges[i];
+  }
+  Adj g = build_adj(pairs.data(), ne);
+  const uint32_t node_num = (uint32_t)g.n;
+  const uint32_t edge_num = (uint32_t)g.off[g.n];
+  const uint32_t MAXV = 0xFFFFFFFFu;
+  std::vector<uint32_t> flags(node_num, MAXV), rd(node_num), minor(node_num);
+  for (uint32_t v = 0; v < node_num; ++v) rd[v] = minor[v] = (uint32_t)(g.off[v + 1] - g.off[v]);
+  const float deg_thre = (float)edge_num / 2 / node_num;
+  auto collect = [&](uint32_t limit) {
+    std::vector<uint32_t> f;
+    for (uint32_t v = 0; v < node_num; ++v)
+      if (rd[v] <= limit) f.push_back(v);
+    return f;
+  };
+  auto take = [&](const std::vector<uint32_t>& f, uint32_t it) {
+    for (uint32_t v : f) flags[v] = it;
+    for (uint32_t v : f) minor[v] = rd[v];
+    for (uint32_t v : f) rd[v] = MAXV;
+  };
+  std::vector<uint32_t> F = collect((uint32_t)deg_thre);
+  uint32_t visited = (uint32_t)F.size();
+  take(F, 1);
+  uint32_t depth = 1, it = 1;
+  std::vector<uint8_t> reached(node_num), last(node_num);
+  while (visited < node_num * 9 / 10 && depth < 0xFF && it < 50) {
+    ++it;
+    std::fill(reached.begin(), reached.end(), 0);
+    for (uint32_t u : F)
+      for (int64_t j = g.off[u]; j < g.off[u + 1]; ++j)
+        if (flags[g.nbr[j]] == MAXV) reached[g.nbr[j]] = 1;
+    std::fill(last.begin(), last.end(), 0);
+    for (uint32_t u : F) last[u] = 1;
+    for (uint32_t w = 0; w < node_num; ++w) {
+      if (!reached[w]) continue;
+      uint32_t sum = 0;
+      for (int64_t j = g.off[w]; j < g.off[w + 1]; ++j) sum += last[g.nbr[j]] != 0;
+      rd[w] -= sum;
+    }
+    F = collect((uint32_t)deg_thre * depth);
+    while (F.empty() && depth < 0xFF && visited < 9 * node_num / 10) {
+      ++depth;
+      F = collect((uint32_t)deg_thre * depth);
+    }
+    visited += (uint32_t)F.size();
+    take(F, it);
+    if (F.size() <= node_num / 500) ++depth;
+  }
+  for (uint64_t i = 0; i < ne; ++i) {
+    uint32_t a = (uint32_t)(edges[i] >> 32), b = (uint32_t)edges[i];
+    int flag_d = (int)flags[a] - flags[b];
+    int minor_d = (int)minor[a] - (compat ? flags[b] : minor[b]);
+    if (flag_d > 0 || (flag_d == 0 && minor_d > 0) || (flag_d == 0 && minor_d == 0 && a > b)) std::swap(a, b);
+    oriented[i] = ((uint64_t)a << 32) | b;
+  }
+  if (flags_out) std::copy(flags.begin(), flags.end(), flags_out);
+  if (minor_out) std::copy(minor.begin(), minor.end(), minor_out);
+  if (iterations) *iterations = (int32_t)it;
+}
+
 // Masked-MSE loss and gradients of the selector MLP in double precision: the checker for
 // the library's FP32 training kernels.  Same parameter layout (W1[I][H] b1 W2[H][H] b2
 // W3[H][O] b3), ReLU hidden layers, inputs standardised with (mean, std) first.

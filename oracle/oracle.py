@@ -47,6 +47,7 @@ def lib():
         L.orc_mlp_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P,
                                    C.POINTER(C.c_double)]
         L.orc_core_numbers.argtypes = [_P, C.c_uint64, _P]
+        L.orc_adirection_par.argtypes = [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]
         L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
         L.orc_hu_csr.restype = C.c_int64
@@ -168,6 +169,20 @@ def core_numbers(pairs):
     out = np.empty(max(n, 1), dtype=np.int32)
     lib().orc_core_numbers(_ptr(p), p.shape[0], _ptr(out))
     return out[:n]
+
+
+def adirection_par(edges_u64, compat=False):
+    """peel.cu on packed uint64 edges: (oriented edges, flags, minor, iterations)."""
+    e = np.ascontiguousarray(edges_u64, dtype=np.uint64)
+    hi = (e >> np.uint64(32)).max() if e.size else 0
+    lo = (e & np.uint64(0xFFFFFFFF)).max() if e.size else 0
+    n = int(max(hi, lo)) + 1 if e.size else 0
+    out = np.empty(max(e.size, 1), dtype=np.uint64)
+    flags = np.empty(max(n, 1), dtype=np.uint32)
+    minor = np.empty(max(n, 1), dtype=np.uint32)
+    it = np.zeros(1, dtype=np.int32)
+    lib().orc_adirection_par(_ptr(e), e.size, 1 if compat else 0, _ptr(out), _ptr(flags), _ptr(minor), _ptr(it))
+    return out[: e.size], flags[:n], minor[:n], int(it[0])
 
 
 def costfunc(pairs, k):

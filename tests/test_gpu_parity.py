@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 
 CASES = sorted(load_golden()["cases"])
 KERNELS = [atc.Kernel.HU, atc.Kernel.BISSON, atc.Kernel.FOX, atc.Kernel.TRICORE]
-DIRS = [atc.Dir.ID, atc.Dir.DEGREE, atc.Dir.DEGREE_LOWID, atc.Dir.ADIRECTION, atc.Dir.KCORE]
+DIRS = [atc.Dir.ID, atc.Dir.DEGREE, atc.Dir.DEGREE_LOWID, atc.Dir.ADIRECTION, atc.Dir.KCORE,
+        atc.Dir.ADIRECTION_PAR]
 
 
 def sha(a):
@@ -295,6 +296,10 @@ def test_cli_dropins(tmp_path):
     r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout
+    r = subprocess.run([os.path.join(bindir, "Peel"), str(tmp_path / "E.u64"), str(tmp_path / "P.u64")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(np.fromfile(tmp_path / "P.u64", dtype=np.uint64), oracle.adirection_par(u64)[0])
     r = subprocess.run([os.path.join(bindir, "kcore_direction"), str(tmp_path / "E.u64"), str(tmp_path / "K.u64")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -436,3 +441,45 @@ def test_kcore_direction_program_matches_oracle():
         swap = (want_core[a] > want_core[b]) | ((want_core[a] == want_core[b]) & (a > b))
         assert np.array_equal(src, np.where(swap, b, a)) and np.array_equal(dst, np.where(swap, a, b))
     assert atc.kcore_direction(np.zeros(0, dtype=np.uint64)).size == 0
+
+
+def _packed(g):
+    return (g[:, 0].astype(np.uint64) << np.uint64(32)) | g[:, 1].astype(np.uint32).astype(np.uint64)
+
+
+def _apeel_graphs():
+    rng = np.random.default_rng(21)
+    yield "rmat12-sym", atc.rmat_graph(12, 16, 2)
+    yield "rmat13-once", atc.simplify(atc.gen_rmat(13, 8, 9), symmetric=False)
+    yield "rmat11-raw", atc.gen_rmat(11, 16, 4)                       # repeats and loops kept
+    yield "uniform", rng.integers(0, 2000, size=(20000, 2)).astype(np.int32)
+    yield "rgg", atc.gen_rgg(20000, 12.0, 3)
+    yield "sparse", rng.integers(0, 5000, size=(2000, 2)).astype(np.int32)  # m / n < 1
+    yield "clique", np.array([(i, j) for i in range(40) for j in range(40) if i != j], dtype=np.int32)
+
+
+@pytest.mark.parametrize("compat", [False, True])
+def test_adirection_par_matches_oracle(compat):
+    """peel.cu:130-317 bit-exact: flags, minor priorities, iterations and the output file."""
+    for name, g in _apeel_graphs():
+        e = _packed(g)
+        got = atc.adirection_par(e, compat=compat)
+        want = oracle.adirection_par(e, compat=compat)
+        assert np.array_equal(got[1], want[1]), name
+        assert np.array_equal(got[2], want[2]), name
+        assert got[3] == want[3], name
+        assert np.array_equal(got[0], want[0]), name
+
+
+def test_adirection_par_direction_in_pretc():
+    for name, g in _apeel_graphs():
+        _, flags, minor, _ = oracle.adirection_par(_packed(g))
+        off, cols = atc.pretc(g, atc.Dir.ADIRECTION_PAR).to_host()
+        src = np.repeat(np.arange(off.size - 1), np.diff(off))
+        fs, fd = flags.view(np.int32)[src], flags.view(np.int32)[cols]
+        ms, md = minor.astype(np.int64)[src], minor.astype(np.int64)[cols]
+        assert np.all((fs < fd) | ((fs == fd) & ((ms < md) | ((ms == md) & (src < cols))))), name
+        assert off[-1] == oracle.simple_stats(g)[1], name
+        want = oracle.tc_count(g)
+        for k in KERNELS:
+            assert atc.tc(atc.pretc(g, atc.Dir.ADIRECTION_PAR), k)[0] == want, (name, k.name)

@@ -146,3 +146,37 @@ def test_oracle_core_numbers_match_networkx():
         want = nx.core_number(G)
         got = oracle.core_numbers(g)
         assert all(got[v] == want[v] for v in G.nodes)
+
+
+def _pack(pairs):
+    p = np.asarray(pairs, dtype=np.uint64).reshape(-1, 2)
+    return (p[:, 0] << np.uint64(32)) | p[:, 1]
+
+
+def test_oracle_adirection_par_hand_worked():
+    """peel.cu:130-317 worked by hand on a star 0-{1,2,3,4} plus edge 1-2: m/n = 1, the
+    first frontier is the two leaves {3, 4}; vertex 0 drops to degree 2, the next limit 1
+    finds nothing, the depth rises to 2 and {0, 1, 2} join as iteration 2."""
+    e = _pack([[0, 1], [0, 2], [0, 3], [0, 4], [1, 2], [3, 0]])
+    out, flags, minor, it = oracle.adirection_par(e)
+    assert flags.tolist() == [2, 2, 2, 1, 1]
+    assert minor.tolist() == [2, 2, 2, 1, 1]
+    assert it == 2
+    assert out.tolist() == _pack([[0, 1], [0, 2], [3, 0], [4, 0], [1, 2], [3, 0]]).tolist()
+
+
+def test_oracle_adirection_par_compat_term():
+    """The compat comparison uses minor[src] - flag[dst] (peel.cu:49).  A 4-cycle 0-1-2-3
+    with chord 0-2: m/n = 1.25 -> limit 1 and no degree is <= 1, so the depth climbs to 2
+    and {1, 3} (degree 2) join as iteration 2; 0 and 2 (degree 3, now 1) join as 3."""
+    e = _pack([[0, 1], [1, 2], [2, 3], [3, 0], [0, 2], [2, 0]])
+    out, flags, minor, it = oracle.adirection_par(e)
+    assert flags.tolist() == [3, 2, 3, 2]
+    assert minor.tolist() == [1, 2, 1, 2]
+    assert it == 3
+    # fixed rule: 1 -> 0, 1 -> 2, 3 -> 2, 3 -> 0; 0 and 2 tie on flag and minor, 0 first
+    assert out.tolist() == _pack([[1, 0], [1, 2], [3, 2], [3, 0], [0, 2], [0, 2]]).tolist()
+    out_c, _, _, _ = oracle.adirection_par(e, compat=True)
+    # compat: minor[0] - flag[2] = 1 - 3 < 0 keeps 0 -> 2, and minor[2] - flag[0] < 0 keeps
+    # 2 -> 0 as well: the program's rule is not antisymmetric
+    assert out_c.tolist() == _pack([[1, 0], [1, 2], [3, 2], [3, 0], [0, 2], [2, 0]]).tolist()
