@@ -46,6 +46,14 @@ class Dir(enum.IntEnum):
 class Order(enum.IntEnum):
     NONE = 0
     AORDER = 1
+    DEGREE_DESC = 2
+    AORDER_V2 = 3
+
+
+class Relabel(enum.IntEnum):
+    DEGREE_DESC = 0
+    AORDER_V2 = 1
+    OUTDEG_DESC = 2
 
 
 class Kernel(enum.IntEnum):
@@ -139,6 +147,7 @@ _SIGS = {
     "atc_csr_load": (C.c_int, [C.c_char_p, C.POINTER(CSRStruct), _P]),
     "atc_adirection": (C.c_int, [_P, C.c_uint64, _P, C.POINTER(C.c_uint64), _P, _P]),
     "atc_aorder": (C.c_int, [_P, C.c_uint64, _P, _P, _P, _P]),
+    "atc_relabel": (C.c_int, [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]),
     "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_tc_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_uint64), _P]),
     "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
@@ -554,6 +563,17 @@ def adirection_par(edges_u64, compat=False, stream=None):
     _check(lib().atc_adirection_par(_ptr(e), e.size, 1 if compat else 0, _ptr(out), _ptr(flags), _ptr(minor),
                                     C.byref(nv), C.byref(it), stream))
     return out[: e.size].copy(), flags[: nv.value].copy(), minor[: nv.value].copy(), it.value
+
+
+def relabel(pairs, kind, stream=None):
+    """(lookup, normal, relabeled) as A-order-v2 / relabel-naive / relabel4lpOut compute them."""
+    p = _pairs(pairs)
+    n_v = int(p.max()) + 1 if p.size else 1
+    lookup = np.empty(n_v, dtype=np.int32)
+    normal = np.empty((max(p.shape[0], 1), 2), dtype=np.int32)
+    rel = np.empty_like(normal)
+    _check(lib().atc_relabel(_ptr(p), p.shape[0], int(kind), _ptr(lookup), _ptr(normal), _ptr(rel), stream))
+    return lookup, normal[: p.shape[0]], rel[: p.shape[0]]
 
 
 def aorder(pairs, stream=None):

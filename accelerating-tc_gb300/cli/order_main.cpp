@@ -4,6 +4,8 @@
 //        writes lpBasedGraph (text "src dst") and lpBasedGraph.bin in the working directory
 //   a_order <edges.bin>              vertex_ordering/A-order/A-order.cpp:62-247
 //        writes normal and reordered in the working directory
+//   a_order_v2 <edges.bin>           vertex_ordering/A-order/A-order-v2.cpp:14-193
+//        writes naive (and the empty degreeOrder) in the working directory
 //   cost_func_cal <edges.bin> <k>    tools/costFuncCal.cpp:15-95 (prints the three costs)
 //   Peel <in> <out> [--compat]       edge_directing/A-direction-parallel/peel.cu:130-317 (uint64
 //        edges, src = x >> 32; --compat keeps the program's minor-priority term, peel.cu:49)
@@ -68,6 +70,13 @@ int main(int argc, char** argv) {
   s = atc_aorder(pairs.data(), np, lookup.data(), normal.data(), reordered.data(), nullptr);
   if (s != ATC_OK) return fail("atc_aorder", s);
   if (!write_pairs("normal", normal.data(), np) || !write_pairs("reordered", reordered.data(), np)) return 1;
+#elif defined(ATC_PROGRAM_A_ORDER_V2)
+  int32_t mx = 0;
+  for (int32_t x : pairs) mx = x > mx ? x : mx;
+  std::vector<int32_t> lookup((size_t)mx + 1), naive(pairs.size() + 2);
+  s = atc_relabel(pairs.data(), np, ATC_RELABEL_AORDER_V2, lookup.data(), nullptr, naive.data(), nullptr);
+  if (s != ATC_OK) return fail("atc_relabel", s);
+  if (!write_pairs("naive", naive.data(), np) || !write_pairs("degreeOrder", naive.data(), 0)) return 1;
 #elif defined(ATC_PROGRAM_COST_FUNC_CAL)
   if (argc < 3) { fprintf(stderr, "usage: %s <edges.bin> <k>\n", argv[0]); return 2; }
   float c[3];

@@ -84,6 +84,32 @@ __global__ void rt_kernel(const int2* p, const uint64_t* k, int B, uint64_t ne, 
   }
 }
 
+// rt = out-degree of the pairs as given (relabel4lpOut.cpp:27-31); oriented = the input.
+__global__ void outdeg_kernel(const int2* p, uint64_t ne, int32_t* rt, int2* oriented) {
+  uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ne; i += stride) {
+    atomicAdd(&rt[p[i].x], 1);
+    if (oriented) oriented[i] = p[i];
+  }
+}
+
+// Rank lookups over the ascending (rt, id) order of all n vertices; q = n - 1 - rank is
+// the position in the reversed (descending) list.
+//   DEGREE_DESC: new id = q (goodLookUpTable, A-order-v2.cpp:67-74).
+//   AORDER_V2:   the descending list dealt into 40 columns of chunk = n / 40 rows,
+//                position i + 40 j <- q = i * chunk + j; the last n % 40 stay in place
+//                (A-order-v2.cpp:102-146, the mix without shuffle or reversal).
+__global__ void rank_lookup_kernel(const uint64_t* sorted, int B, int64_t n, int kind, int32_t* lookup) {
+  const uint64_t mask = (1ull << B) - 1;
+  const int64_t chunk = n / 40;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = n - 1 - r;
+    int64_t pos = q;
+    if (kind == ATC_RELABEL_AORDER_V2 && q < 40 * chunk) pos = q / chunk + 40 * (q % chunk);
+    lookup[sorted[r] & mask] = (int32_t)pos;
+  }
+}
+
 __global__ void rt_hist_kernel(const int32_t* rt, int64_t n, int32_t* hist, int* maxrt) {
   int best = 0;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -183,6 +209,46 @@ void bucket_heap(const std::vector<int64_t>& hist, int maxrt, int64_t S, int64_t
 }
 
 }  // namespace
+
+atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int kind,
+                          int32_t* lookup, int2* oriented, cudaStream_t s) {
+  if (n_v <= 0) return ATC_OK;
+  ATC_CHECK_ARG(kind != ATC_RELABEL_OUTDEG_DESC || pairs != nullptr, "OUTDEG_DESC needs pairs");
+  DevBuf<int32_t> deg, rt;
+  DevBuf<int> mx;
+  ATC_TRY(rt.alloc(n_v, s));
+  ATC_TRY(mx.alloc(1, s));
+  ATC_CK(cudaMemsetAsync(rt.p, 0, sizeof(int32_t) * n_v, s));
+  ATC_CK(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
+  if (ne && kind == ATC_RELABEL_OUTDEG_DESC) {
+    outdeg_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, ne, rt.p, oriented);
+  } else if (ne) {
+    ATC_TRY(deg.alloc(n_v, s));
+    ATC_CK(cudaMemsetAsync(deg.p, 0, sizeof(int32_t) * n_v, s));
+    if (pairs) deg_pairs_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, ne, deg.p);
+    else deg_keys_kernel<<<grid_for(ne, 256), 256, 0, s>>>(keys, ne, bits, deg.p);
+    ATC_CK(cudaGetLastError());
+    rt_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, keys, bits, ne, deg.p, rt.p, oriented);
+  }
+  ATC_CK(cudaGetLastError());
+  rt_hist_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(rt.p, n_v, nullptr, mx.p);
+  ATC_CK(cudaGetLastError());
+  int maxrt = 0;
+  ATC_CK(cudaMemcpyAsync(&maxrt, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  const int B = id_bits(n_v), rb = id_bits((int64_t)maxrt + 1);
+  DevBuf<uint64_t> ka, kb;
+  ATC_TRY(ka.alloc(n_v, s));
+  ATC_TRY(kb.alloc(n_v, s));
+  rtid_keys_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(rt.p, n_v, B, ka.p);
+  ATC_CK(cudaGetLastError());
+  uint64_t* a = ka.p;
+  uint64_t* b = kb.p;
+  ATC_TRY(sort_keys_u64(a, b, n_v, 0, B + rb, s));
+  rank_lookup_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(a, B, n_v, kind, lookup);
+  ATC_CK(cudaGetLastError());
+  return ATC_OK;
+}
 
 atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int32_t* lookup,
                          int2* oriented, cudaStream_t s) {
@@ -290,6 +356,37 @@ extern "C" atc_status atc_aorder(const int32_t* pairs, uint64_t np, int32_t* loo
     relabel_pairs_kernel<<<grid_for(np, 256), 256, 0, s>>>(o.p, np, lk.p, r.p);
     ATC_CK(cudaGetLastError());
     ATC_CK(cudaMemcpyAsync(reordered, r.p, sizeof(int2) * np, cudaMemcpyDeviceToHost, s));
+  }
+  ATC_CK(cudaStreamSynchronize(s));
+  return ATC_OK;
+}
+
+extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel_kind kind, int32_t* lookup,
+                                  int32_t* normal, int32_t* relabeled, atc_stream st) {
+  ATC_CHECK_ARG(lookup != nullptr, "lookup is NULL");
+  ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
+  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_OUTDEG_DESC, "unknown atc_relabel_kind");
+  cudaStream_t s = as_stream(st);
+  int maxid = 0;  // the programs start maxNodeId at 0, so an empty list has one vertex
+  for (uint64_t i = 0; i < 2 * np; ++i) {
+    ATC_CHECK_ARG(pairs[i] >= 0, "negative vertex id");
+    maxid = std::max(maxid, (int)pairs[i]);
+  }
+  const int64_t n_v = (int64_t)maxid + 1;
+  DevBuf<int2> d, o, r;
+  DevBuf<int32_t> lk;
+  ATC_TRY(d.alloc(np + 1, s));
+  ATC_TRY(o.alloc(np + 1, s));
+  ATC_TRY(lk.alloc(n_v, s));
+  if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, s));
+  ATC_TRY(relabel_lookup(d.p, nullptr, 1, np, n_v, kind, lk.p, o.p, s));
+  ATC_CK(cudaMemcpyAsync(lookup, lk.p, sizeof(int32_t) * n_v, cudaMemcpyDeviceToHost, s));
+  if (normal && np) ATC_CK(cudaMemcpyAsync(normal, o.p, sizeof(int2) * np, cudaMemcpyDeviceToHost, s));
+  if (relabeled && np) {
+    ATC_TRY(r.alloc(np, s));
+    relabel_pairs_kernel<<<grid_for(np, 256), 256, 0, s>>>(o.p, np, lk.p, r.p);
+    ATC_CK(cudaGetLastError());
+    ATC_CK(cudaMemcpyAsync(relabeled, r.p, sizeof(int2) * np, cudaMemcpyDeviceToHost, s));
   }
   ATC_CK(cudaStreamSynchronize(s));
   return ATC_OK;

@@ -61,6 +61,12 @@ atc_status approx_peel(const SimpleEdges& e, const int32_t* deg, uint32_t* flags
 atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v,
                          int32_t* lookup, int2* oriented, cudaStream_t s);
 
+// Rank relabellings (vertex_ordering/A-order/A-order-v2.cpp, relabel-naive.cpp,
+// relabel4lpOut.cpp) of an edge list with repeats counted: lookup (n_v ints, device);
+// oriented (nullable) = the degree-oriented pairs (or the input, for OUTDEG_DESC).
+atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int kind,
+                          int32_t* lookup, int2* oriented, cudaStream_t s);
+
 // Private part of an atc_csr.
 struct CsrPriv {
   int32_t* esrc = nullptr;       // m: source vertex of every edge, in edge order

@@ -288,7 +288,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
                              atc_csr* out, int32_t* perm_out, cudaStream_t s) {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION_PAR, "unknown atc_dir");
-  ATC_CHECK_ARG(order == ATC_ORDER_NONE || order == ATC_ORDER_AORDER, "unknown atc_order");
+  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_AORDER_V2, "unknown atc_order");
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
   SimpleEdges e;
@@ -298,9 +298,10 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   DevBuf<uint32_t> minor;
   ATC_TRY(deg.alloc(n_in, s));
   ATC_TRY(simple_degrees(e, deg.p, s));
-  if (order == ATC_ORDER_AORDER) {
-    // A-order sees the simple graph with each edge once, as when it reads the output
-    // of A-direction-seri; its id range ends at the largest id that has an edge.
+  if (order != ATC_ORDER_NONE) {
+    // The relabelling programs see the simple graph with each edge once, as when they
+    // read the output of A-direction-seri; their id range ends at the largest id that
+    // has an edge.
     ATC_TRY(perm.alloc(n_in, s));
     iota_kernel<<<grid_for(n_in, 256), 256, 0, s>>>(perm.p, n_in);
     ATC_CK(cudaGetLastError());
@@ -316,7 +317,12 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
       ATC_CK(cudaStreamSynchronize(s));
       n_v = (int64_t)h + 1;
     }
-    ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s));
+    if (order == ATC_ORDER_AORDER)
+      ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s));
+    else
+      ATC_TRY(relabel_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v,
+                             order == ATC_ORDER_DEGREE_DESC ? ATC_RELABEL_DEGREE_DESC : ATC_RELABEL_AORDER_V2, perm.p,
+                             nullptr, s));
   }
   if (dir == ATC_DIR_ADIRECTION) {
     ATC_TRY(prio.alloc(n_in, s));
@@ -391,7 +397,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   ATC_CK(cudaGetLastError());
   unsigned long long hw[3] = {0, 0, 0};
   ATC_CK(cudaMemcpyAsync(hw, counter.p, sizeof(hw), cudaMemcpyDeviceToHost, s));
-  if (perm_out && order == ATC_ORDER_AORDER && n_in)
+  if (perm_out && order != ATC_ORDER_NONE && n_in)
     ATC_CK(cudaMemcpyAsync(perm_out, perm.p, sizeof(int32_t) * n_in, cudaMemcpyDeviceToHost, s));
   else if (perm_out && n_in) {
     std::vector<int32_t> id(n_in);

@@ -63,8 +63,27 @@ typedef enum atc_dir {
 typedef enum atc_order {
   ATC_ORDER_NONE = 0,
   /* A-order relabelling (vertex_ordering/A-order/A-order.cpp:62-247). */
-  ATC_ORDER_AORDER = 1
+  ATC_ORDER_AORDER = 1,
+  /* descending degree-orientation out-degree, larger id first on a tie: the "good"
+     relabelling of vertex_ordering/A-order/relabel-naive.cpp:67-74 (ATC_RELABEL_DEGREE_DESC) */
+  ATC_ORDER_DEGREE_DESC = 2,
+  /* A-order-v2's 40-column mix of that list (A-order-v2.cpp:102-146, ATC_RELABEL_AORDER_V2) */
+  ATC_ORDER_AORDER_V2 = 3
 } atc_order;
+
+/* Rank relabellings of vertex_ordering/A-order (atc_relabel). */
+typedef enum atc_relabel_kind {
+  /* rt = out-degree after the degree orientation (src = lower degree, larger id on a
+     tie; A-order-v2.cpp:38-50); new id = position in the (rt, id)-descending list of all
+     ids 0..max (relabel-naive.cpp:67-74,165-172 writes it as "degreeOrder";
+     relabel-random.cpp:67-74 as "good"). */
+  ATC_RELABEL_DEGREE_DESC = 0,
+  /* the same list dealt into 40 columns (A-order-v2.cpp:102-146, output file "naive") */
+  ATC_RELABEL_AORDER_V2 = 1,
+  /* rt = out-degree of the pairs as given ("good" of relabel4lpOut.cpp:27-54, whose
+     input is already oriented) */
+  ATC_RELABEL_OUTDEG_DESC = 2
+} atc_relabel_kind;
 
 typedef enum atc_kernel {
   ATC_KERNEL_AUTO = 0,    /* library default for the graph */
@@ -211,6 +230,13 @@ atc_status atc_kcore_direction(const uint64_t* edges, uint64_t n_edges, uint64_t
 atc_status atc_adirection_par(const uint64_t* edges, uint64_t n_edges, int compat, uint64_t* oriented_out,
                               uint32_t* flags_out, uint32_t* minor_out, uint64_t* n_vertices, int32_t* iterations,
                               atc_stream s);
+/* A-order-v2 / relabel-naive / relabel4lpOut on raw pairs, repeats included: `lookup`
+   (max id + 1 ints, at least 1) = new id of every id; `normal` (n_pairs pairs, nullable)
+   = the degree-oriented pairs (the input as given for OUTDEG_DESC); `relabeled`
+   (nullable) = lookup applied to `normal` (the "naive" / "good" output file).  The
+   programs' shuffled "bad" outputs depend on the C library's rand() and are not built. */
+atc_status atc_relabel(const int32_t* pairs, uint64_t n_pairs, atc_relabel_kind kind, int32_t* lookup,
+                       int32_t* normal, int32_t* relabeled, atc_stream s);
 /* A-order <file> (vertex_ordering/A-order/A-order.cpp:62-247) on the raw pairs,
    repeats included: `lookup` (max id + 1 ints) = new id of every id (badLookUpTable);
    `normal` / `reordered` (n_pairs pairs each, nullable) = the two output files.

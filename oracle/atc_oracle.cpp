@@ -782,6 +782,47 @@ void orc_adirection_par(const uint64_t* edges, uint64_t ne, int compat, uint64_t
   if (iterations) *iterations = (int32_t)it;
 }
 
+// Rank relabellings of vertex_ordering/A-order: kind 0 = "good" of relabel-naive.cpp /
+// relabel-random.cpp (:29-74), kind 1 = "naive" of A-order-v2.cpp (:29-160), kind 2 =
+// "good" of relabel4lpOut.cpp (:27-54, out-degree as given).  Degrees count repeats;
+// the degree orientation flips a pair when src has the larger degree or equal degree and
+// the smaller id.  lookup: maxNodeId + 1 ints (maxNodeId starts at 0); normal: np pairs.
+void orc_relabel(const int32_t* pairs, uint64_t np, int kind, int32_t* lookup, int32_t* normal) {
+  int max_node = 0;
+  for (uint64_t i = 0; i < 2 * np; ++i) max_node = std::max(max_node, pairs[i]);
+  const int n = max_node + 1;
+  std::vector<int> degree(n, 0), rt(n, 0);
+  for (uint64_t i = 0; i < np; ++i) {
+    degree[pairs[2 * i]]++;
+    if (kind != 2) degree[pairs[2 * i + 1]]++;
+  }
+  for (uint64_t i = 0; i < np; ++i) {
+    int src = pairs[2 * i], dst = pairs[2 * i + 1];
+    if (kind != 2 && (degree[src] > degree[dst] || (degree[src] == degree[dst] && src < dst))) std::swap(src, dst);
+    normal[2 * i] = src;
+    normal[2 * i + 1] = dst;
+    rt[src]++;
+  }
+  if (kind == 2) rt = degree;
+  int max_rt = 0;
+  for (int v = 0; v < n; ++v) max_rt = std::max(max_rt, rt[v]);
+  std::vector<std::vector<int>> bucket(max_rt + 1);
+  for (int v = 0; v < n; ++v) bucket[rt[v]].push_back(v);
+  std::vector<int> order;  // ascending (rt, id)
+  for (int r = 0; r <= max_rt; ++r) order.insert(order.end(), bucket[r].begin(), bucket[r].end());
+  if (kind != 1) {
+    for (int i = 0; i < n; ++i) lookup[order[i]] = n - 1 - i;
+    return;
+  }
+  std::reverse(order.begin(), order.end());
+  const int mix = 40, chunk = n / mix;
+  std::vector<int> distri(n, 0);
+  for (int i = 0; i < mix; ++i)
+    for (int j = 0; j < chunk; ++j) distri[i + j * mix] = order[i * chunk + j];
+  for (int i = n - n % mix; i < n; ++i) distri[i] = order[i];
+  for (int i = 0; i < n; ++i) lookup[distri[i]] = i;
+}
+
 // Masked-MSE loss and gradients of the selector MLP in double precision: the checker for
 // the library's FP32 training kernels.  Same parameter layout (W1[I][H] b1 W2[H][H] b2
 // W3[H][O] b3), ReLU hidden layers, inputs standardised with (mean, std) first.

@@ -47,6 +47,7 @@ def lib():
         L.orc_mlp_grad.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P,
                                    C.POINTER(C.c_double)]
         L.orc_core_numbers.argtypes = [_P, C.c_uint64, _P]
+        L.orc_relabel.argtypes = [_P, C.c_uint64, C.c_int, _P, _P]
         L.orc_adirection_par.argtypes = [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]
         L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
@@ -169,6 +170,17 @@ def core_numbers(pairs):
     out = np.empty(max(n, 1), dtype=np.int32)
     lib().orc_core_numbers(_ptr(p), p.shape[0], _ptr(out))
     return out[:n]
+
+
+def relabel(pairs, kind):
+    """(lookup, normal, relabeled) of A-order-v2 / relabel-naive / relabel4lpOut."""
+    p = _pairs(pairs)
+    n = int(p.max()) + 1 if p.size else 1
+    lookup = np.empty(n, dtype=np.int32)
+    normal = np.empty((max(p.shape[0], 1), 2), dtype=np.int32)
+    lib().orc_relabel(_ptr(p), p.shape[0], int(kind), _ptr(lookup), _ptr(normal))
+    normal = normal[: p.shape[0]]
+    return lookup, normal, lookup[normal] if normal.size else normal.copy()
 
 
 def adirection_par(edges_u64, compat=False):

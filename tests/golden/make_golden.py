@@ -9,6 +9,9 @@ case the script records what the reference programs output:
   adirection   A-direction-seri E.bin        -> lpBasedGraph.bin
   aorder       A-order lpBasedGraph.bin      -> lookup-free outputs normal / reordered
   aorder_raw   A-order E.bin                 -> normal / reordered on the raw input
+  aorder_v2    A-order-v2 lpBasedGraph.bin   -> naive (the 40-column mix, relabelled)
+  relabel_good relabel-naive lpBasedGraph.bin -> degreeOrder (descending runtime degree)
+  relabel4lp   relabel4lpOut lpBasedGraph   -> good (descending out-degree as given; text input)
   costfunc     costFuncCal lpBasedGraph.bin k -> three printed floats, k = 1, 2
   verification verification lpBasedGraph    -> two printed floats (text input)
   triangles    OrgTriangleCount on E symmetrised (x86 only; int result, small graphs)
@@ -104,6 +107,17 @@ def case(name, pairs):
             assert r.returncode == 0, r.stdout
             out[key] = {"normal": record(read_pairs(os.path.join(d, "normal"))),
                         "reordered": record(read_pairs(os.path.join(d, "reordered")))}
+
+        lpb = os.path.join(d, "lpBasedGraph.bin")
+        r = run([os.path.join(REF, "A-order-v2"), lpb], d)
+        assert r.returncode == 0, r.stdout
+        out["aorder_v2"] = record(read_pairs(os.path.join(d, "naive")))
+        r = run([os.path.join(REF, "relabel-naive"), lpb], d)
+        assert r.returncode == 0, r.stdout
+        out["relabel_good"] = record(read_pairs(os.path.join(d, "degreeOrder")))
+        r = run([os.path.join(REF, "relabel4lpOut"), os.path.join(d, "lpBasedGraph")], d)
+        assert r.returncode == 0, r.stdout
+        out["relabel4lp"] = record(read_pairs(os.path.join(d, "good")))
 
         cf = {}
         for k in (1, 2):

@@ -67,6 +67,32 @@ def test_aorder_matches_reference(golden, name, which):
 
 
 @pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("which,kind", [("aorder_v2", atc.Relabel.AORDER_V2), ("relabel_good", atc.Relabel.DEGREE_DESC),
+                                        ("relabel4lp", atc.Relabel.OUTDEG_DESC)])
+def test_relabel_matches_reference(golden, name, which, kind):
+    c = golden["cases"][name]
+    src = oracle.adirection(golden_input(c))
+    lookup, normal, rel = atc.relabel(src, kind)
+    assert rel.shape[0] == c[which]["count"] and sha(rel) == c[which]["sha256"]
+    olookup, onormal, _ = oracle.relabel(src, kind)
+    assert np.array_equal(lookup, olookup) and np.array_equal(normal, onormal)
+
+
+@pytest.mark.parametrize("order", [atc.Order.DEGREE_DESC, atc.Order.AORDER_V2])
+def test_relabel_orders_in_pretc(order):
+    g = atc.rmat_graph(13, 16, 6)
+    want = oracle.tc_count(g)
+    kind = atc.Relabel.DEGREE_DESC if order == atc.Order.DEGREE_DESC else atc.Relabel.AORDER_V2
+    once = atc.simplify(g, symmetric=False)
+    olookup, _, _ = oracle.relabel(once, kind)
+    for d in DIRS:
+        csr = atc.pretc(g, d, order, want_perm=True)
+        assert np.array_equal(csr.perm[: olookup.size], olookup)
+        for k in KERNELS:
+            assert atc.tc(csr, k)[0] == want, (order.name, d.name, k.name)
+
+
+@pytest.mark.parametrize("name", CASES)
 def test_costs_match_reference(golden, name):
     c = golden["cases"][name]
     lp = oracle.adirection(golden_input(c))
@@ -293,6 +319,10 @@ def test_cli_dropins(tmp_path):
     assert r.returncode == 0, r.stderr
     _, normal, reordered = oracle.aorder(lp)
     assert np.array_equal(np.fromfile(tmp_path / "reordered", dtype=np.int32).reshape(-1, 2), reordered)
+    r = subprocess.run([os.path.join(bindir, "a_order_v2"), str(tmp_path / "lpBasedGraph.bin")], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(np.fromfile(tmp_path / "naive", dtype=np.int32).reshape(-1, 2), oracle.relabel(lp, 1)[2])
     r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout

@@ -62,6 +62,16 @@ def test_aorder(golden, name, which):
 
 
 @pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("which,kind", [("aorder_v2", 1), ("relabel_good", 0), ("relabel4lp", 2)])
+def test_relabel(golden, name, which, kind):
+    """A-order-v2 "naive", relabel-naive "degreeOrder", relabel4lpOut "good" on lpBasedGraph."""
+    c = golden["cases"][name]
+    lookup, normal, rel = oracle.relabel(oracle.adirection(golden_input(c)), kind)
+    check_pairs(rel, c[which])
+    assert np.array_equal(np.sort(lookup), np.arange(lookup.size))
+
+
+@pytest.mark.parametrize("name", CASES)
 def test_costfunc(golden, name):
     c = golden["cases"][name]
     lp = oracle.adirection(golden_input(c))
