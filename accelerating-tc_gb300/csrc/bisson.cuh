@@ -348,14 +348,13 @@ __device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t 
 // Streams the lists of the partners plist[base, base+32) for every batch start `base`
 // that `next_batch()` hands out (until it reaches i1) through `probe`, and returns the
 // hits.  Lists of 32 or more elements are walked by the whole warp, one list at a
-// time, four coalesced loads in flight per lane.  Shorter lists are spread over the
-// lanes by a warp prefix sum of their lengths, so they do not leave lanes idle; each
-// lane follows the list it is in with a cursor kept in registers.  sx/sp: the warp's
-// 32-entry shared scratch.
+// time, four coalesced loads in flight per lane.  Shorter lists are laid end to end by
+// a warp prefix sum of their lengths and dealt 32 elements per round; each lane finds
+// the list holding its element by a 5-step binary search over the lanes' start offsets,
+// done with shuffles so that every lane runs the same steps.
 template <class NextBatch, class Probe>
 __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
-                                                    int lane, int* sx, int64_t* sp, NextBatch next_batch,
-                                                    Probe probe) {
+                                                    int lane, NextBatch next_batch, Probe probe) {
   unsigned cnt = 0;
   for (int64_t base = next_batch(); base < i1; base = next_batch()) {
     int64_t i = base + lane;
@@ -387,24 +386,20 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
       if (lane >= o) incl += y;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) continue;
-    sx[lane] = incl - slen;
-    sp[lane] = pb;
-    __syncwarp();
-    // k = the last lane whose start is <= t: always a lane with a non-empty short list
-    int k = 0;
-    int kx = sx[0], knext = sx[1];
-    int64_t kp = sp[0];
-    for (int t = lane; t < total; t += 32) {
-      while (k < 31 && knext <= t) {
-        ++k;
-        kx = knext;
-        kp = sp[k];
-        knext = k < 31 ? sx[k + 1] : total;
+    const int start = incl - slen;
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      // k = the last lane whose start is <= t: a lane with a non-empty short list
+      int k = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int sk = __shfl_sync(0xffffffffu, start, k + step);
+        if (sk <= t) k += step;
       }
-      cnt += probe(__ldg(g.cols + kp + (t - kx)));
+      const int64_t kp = __shfl_sync(0xffffffffu, pb, k);
+      const int kx = __shfl_sync(0xffffffffu, start, k);
+      if (t < total) cnt += probe(__ldg(g.cols + kp + (t - kx)));
     }
-    __syncwarp();
   }
   return cnt;
 }
@@ -416,8 +411,6 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
                                                                   const int* nitems_dev, int* next, GraphTags tags,
                                                                   unsigned long long* out) {
   __shared__ int32_t tab[kBgWarps][kWarpSlots];
-  __shared__ int sx[kBgWarps][32];
-  __shared__ int64_t sp[kBgWarps][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
   __syncwarp();
@@ -438,7 +431,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
     if (gi.mode == 0) {
       for (int j = lane; j < dh; j += 32) T[j] = __ldg(g.cols + hb + j);
       __syncwarp();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+      cnt = stream_partners(g, plist, gi.e, lane, nb, [&](int32_t x) -> unsigned {
         int lo = 0, n = dh;
         while (n > 1) {  // branch-free lower bound over the sorted copy
           int half = n >> 1;
@@ -455,7 +448,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
       const uint32_t mask = cap - 1;
       for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
+      cnt = stream_partners(g, plist, gi.e, lane, nb,
                             [&](int32_t x) -> unsigned { return hash_has(T, mask, x); });
       __syncwarp();
       for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
@@ -473,8 +466,6 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
                                                                    const int* nitems_dev, int* next, uint32_t tab_words,
                                                                    GraphTags tags, unsigned long long* out) {
   extern __shared__ int32_t tab[];  // tab_words
-  __shared__ int sx[kBgWarps][32];
-  __shared__ int64_t sp[kBgWarps][32];
   __shared__ int cur_item;
   __shared__ unsigned long long bnext;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -506,7 +497,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       const uint32_t mask = cap - 1;
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
       __syncthreads();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb,
+      cnt = stream_partners(g, plist, gi.e, lane, nb,
                             [&](int32_t x) -> unsigned { return hash_has(tab, mask, x); });
       __syncthreads();
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
@@ -521,7 +512,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
         atomicOr(&bits[x >> 5], 1u << (x & 31));
       }
       __syncthreads();
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+      cnt = stream_partners(g, plist, gi.e, lane, nb, [&](int32_t x) -> unsigned {
         if (x < lo || x > hi) return 0u;
         x -= lo;
         return (bits[x >> 5] >> (x & 31)) & 1u;
@@ -529,7 +520,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       __syncthreads();
       for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0xffffffffu;  // back to empty slots (-1)
     } else {
-      cnt = stream_partners(g, plist, gi.e, lane, sx[w], sp[w], nb, [&](int32_t x) -> unsigned {
+      cnt = stream_partners(g, plist, gi.e, lane, nb, [&](int32_t x) -> unsigned {
         int64_t lo = 0, hi = dh;
         while (lo < hi) {
           int64_t mid = (lo + hi) >> 1;
