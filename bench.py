@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--select-train", type=int, default=2048, help="training graphs of the selector")
     ap.add_argument("--select-eval", type=int, default=512, help="held-out graphs of the selector")
     ap.add_argument("--select-out", default="", help="write features and timings (.npz) here")
+    ap.add_argument("--select-space", choices=("config", "extended"), default="config",
+                    help="triples timed: the config's 24, or also k-core / approximate A-direction and the "
+                         "rank relabellings (60)")
     ap.add_argument("--batch-plain-kernels", default="bisson",
                     help="fixed kernels timed in the per-graph loop (the first is the reference line)")
     ap.add_argument("--batch-select", action="store_true",
@@ -535,6 +538,17 @@ SEL_ORDERS = ("NONE", "AORDER")
 SEL_KERNELS = ("HU", "BISSON", "FOX", "TRICORE")
 
 
+def set_select_space(name):
+    """The config's direction x ordering x kernel space, or the extended one."""
+    global SEL_DIRS, SEL_ORDERS
+    if name == "extended":
+        SEL_DIRS = ("ID", "DEGREE", "ADIRECTION", "KCORE", "ADIRECTION_PAR")
+        SEL_ORDERS = ("NONE", "AORDER", "DEGREE_DESC")
+    else:
+        SEL_DIRS = ("ID", "DEGREE", "ADIRECTION")
+        SEL_ORDERS = ("NONE", "AORDER")
+
+
 def triple_name(i):
     d, rest = divmod(i, len(SEL_ORDERS) * len(SEL_KERNELS))
     o, k = divmod(rest, len(SEL_KERNELS))
@@ -636,6 +650,7 @@ def run_select(a):
     torch.cuda.set_device(0)
     atc.init(0)
     sp = torch.cuda.current_stream().cuda_stream
+    set_select_space(a.select_space)
     specs = select_graphs(a.select_train + a.select_eval, a.seed)
     measure_graph(("rmat", 10, 8, None), 999, sp)  # warm-up: module load, pools
     feats, times, costs = [], [], []
@@ -652,7 +667,8 @@ def run_select(a):
                             triples=np.array([triple_name(i) for i in range(times.shape[1])]))
     ntr = a.select_train
     result = train_and_evaluate(feats, times, costs, ntr, seed=a.seed)
-    result.update({"mode": "select", "graphs_train": ntr, "graphs_eval": len(specs) - ntr,
+    result.update({"mode": "select", "space": a.select_space, "triples": int(times.shape[1]),
+                   "graphs_train": ntr, "graphs_eval": len(specs) - ntr,
                    "measure_s": gen_s, "data": "seeded Chung-Lu (n log-uniform 1e3..2e5) and R-MAT (scale 10..17)"})
     print(json.dumps(result), flush=True)
 
