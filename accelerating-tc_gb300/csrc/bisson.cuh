@@ -308,7 +308,13 @@ __device__ __forceinline__ void add_item_to_graph(const GraphTags& t, int64_t h,
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(&t.counts[graph_of(t, h)], c);
 }
 
-__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) { return ((uint32_t)x * 0x9E3779B1u) & mask; }
+// Fibonacci hashing: the top log2(cap) bits of x * 2^32/phi.  The low bits of that
+// product depend only on the low bits of x, and neighbour ids after relabelling share
+// low-bit patterns, which clustered the linear-probing tables (22 % of the hits at R-MAT
+// scale 24 were not in their home slot); the top bits mix all of x.
+__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) {
+  return ((uint32_t)x * 0x9E3779B1u) >> (32 - __popc(mask));
+}
 
 // Linear-probing lookup; the table always has empty slots, and `cap` bounds the walk.
 // Most lookups end at the first slot (load factor <= 1/4).
