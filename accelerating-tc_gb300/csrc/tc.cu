@@ -382,7 +382,14 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
 
 static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                              int* launches) {
-  int cutover = t && t->bisson_cutover > 0 ? std::min(t->bisson_cutover, kWarpMax) : 32;
+  // item shape: defaults, overridden field by field by the tuning (chunks >= 32 partners)
+  ItemShape sh = default_shape(32);
+  if (t) {
+    if (t->bisson_cutover > 0) sh.cutover = std::min(t->bisson_cutover, kWarpMax);
+    if (t->bisson_warp_max > 0) sh.warp_max = std::min(t->bisson_warp_max, kWarpMax);
+    if (t->bisson_warp_chunk > 0) sh.warp_chunk = std::max(t->bisson_warp_chunk, 32);
+    if (t->bisson_block_chunk > 0) sh.block_chunk = std::max(t->bisson_block_chunk, 32);
+  }
   DevBuf<int32_t> cnt, cur, plist;
   DevBuf<int64_t> gstart;
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
@@ -403,12 +410,11 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   group_scatter_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, gstart.p, cur.p, plist.p);
   ATC_CK(cudaGetLastError());
   // items: at most one per group plus one per chunk boundary
-  int64_t max_items = g.n + total / kWarpChunk + 1;
+  int64_t max_items = g.n + total / std::min(sh.warp_chunk, sh.block_chunk) + 1;
   DevBuf<GroupItem> witems, bitems;
   ATC_TRY(witems.alloc(max_items, s));
   ATC_TRY(bitems.alloc(max_items, s));
-  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p,
-                                                        default_shape(cutover));
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p, sh);
   ATC_CK(cudaGetLastError());
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
