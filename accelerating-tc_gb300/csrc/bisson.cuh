@@ -316,22 +316,6 @@ __device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) {
   return ((uint32_t)x * 0x9E3779B1u) >> (32 - __popc(mask));
 }
 
-// Linear-probing lookup; the table always has empty slots, and `cap` bounds the walk.
-// Most lookups end at the first slot (load factor <= 1/4).
-__device__ __forceinline__ unsigned hash_has(const int32_t* tab, uint32_t mask, int32_t x) {
-  uint32_t s = hash_slot(x, mask);
-  int32_t y = tab[s];
-  if (y == x) return 1u;
-  if (y == -1) return 0u;
-  for (uint32_t n = 0; n < mask; ++n) {
-    s = (s + 1) & mask;
-    y = tab[s];
-    if (y == x) return 1u;
-    if (y == -1) return 0u;
-  }
-  return 0u;
-}
-
 // Inserts x (not yet present); concurrent inserters use atomicCAS.
 __device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t x) {
   uint32_t s = hash_slot(x, mask);
@@ -351,16 +335,101 @@ __device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t 
   }
 }
 
+// Probers: what stream_partners does with each element.  probe(x, valid) is called by
+// all 32 lanes together (valid = false on lanes without an element) and returns this
+// lane's hits; finish() returns hits still pending when an item ends.
+template <class F>
+struct DirectProber {  // a branch-light test per element (sorted search, bitmap)
+  F f;
+  __device__ __forceinline__ unsigned probe(int32_t x, bool valid) { return valid ? f(x) : 0u; }
+  __device__ __forceinline__ unsigned finish() { return 0u; }
+};
+template <class F>
+__device__ __forceinline__ DirectProber<F> direct_prober(F f) { return DirectProber<F>{f}; }
+
+// Linear-probing lookups with the chains taken out of the warp's lockstep.  Every key
+// reads its home slot; a key that is neither there nor stopped by an empty slot is
+// queued (key, next slot, steps) in the warp's 64-entry shared queue, and whenever 32
+// are queued the warp advances all of them one slot together.  A lookup loop per lane
+// would make the whole warp wait for its longest chain: at load 1/4 nearly every warp
+// has a lane whose home slot holds another key.
+struct HashQueueProber {
+  const int32_t* tab;
+  uint32_t mask;
+  int32_t* qx;   // 64 keys
+  uint32_t* qs;  // 64 (next slot | steps << 16)
+  int n;         // queued entries, the same on every lane
+  int lane;
+  __device__ __forceinline__ void push(bool pend, int32_t x, uint32_t next) {
+    const unsigned pm = __ballot_sync(0xffffffffu, pend);
+    if (pm) {
+      if (pend) {
+        const int pos = n + __popc(pm & ((1u << lane) - 1));
+        qx[pos] = x;
+        qs[pos] = next;
+      }
+      n += __popc(pm);
+    }
+  }
+  // one slot further for up to 32 queued keys (the newest); unresolved ones go back
+  __device__ __forceinline__ unsigned step() {
+    const int take = n < 32 ? n : 32;
+    const int base = n - take;
+    __syncwarp();
+    const bool v = lane < take;
+    int32_t x = 0;
+    uint32_t q = 0;
+    if (v) {
+      x = qx[base + lane];
+      q = qs[base + lane];
+    }
+    __syncwarp();
+    n = base;
+    unsigned hit = 0;
+    bool pend = false;
+    const uint32_t slot = q & 0xffffu, steps = q >> 16;
+    if (v) {
+      const int32_t y = tab[slot];
+      hit = y == x;
+      // a key that walked the whole table is absent (cannot happen below load 1)
+      pend = y != x && y != -1 && steps < mask;
+    }
+    push(pend, x, ((slot + 1) & mask) | ((steps + 1) << 16));
+    return hit;
+  }
+  __device__ __forceinline__ unsigned probe(int32_t x, bool valid) {
+    unsigned hit = 0;
+    bool pend = false;
+    uint32_t s = 0;
+    if (valid) {
+      s = hash_slot(x, mask);
+      const int32_t y = tab[s];
+      hit = y == x;
+      pend = y != x && y != -1;
+    }
+    push(pend, x, ((s + 1) & mask) | (1u << 16));
+    while (n >= 32) hit += step();
+    return hit;
+  }
+  __device__ __forceinline__ unsigned finish() {
+    unsigned hit = 0;
+    while (n > 0) hit += step();
+    __syncwarp();
+    return hit;
+  }
+};
+
 // Streams the lists of the partners plist[base, base+32) for every batch start `base`
-// that `next_batch()` hands out (until it reaches i1) through `probe`, and returns the
-// hits.  Lists of 32 or more elements are walked by the whole warp, one list at a
+// that `next_batch()` hands out (until it reaches i1) through the prober, and returns
+// the hits.  Lists of 32 or more elements are walked by the whole warp, one list at a
 // time, four coalesced loads in flight per lane.  Shorter lists are laid end to end by
 // a warp prefix sum of their lengths and dealt 32 elements per round; each lane finds
 // the list holding its element by a 5-step binary search over the lanes' start offsets,
-// done with shuffles so that every lane runs the same steps.
-template <class NextBatch, class Probe>
+// done with shuffles so that every lane runs the same steps.  Every probe call is made
+// by all 32 lanes together.
+template <class NextBatch, class Prober>
 __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
-                                                    int lane, NextBatch next_batch, Probe probe) {
+                                                    int lane, NextBatch next_batch, Prober& pr) {
   unsigned cnt = 0;
   for (int64_t base = next_batch(); base < i1; base = next_batch()) {
     int64_t i = base + lane;
@@ -377,12 +446,19 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
       longm &= longm - 1;
       const int32_t* P = g.cols + __shfl_sync(0xffffffffu, pb, k);
       const int ln = __shfl_sync(0xffffffffu, len, k);
-      int j = lane;
-      for (; j + 96 < ln; j += 128) {
-        int32_t x0 = __ldg(P + j), x1 = __ldg(P + j + 32), x2 = __ldg(P + j + 64), x3 = __ldg(P + j + 96);
-        cnt += probe(x0) + probe(x1) + probe(x2) + probe(x3);
+      int j0 = 0;
+      for (; j0 + 128 <= ln; j0 += 128) {
+        const int32_t x0 = __ldg(P + j0 + lane), x1 = __ldg(P + j0 + 32 + lane), x2 = __ldg(P + j0 + 64 + lane),
+                      x3 = __ldg(P + j0 + 96 + lane);
+        cnt += pr.probe(x0, true);
+        cnt += pr.probe(x1, true);
+        cnt += pr.probe(x2, true);
+        cnt += pr.probe(x3, true);
       }
-      for (; j < ln; j += 32) cnt += probe(__ldg(P + j));
+      for (; j0 < ln; j0 += 32) {
+        const bool v = j0 + lane < ln;
+        cnt += pr.probe(v ? __ldg(P + j0 + lane) : 0, v);
+      }
     }
     const int slen = len < 32 ? len : 0;
     int incl = slen;
@@ -404,9 +480,11 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
       }
       const int64_t kp = __shfl_sync(0xffffffffu, pb, k);
       const int kx = __shfl_sync(0xffffffffu, start, k);
-      if (t < total) cnt += probe(__ldg(g.cols + kp + (t - kx)));
+      const bool v = t < total;
+      cnt += pr.probe(v ? __ldg(g.cols + kp + (t - kx)) : 0, v);
     }
   }
+  cnt += pr.finish();
   return cnt;
 }
 
@@ -417,6 +495,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
                                                                   const int* nitems_dev, int* next, GraphTags tags,
                                                                   unsigned long long* out) {
   __shared__ int32_t tab[kBgWarps][kWarpSlots];
+  __shared__ int32_t qx[kBgWarps][64];
+  __shared__ uint32_t qs[kBgWarps][64];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
   __syncwarp();
@@ -437,7 +517,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
     if (gi.mode == 0) {
       for (int j = lane; j < dh; j += 32) T[j] = __ldg(g.cols + hb + j);
       __syncwarp();
-      cnt = stream_partners(g, plist, gi.e, lane, nb, [&](int32_t x) -> unsigned {
+      auto pr = direct_prober([&](int32_t x) -> unsigned {
         int lo = 0, n = dh;
         while (n > 1) {  // branch-free lower bound over the sorted copy
           int half = n >> 1;
@@ -446,6 +526,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
         }
         return T[lo] == x;
       });
+      cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncwarp();
       for (int j = lane; j < dh; j += 32) T[j] = -1;
     } else {
@@ -454,8 +535,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
       const uint32_t mask = cap - 1;
       for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();
-      cnt = stream_partners(g, plist, gi.e, lane, nb,
-                            [&](int32_t x) -> unsigned { return hash_has(T, mask, x); });
+      HashQueueProber pr{T, mask, qx[w], qs[w], 0, lane};
+      cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncwarp();
       for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
     }
@@ -472,6 +553,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
                                                                    const int* nitems_dev, int* next, uint32_t tab_words,
                                                                    GraphTags tags, unsigned long long* out) {
   extern __shared__ int32_t tab[];  // tab_words
+  __shared__ int32_t qx[kBgWarps][64];
+  __shared__ uint32_t qs[kBgWarps][64];
   __shared__ int cur_item;
   __shared__ unsigned long long bnext;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -503,8 +586,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       const uint32_t mask = cap - 1;
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
       __syncthreads();
-      cnt = stream_partners(g, plist, gi.e, lane, nb,
-                            [&](int32_t x) -> unsigned { return hash_has(tab, mask, x); });
+      HashQueueProber pr{tab, mask, qx[w], qs[w], 0, lane};
+      cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncthreads();
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
     } else if (gi.mode == 1) {
@@ -518,15 +601,16 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
         atomicOr(&bits[x >> 5], 1u << (x & 31));
       }
       __syncthreads();
-      cnt = stream_partners(g, plist, gi.e, lane, nb, [&](int32_t x) -> unsigned {
+      auto pr = direct_prober([&](int32_t x) -> unsigned {
         if (x < lo || x > hi) return 0u;
         x -= lo;
         return (bits[x >> 5] >> (x & 31)) & 1u;
       });
+      cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncthreads();
       for (int j = threadIdx.x; j < words; j += blockDim.x) bits[j] = 0xffffffffu;  // back to empty slots (-1)
     } else {
-      cnt = stream_partners(g, plist, gi.e, lane, nb, [&](int32_t x) -> unsigned {
+      auto pr = direct_prober([&](int32_t x) -> unsigned {
         int64_t lo = 0, hi = dh;
         while (lo < hi) {
           int64_t mid = (lo + hi) >> 1;
@@ -534,6 +618,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
         }
         return lo < dh && Nh[lo] == x;
       });
+      cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
     }
     __syncthreads();
     if (tags.counts) add_item_to_graph(tags, gi.h, cnt);
