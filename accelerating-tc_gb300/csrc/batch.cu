@@ -219,8 +219,11 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   ATC_CK(cudaStreamSynchronize(s));
   if (!b->cap_stream) ATC_CK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
 
-  const BlockSmem bs = block_smem(b->max_outdeg);
-  const size_t smem = bs.bytes();
+  uint32_t words = 64;
+  const uint32_t want = 4u * (uint32_t)std::min(std::max(b->max_outdeg, 1), kHashMax);
+  while (words < want) words <<= 1;
+  if (b->max_outdeg > kHashMax) words = kTabWords;
+  size_t smem = sizeof(int32_t) * words;
   ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<CompactItems>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int grid_block = sm_count() * blocks_per_sm((const void*)bisson_block_kernel<CompactItems>, kBgWarps * 32, smem);
@@ -244,7 +247,7 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist);
   group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->gstart, b->items, cap_items, b->counters, sh);
   bisson_block_kernel<CompactItems><<<grid_block, kBgWarps * 32, smem, c>>>(g, b->plist, bitems, 0, b->counters + 1,
-                                                                            b->counters + 5, bs.tab_words, bs.filt_words, tags, b->gcounts);
+                                                                            b->counters + 5, words, tags, b->gcounts);
   bisson_warp_kernel<CompactItems><<<grid_warp, kBgWarps * 32, 0, c>>>(g, b->plist, witems, 0, b->counters,
                                                                        b->counters + 4, tags, b->gcounts);
   cudaError_t launch_err = cudaGetLastError();

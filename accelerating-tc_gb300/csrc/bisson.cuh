@@ -48,23 +48,6 @@ constexpr int kWarpChunk = 512;     // partners per warp item
 constexpr int kBlockChunk = 2048;   // partners per block item
 constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
 constexpr int kHashMax = kTabWords / 4;
-constexpr int kFilterBitsPerKey = 16;  // block tables: miss filter of >= 16 bits per key
-
-// Dynamic shared memory of the block kernel: the table / bitmap words, then the miss
-// filter of the hashed lists.  max_hashed = longest list the items hash (kHashMax when
-// some item needs the full bitmap or search).
-struct BlockSmem {
-  uint32_t tab_words, filt_words;
-  size_t bytes() const { return sizeof(int32_t) * ((size_t)tab_words + filt_words); }
-};
-inline BlockSmem block_smem(int max_hashed) {
-  const uint32_t d = (uint32_t)(max_hashed < 1 ? 1 : (max_hashed > kHashMax ? kHashMax : max_hashed));
-  uint32_t words = 64;
-  while (words < 4u * d) words <<= 1;
-  uint32_t fw = 32;
-  while (fw * 32u < (uint32_t)kFilterBitsPerKey * d) fw <<= 1;
-  return BlockSmem{words, fw};
-}
 
 struct GroupItem {
   int32_t h;
@@ -333,11 +316,6 @@ __device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) {
   return ((uint32_t)x * 0x9E3779B1u) >> (32 - __popc(mask));
 }
 
-// Bit of x in a miss filter of (mask + 1) bits: an independent multiplier's top bits.
-__device__ __forceinline__ uint32_t filter_bit(int32_t x, uint32_t mask) {
-  return ((uint32_t)x * 0x85EBCA77u) >> (32 - __popc(mask));
-}
-
 // Inserts x (not yet present); concurrent inserters use atomicCAS.
 __device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t x) {
   uint32_t s = hash_slot(x, mask);
@@ -370,16 +348,14 @@ template <class F>
 __device__ __forceinline__ DirectProber<F> direct_prober(F f) { return DirectProber<F>{f}; }
 
 // Linear-probing lookups with the chains taken out of the warp's lockstep.  Every key
-// reads its home slot; a key that is neither there nor stopped by an empty slot (nor,
-// with a filter, excluded by a clear filter bit) is queued (key, next slot, steps) in the warp's 64-entry shared queue, and whenever 32
+// reads its home slot; a key that is neither there nor stopped by an empty slot is
+// queued (key, next slot, steps) in the warp's 64-entry shared queue, and whenever 32
 // are queued the warp advances all of them one slot together.  A lookup loop per lane
 // would make the whole warp wait for its longest chain: at load 1/4 nearly every warp
 // has a lane whose home slot holds another key.
 struct HashQueueProber {
   const int32_t* tab;
   uint32_t mask;
-  const uint32_t* filt;  // miss filter bits of the table's keys, or null
-  uint32_t fmask;        // filter bits - 1
   int32_t* qx;   // 64 keys
   uint32_t* qs;  // 64 (next slot | steps << 16)
   int n;         // queued entries, the same on every lane
@@ -430,10 +406,6 @@ struct HashQueueProber {
       const int32_t y = tab[s];
       hit = y == x;
       pend = y != x && y != -1;
-      if (filt && pend) {  // home slot taken by another key: a clear filter bit settles the miss
-        const uint32_t b = filter_bit(x, fmask);
-        pend = (filt[b >> 5] >> (b & 31)) & 1u;
-      }
     }
     push(pend, x, ((s + 1) & mask) | (1u << 16));
     while (n >= 32) hit += step();
@@ -563,7 +535,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
       const uint32_t mask = cap - 1;
       for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();
-      HashQueueProber pr{T, mask, nullptr, 0u, qx[w], qs[w], 0, lane};
+      HashQueueProber pr{T, mask, qx[w], qs[w], 0, lane};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncwarp();
       for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
@@ -579,17 +551,14 @@ template <class Items>
 __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                    Items items, int nitems,
                                                                    const int* nitems_dev, int* next, uint32_t tab_words,
-                                                                   uint32_t filt_words, GraphTags tags,
-                                                                   unsigned long long* out) {
-  extern __shared__ int32_t tab[];  // tab_words, then filt_words of miss filter
-  uint32_t* filt = reinterpret_cast<uint32_t*>(tab + tab_words);
+                                                                   GraphTags tags, unsigned long long* out) {
+  extern __shared__ int32_t tab[];  // tab_words
   __shared__ int32_t qx[kBgWarps][64];
   __shared__ uint32_t qs[kBgWarps][64];
   __shared__ int cur_item;
   __shared__ unsigned long long bnext;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t j = threadIdx.x; j < tab_words; j += blockDim.x) tab[j] = -1;
-  for (uint32_t j = threadIdx.x; j < filt_words; j += blockDim.x) filt[j] = 0u;
   unsigned long long total = 0;
   if (nitems_dev) nitems = *nitems_dev;
   for (;;) {
@@ -615,25 +584,12 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       uint32_t cap = 64;
       while (cap < 4u * (uint32_t)dh) cap <<= 1;
       const uint32_t mask = cap - 1;
-      uint32_t fbits = 1024;
-      while (fbits < (uint32_t)kFilterBitsPerKey * (uint32_t)dh && fbits < 32u * filt_words) fbits <<= 1;
-      const bool use_filter = filt_words >= 32 && fbits <= 32u * filt_words;
-      const uint32_t fmask = fbits - 1;
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) {
-        const int32_t x = Nh[j];
-        hash_insert(tab, mask, x);
-        if (use_filter) {
-          const uint32_t b = filter_bit(x, fmask);
-          atomicOr(&filt[b >> 5], 1u << (b & 31));
-        }
-      }
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
       __syncthreads();
-      HashQueueProber pr{tab, mask, use_filter ? filt : nullptr, fmask, qx[w], qs[w], 0, lane};
+      HashQueueProber pr{tab, mask, qx[w], qs[w], 0, lane};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncthreads();
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
-      if (use_filter)
-        for (uint32_t j = threadIdx.x; j < (fbits >> 5); j += blockDim.x) filt[j] = 0u;
     } else if (gi.mode == 1) {
       const int32_t lo = Nh[0], hi = Nh[dh - 1];
       const int words = ((hi - lo) >> 5) + 1;

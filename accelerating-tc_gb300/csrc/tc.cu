@@ -423,13 +423,15 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   if (hc[1]) {
     // block table: enough slots for the longest hashed list at load factor 1/4, or the
     // full bitmap when some list needs it
-    const BlockSmem bs = block_smem(hc[3]);
-    const size_t smem = bs.bytes();
+    uint32_t words = 64;
+    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
+    if (words > (uint32_t)kTabWords) words = kTabWords;
+    size_t smem = sizeof(int32_t) * words;
     ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
     int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems>, kBgWarps * 32, smem);
     int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, FullItems{bitems.p}, hc[1], nullptr, counters.p + 5, bs.tab_words, bs.filt_words,
+    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, FullItems{bitems.p}, hc[1], nullptr, counters.p + 5, words,
                                                           GraphTags{nullptr, 0, nullptr}, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
@@ -589,13 +591,15 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
   ATC_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   if (hc[1]) {
-    const BlockSmem bs = block_smem(hc[3]);
-    const size_t smem = bs.bytes();
+    uint32_t words = 64;
+    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
+    if (words > (uint32_t)kTabWords) words = kTabWords;
+    size_t smem = sizeof(int32_t) * words;
     ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
     int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems>, kBgWarps * 32, smem);
     int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, bs.tab_words, bs.filt_words,
+    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, words,
                                                           GraphTags{nullptr, 0, nullptr}, total_ctr);
     ATC_CK(cudaGetLastError());
   }
