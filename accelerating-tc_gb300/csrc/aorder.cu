@@ -3,13 +3,16 @@
 // GPU part: degrees (repeats counted), degree orientation and runtime degree rt (the
 // out-degree it gives), the histogram of rt, the (rt, id) order of all vertices, and
 // the final lookup table.  Host part: the bucket heap of A-order.cpp:123-181, which is
-// sequential by definition — its result is fixed by the order in which libstdc++'s
-// make_heap / pop_heap / push_heap / sort_heap move elements, so it calls those same
-// functions on the same keys.  The heap only needs each position's rt, which the rt
-// histogram gives, so no vertex list crosses to the host; the bucket contents go back
-// to the device as positions into the (rt, id) order.
+// sequential by definition.  Its result is fixed by which bucket each pop takes (the
+// extreme key; keys are unique) and by the array that the final sort_heap reorders
+// (the buckets in reverse order of filling), so a faster queue with the same pops
+// replaces the heap and std::sort_heap is applied to the same array (bucket_heap).  The
+// heap only needs each position's rt, which the rt histogram gives, so no vertex list
+// crosses to the host; the pops go back to the device, which scatters them into the
+// bucket order of positions in the (rt, id) order.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "internal.cuh"
@@ -34,19 +37,95 @@ float equal_bandwidth_of(int len) {
   return 12 * std::sqrt(bandwidth_of(len)) / std::sqrt((float)len);
 }
 
-struct HeapItem {
-  int id;
-  float sup;   // memory superiority
-  int slot;    // member block of this bucket
-};
-struct ByLess {
-  bool operator()(const HeapItem& a, const HeapItem& b) const { return a.sup < b.sup || (a.sup == b.sup && a.id < b.id); }
-};
-struct ByGreat {
-  bool operator()(const HeapItem& a, const HeapItem& b) const { return a.sup > b.sup || (a.sup == b.sup && a.id > b.id); }
-};
-struct ByIdDesc {
-  bool operator()(const HeapItem& a, const HeapItem& b) const { return a.id > b.id; }
+// Bucket keys of the heap as one integer: the float memory superiority mapped to an
+// order-preserving uint32 (high half), then the bucket id << 6 | its fill count (low
+// half).  Bucket ids are unique, so (superiority, id) decides every comparison exactly as
+// the reference's comparators (A-order.cpp:40-60) do and the fill count only rides along.
+// Superiorities are never NaN; -0 is folded into +0 so that the two compare equal, as
+// floats do.
+inline uint32_t order_bits(float f) {
+  f += 0.0f;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+inline float from_order_bits(uint32_t o) {
+  uint32_t u = (o >> 31) ? (o & 0x7fffffffu) : ~o;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+inline uint64_t bucket_key(float sup, uint32_t id_fill) { return ((uint64_t)order_bits(sup) << 32) | id_fill; }
+
+// The priority queue of the bucket heap.  Keys leave in ascending order (Up) or descending
+// order (!Up).  Between two changes of the runtime degree d every popped bucket goes back
+// with sup + delta(d) for one fixed delta, and float addition is monotone, so the keys put
+// back during one run of equal d arrive already in pop order (keys of equal sup can
+// arrive out of id order; push() moves them into place from the back).  Each run's keys
+// therefore form a sorted sequence: the queue keeps one sequence per run and pops the
+// first of their fronts.  A closed sequence is merged into the one before it when it holds
+// at least half as many keys, which keeps the number of sequences logarithmic.
+template <bool Up>
+struct RunQueue {
+  static bool first(uint64_t x, uint64_t y) { return Up ? x < y : x > y; }
+  std::vector<std::vector<uint64_t>> seq;  // closed runs, each in pop order
+  std::vector<size_t> head;                // next key of each closed run
+  std::vector<uint64_t> open;              // keys put back during the current run
+  size_t open_head = 0;
+
+  void close_run() {
+    if (open_head < open.size()) {
+      seq.emplace_back(open.begin() + open_head, open.end());
+      head.push_back(0);
+    }
+    open.clear();
+    open_head = 0;
+    while (seq.size() >= 2) {
+      const size_t l = seq.size() - 1;
+      const size_t nl = seq[l].size() - head[l], np = seq[l - 1].size() - head[l - 1];
+      if (2 * nl < np) break;
+      std::vector<uint64_t> out(nl + np);
+      const uint64_t* a = seq[l - 1].data() + head[l - 1];
+      const uint64_t* b = seq[l].data() + head[l];
+      size_t i = 0, j = 0, k = 0;
+      while (i < np && j < nl) out[k++] = first(b[j], a[i]) ? b[j++] : a[i++];
+      while (i < np) out[k++] = a[i++];
+      while (j < nl) out[k++] = b[j++];
+      seq.pop_back();
+      head.pop_back();
+      seq.back().swap(out);
+      head.back() = 0;
+    }
+  }
+  uint64_t pop() {  // the queue is not empty
+    int best = -1;
+    uint64_t bk = 0;
+    for (size_t r = 0; r < seq.size(); ++r)
+      if (head[r] < seq[r].size() && (best < 0 || first(seq[r][head[r]], bk))) {
+        best = (int)r;
+        bk = seq[r][head[r]];
+      }
+    if (open_head < open.size() && (best < 0 || first(open[open_head], bk))) return open[open_head++];
+    ++head[best];
+    return bk;
+  }
+  void push(uint64_t k) {
+    open.push_back(k);
+    size_t i = open.size() - 1;
+    while (i > open_head && first(k, open[i - 1])) {
+      open[i] = open[i - 1];
+      --i;
+    }
+    open[i] = k;
+  }
+  std::vector<uint64_t> drain() {  // every key left, in no particular order
+    close_run();
+    std::vector<uint64_t> all;
+    for (size_t r = 0; r < seq.size(); ++r) all.insert(all.end(), seq[r].begin() + head[r], seq[r].end());
+    seq.clear();
+    head.clear();
+    return all;
+  }
 };
 
 __global__ void deg_pairs_kernel(const int2* p, uint64_t ne, int32_t* deg) {
@@ -152,60 +231,97 @@ __global__ void relabel_pairs_kernel(const int2* in, uint64_t ne, const int32_t*
     out[i] = make_int2(lookup[in[i].x], lookup[in[i].y]);
 }
 
-// The bucket heap of A-order.cpp:123-181 over positions of the rt>=2 list.  `cum[r]` =
-// first position of runtime degree r in that list (r >= 2).  Fills `pos` (40*nb ints)
-// with list positions in final bucket order.
-void bucket_heap(const std::vector<int64_t>& hist, int maxrt, int64_t S, int64_t mdp, std::vector<int32_t>& pos) {
-  int64_t nb = S / kBucket;
+// Scatters the pops of the bucket heap into the bucket order: pop t filled slot `fill` of
+// bucket `id` (log[t] = id * 40 + fill) with list position total-1-t (phase 1, the first
+// n1 pops) or t-n1 (phase 2); the bucket's place in the output is rank[id].
+__global__ void bucket_scatter_kernel(const uint32_t* log, const uint32_t* rank, int64_t total, int64_t n1,
+                                      int32_t* bucket_pos) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = log[t];
+    const uint32_t id = v / kBucket, f = v - id * kBucket;
+    bucket_pos[(int64_t)rank[id] * kBucket + f] = (int32_t)(t < n1 ? total - 1 - t : t - n1);
+  }
+}
+
+// The bucket heap of A-order.cpp:123-181 over positions of the rt>=2 list, `hist[r]` =
+// number of vertices of runtime degree r.  Output: log[t] = id * 40 + fill of the bucket
+// that pop t filled, and rank[id] = the bucket's place after the final sort_heap.
+//
+// The reference's result depends on two things only.  (1) Which bucket each pop takes:
+// keys are unique, so that is the extreme key, whatever the heap's internal layout.
+// (2) The array that sort_heap(idSort) (:181) reorders: every pop fills one slot and the
+// two phases make exactly 40 * nb pops, so at the end every bucket is full and has left
+// the heap range; pop_heap left each one at the back of the shrinking range when it
+// filled, so the array holds the buckets in reverse order of filling.  The queue below
+// reproduces (1), and std::sort_heap with the reference's comparator is applied to the
+// array of (2).
+void bucket_heap(const std::vector<int64_t>& hist, int maxrt, int64_t S, int64_t mdp, std::vector<uint32_t>& log,
+                 std::vector<uint32_t>& rank) {
+  const int64_t nb = S / kBucket, total = nb * kBucket;
   std::vector<float> bw(maxrt + 1), ebw(maxrt + 1);
   for (int r = 0; r <= maxrt; ++r) {
     bw[r] = bandwidth_of(r);
     ebw[r] = equal_bandwidth_of(r);
   }
-  std::vector<HeapItem> heap(nb);
-  for (int64_t i = 0; i < nb; ++i) heap[i] = HeapItem{(int)i, 0.0f, (int)i};
-  std::vector<int32_t> members((size_t)nb * kBucket);
-  std::vector<int32_t> fill(nb, 0);
-  std::make_heap(heap.begin(), heap.end(), ByGreat());
-  // rt of list position i: positions are in rt order, so a cursor over the histogram
-  // gives it; [lo_hi, lo_hi + hist[r_hi]) are the positions of runtime degree r_hi.
+  // ids < 2^26 and id * 40 + fill < 2^32 hold because S <= 2^31 (int32 vertex ids)
+  std::vector<int32_t> filled;  // bucket ids in the order they filled
+  filled.reserve(nb);
+  log.resize(total);
+  int64_t t = 0;
+  RunQueue<true> up;  // phase 1 pops the smallest (greatCmp heap, :144-157)
+  up.open.resize(nb);
+  for (int64_t i = 0; i < nb; ++i) up.open[i] = bucket_key(0.0f, (uint32_t)i << 6);
+  // rt of list position i: positions are in rt order; [lo, lo + hist[r]) holds rt r
   int r_hi = maxrt;
   int64_t lo_hi = S - hist[maxrt];
-  int64_t finished = 0;
-  for (int64_t i = nb * kBucket - 1; i >= mdp; --i) {  // phase 1, :144-157
-    while (i < lo_hi) {
-      --r_hi;
-      lo_hi -= hist[r_hi];
+  for (int64_t i = total - 1; i >= mdp;) {
+    while (i < lo_hi) lo_hi -= hist[--r_hi];
+    const int d = r_hi;
+    const float delta = (bw[d] - ebw[d]) / kBucket;  // :151
+    up.close_run();
+    for (const int64_t stop = lo_hi > mdp ? lo_hi : mdp; i >= stop; --i) {
+      const uint64_t k = up.pop();
+      const uint32_t low = (uint32_t)k, id = low >> 6, fill = low & 63;
+      log[t++] = id * kBucket + fill;
+      if (fill + 1 >= (uint32_t)kBucket) {
+        filled.push_back((int32_t)id);
+        continue;
+      }
+      float sup = from_order_bits((uint32_t)(k >> 32));
+      sup += delta;
+      up.push(bucket_key(sup, low + 1));
     }
-    int d = r_hi;
-    std::pop_heap(heap.begin(), heap.end() - finished, ByGreat());
-    HeapItem& b = *(heap.rbegin() + finished);
-    members[(size_t)b.slot * kBucket + fill[b.slot]++] = (int32_t)i;
-    b.sup += (bw[d] - ebw[d]) / kBucket;
-    if (fill[b.slot] >= kBucket) ++finished;
-    else std::push_heap(heap.begin(), heap.end() - finished, ByGreat());
   }
-  std::make_heap(heap.begin(), heap.end() - finished, ByLess());  // :163
+  RunQueue<false> dn;  // phase 2 pops the largest (lessCmp heap, :163-177)
+  dn.open = up.drain();
+  std::sort(dn.open.begin(), dn.open.end(), [](uint64_t a, uint64_t b) { return a > b; });
   int r_lo = 2;
   int64_t hi_lo = hist.size() > 2 ? hist[2] : 0;  // end of rt r_lo
-  for (int64_t i = 0; i < mdp; ++i) {  // phase 2, :165-177
-    while (i >= hi_lo) {
-      ++r_lo;
-      hi_lo += hist[r_lo];
+  for (int64_t i = 0; i < mdp;) {
+    while (i >= hi_lo) hi_lo += hist[++r_lo];
+    const int d = r_lo;
+    const float eps = (ebw[d] - bw[d]) / kBucket;  // :171
+    dn.close_run();
+    for (const int64_t stop = hi_lo < mdp ? hi_lo : mdp; i < stop; ++i) {
+      const uint64_t k = dn.pop();
+      const uint32_t low = (uint32_t)k, id = low >> 6, fill = low & 63;
+      log[t++] = id * kBucket + fill;
+      if (fill + 1 >= (uint32_t)kBucket) {
+        filled.push_back((int32_t)id);
+        continue;
+      }
+      float sup = from_order_bits((uint32_t)(k >> 32));
+      sup -= eps;
+      dn.push(bucket_key(sup, low + 1));
     }
-    int d = r_lo;
-    std::pop_heap(heap.begin(), heap.end() - finished, ByLess());
-    HeapItem& b = *(heap.rbegin() + finished);
-    members[(size_t)b.slot * kBucket + fill[b.slot]++] = (int32_t)i;
-    b.sup -= (ebw[d] - bw[d]) / kBucket;
-    if (fill[b.slot] >= kBucket) ++finished;
-    else std::push_heap(heap.begin(), heap.end() - finished, ByLess());
   }
-  std::sort_heap(heap.begin(), heap.end(), ByIdDesc());  // :181, on a sequence that is not a heap
-  pos.resize((size_t)nb * kBucket);
-  size_t q = 0;
-  for (int64_t i = 0; i < nb; ++i)
-    for (int j = 0; j < kBucket; ++j) pos[q++] = members[(size_t)heap[i].slot * kBucket + j];
+  // the heap array at :181 (reverse filling order), sorted as the reference sorts it;
+  // sort_heap's moves depend only on the comparisons, here of the ids alone (idSort)
+  std::vector<int32_t> arr(nb);
+  for (int64_t k = 0; k < nb; ++k) arr[nb - 1 - k] = filled[k];
+  std::sort_heap(arr.begin(), arr.end(), [](int32_t a, int32_t b) { return a > b; });
+  rank.resize(nb);
+  for (int64_t r = 0; r < nb; ++r) rank[arr[r]] = (uint32_t)r;
 }
 
 }  // namespace
@@ -299,26 +415,34 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
               (long long)mdp, (long long)nb, kBucket, maxrt);
     return ATC_ERR_UNSUPPORTED;
   }
-  std::vector<int32_t> pos;
-  bucket_heap(hist, maxrt, S, mdp, pos);
-
+  // the (rt, id) order of all vertices is sorted on the device while the host runs the
+  // bucket heap
   int B = id_bits(n_v);
   int rb = id_bits((int64_t)maxrt + 1);
   DevBuf<uint64_t> ka, kb;
-  DevBuf<int32_t> dpos;
   ATC_TRY(ka.alloc(n_v, s));
   ATC_TRY(kb.alloc(n_v, s));
-  ATC_TRY(dpos.alloc(pos.size() + 1, s));
   rtid_keys_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(rt.p, n_v, B, ka.p);
   ATC_CK(cudaGetLastError());
   uint64_t* a = ka.p;
   uint64_t* b = kb.p;
   ATC_TRY(sort_keys_u64(a, b, n_v, 0, B + rb, s));
-  if (!pos.empty())
-    ATC_CK(cudaMemcpyAsync(dpos.p, pos.data(), sizeof(int32_t) * pos.size(), cudaMemcpyHostToDevice, s));
-  lookup_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(a, B, n_v, c0, c1, S, nb * kBucket, dpos.p, lookup);
+
+  std::vector<uint32_t> log, rank;
+  bucket_heap(hist, maxrt, S, mdp, log, rank);
+  const int64_t total = nb * kBucket;
+  DevBuf<uint32_t> dlog, drank;
+  DevBuf<int32_t> dpos;
+  ATC_TRY(dlog.alloc(total, s));
+  ATC_TRY(drank.alloc(nb, s));
+  ATC_TRY(dpos.alloc(total + 1, s));
+  ATC_CK(cudaMemcpyAsync(dlog.p, log.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice, s));
+  ATC_CK(cudaMemcpyAsync(drank.p, rank.data(), sizeof(uint32_t) * nb, cudaMemcpyHostToDevice, s));
+  bucket_scatter_kernel<<<grid_for(total, 256), 256, 0, s>>>(dlog.p, drank.p, total, total - mdp, dpos.p);
   ATC_CK(cudaGetLastError());
-  ATC_CK(cudaStreamSynchronize(s));  // `pos` is pageable host memory read by the copy above
+  lookup_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(a, B, n_v, c0, c1, S, total, dpos.p, lookup);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaStreamSynchronize(s));  // `log` and `rank` are pageable host memory read by the copies above
   return ATC_OK;
 }
 
