@@ -76,7 +76,8 @@ class Tuning(C.Structure):
         ("bisson_warp_max", C.c_int32),
         ("bisson_warp_chunk", C.c_int32),
         ("bisson_block_chunk", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("bisson_slots", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 

@@ -224,10 +224,10 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   while (words < want) words <<= 1;
   if (b->max_outdeg > kHashMax) words = kTabWords;
   size_t smem = sizeof(int32_t) * words;
-  ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<CompactItems>,
+  ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<CompactItems, kDefaultSlots>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int grid_block = sm_count() * blocks_per_sm((const void*)bisson_block_kernel<CompactItems>, kBgWarps * 32, smem);
-  const int grid_warp = sm_count() * blocks_per_sm((const void*)bisson_warp_kernel<CompactItems>, kBgWarps * 32, 0);
+  const int grid_block = sm_count() * blocks_per_sm((const void*)bisson_block_kernel<CompactItems, kDefaultSlots>, kBgWarps * 32, smem);
+  const int grid_warp = sm_count() * blocks_per_sm((const void*)bisson_warp_kernel<CompactItems, kDefaultSlots>, kBgWarps * 32, 0);
 
   CsrView g{b->off, b->cols, nullptr, n, m};
   GraphTags tags{b->vbase_d, ng, b->gcounts};
@@ -246,9 +246,9 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   exclusive_scan_i32_to_i64_tmp(b->scan_tmp, &bytes, b->cnt, b->gstart, (size_t)n + 1, c);
   group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist);
   group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->gstart, b->items, cap_items, b->counters, sh);
-  bisson_block_kernel<CompactItems><<<grid_block, kBgWarps * 32, smem, c>>>(g, b->plist, bitems, 0, b->counters + 1,
+  bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(g, b->plist, bitems, 0, b->counters + 1,
                                                                             b->counters + 5, words, tags, b->gcounts);
-  bisson_warp_kernel<CompactItems><<<grid_warp, kBgWarps * 32, 0, c>>>(g, b->plist, witems, 0, b->counters,
+  bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(g, b->plist, witems, 0, b->counters,
                                                                        b->counters + 4, tags, b->gcounts);
   cudaError_t launch_err = cudaGetLastError();
   cudaError_t end_err = cudaStreamEndCapture(c, &b->graph);

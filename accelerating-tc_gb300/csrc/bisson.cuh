@@ -48,6 +48,7 @@ constexpr int kWarpChunk = 512;     // partners per warp item
 constexpr int kBlockChunk = 2048;   // partners per block item
 constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
 constexpr int kHashMax = kTabWords / 4;
+constexpr int kDefaultSlots = 1;  // hash slots per bucket unless tuned
 
 struct GroupItem {
   int32_t h;
@@ -308,17 +309,29 @@ __device__ __forceinline__ void add_item_to_graph(const GraphTags& t, int64_t h,
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(&t.counts[graph_of(t, h)], c);
 }
 
-// Fibonacci hashing: the top log2(cap) bits of x * 2^32/phi.  The low bits of that
-// product depend only on the low bits of x, and neighbour ids after relabelling share
-// low-bit patterns, which clustered the linear-probing tables (22 % of the hits at R-MAT
-// scale 24 were not in their home slot); the top bits mix all of x.
-__device__ __forceinline__ uint32_t hash_slot(int32_t x, uint32_t mask) {
-  return ((uint32_t)x * 0x9E3779B1u) >> (32 - __popc(mask));
+// Hash tables of N+(h): linear probing over buckets of S slots (S = 1, 2 or 4; 4-, 8- or
+// 16-byte aligned), empty slots hold -1.  The home bucket of x is given by Fibonacci
+// hashing: the top log2(buckets) bits of x * 2^32/phi.  The low bits of that product
+// depend only on the low bits of x, and neighbour ids after relabelling share low-bit
+// patterns, which clustered the tables (22 % of the hits at R-MAT scale 24 were not in
+// their home slot); the top bits mix all of x.
+//
+// A key goes into the first empty slot at or after the first slot of its home bucket
+// (slots in order, wrapping), so within a bucket the slots fill in order and the last
+// slot of a bucket is empty only if no key ever passed over the bucket.  A lookup reads
+// a whole bucket with one shared load and is settled by a match or by an empty last
+// slot; otherwise it goes on with the next bucket.  Keys are only emptied after every
+// lookup of an item is done.
+template <int S>
+__device__ __forceinline__ uint32_t hash_home(int32_t x, uint32_t mask) {
+  constexpr int kLogS = S == 1 ? 0 : (S == 2 ? 1 : 2);
+  return (((uint32_t)x * 0x9E3779B1u) >> (32 - (__popc(mask) - kLogS))) * S;
 }
 
 // Inserts x (not yet present); concurrent inserters use atomicCAS.
+template <int S>
 __device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t x) {
-  uint32_t s = hash_slot(x, mask);
+  uint32_t s = hash_home<S>(x, mask);
   for (uint32_t n = 0; n <= mask; ++n) {
     if (atomicCAS(&tab[s], -1, x) == -1) return;
     s = (s + 1) & mask;
@@ -327,11 +340,30 @@ __device__ __forceinline__ void hash_insert(int32_t* tab, uint32_t mask, int32_t
 
 // Empties the slot holding x (x present); keys are cleared only by the thread that
 // inserted them, so the walk always reaches x.
+template <int S>
 __device__ __forceinline__ void hash_erase(int32_t* tab, uint32_t mask, int32_t x) {
-  uint32_t s = hash_slot(x, mask);
+  uint32_t s = hash_home<S>(x, mask);
   for (uint32_t n = 0; n <= mask; ++n) {
     if (tab[s] == x) { tab[s] = -1; return; }
     s = (s + 1) & mask;
+  }
+}
+
+// Reads the bucket at slot `at`: returns whether x is in it; *stop = its last slot is empty.
+template <int S>
+__device__ __forceinline__ bool bucket_has(const int32_t* tab, uint32_t at, int32_t x, bool* stop) {
+  if constexpr (S == 1) {
+    const int32_t y = tab[at];
+    *stop = y == -1;
+    return y == x;
+  } else if constexpr (S == 2) {
+    const int2 y = *reinterpret_cast<const int2*>(tab + at);
+    *stop = y.y == -1;
+    return (y.x == x) | (y.y == x);
+  } else {
+    const int4 y = *reinterpret_cast<const int4*>(tab + at);
+    *stop = y.w == -1;
+    return (y.x == x) | (y.y == x) | (y.z == x) | (y.w == x);
   }
 }
 
@@ -347,12 +379,12 @@ struct DirectProber {  // a branch-light test per element (sorted search, bitmap
 template <class F>
 __device__ __forceinline__ DirectProber<F> direct_prober(F f) { return DirectProber<F>{f}; }
 
-// Linear-probing lookups with the chains taken out of the warp's lockstep.  Every key
-// reads its home slot; a key that is neither there nor stopped by an empty slot is
-// queued (key, next slot, steps) in the warp's 64-entry shared queue, and whenever 32
-// are queued the warp advances all of them one slot together.  A lookup loop per lane
-// would make the whole warp wait for its longest chain: at load 1/4 nearly every warp
-// has a lane whose home slot holds another key.
+// Hash lookups with the chains taken out of the warp's lockstep.  Every key reads its
+// home bucket; a key that is neither there nor stopped by an empty last slot is queued
+// (key, next bucket, steps) in the warp's 64-entry shared queue, and whenever 32 are
+// queued the warp advances all of them one bucket together.  A lookup loop per lane
+// would make the whole warp wait for its longest chain.
+template <int S>
 struct HashQueueProber {
   const int32_t* tab;
   uint32_t mask;
@@ -371,7 +403,7 @@ struct HashQueueProber {
       n += __popc(pm);
     }
   }
-  // one slot further for up to 32 queued keys (the newest); unresolved ones go back
+  // one bucket further for up to 32 queued keys (the newest); unresolved ones go back
   __device__ __forceinline__ unsigned step() {
     const int take = n < 32 ? n : 32;
     const int base = n - take;
@@ -389,12 +421,12 @@ struct HashQueueProber {
     bool pend = false;
     const uint32_t slot = q & 0xffffu, steps = q >> 16;
     if (v) {
-      const int32_t y = tab[slot];
-      hit = y == x;
-      // a key that walked the whole table is absent (cannot happen below load 1)
-      pend = y != x && y != -1 && steps < mask;
+      bool stop;
+      hit = bucket_has<S>(tab, slot, x, &stop);
+      // a key that walked every bucket is absent (cannot happen below load 1)
+      pend = !hit && !stop && steps * S < mask;
     }
-    push(pend, x, ((slot + 1) & mask) | ((steps + 1) << 16));
+    push(pend, x, ((slot + S) & mask) | ((steps + 1) << 16));
     return hit;
   }
   __device__ __forceinline__ unsigned probe(int32_t x, bool valid) {
@@ -402,12 +434,12 @@ struct HashQueueProber {
     bool pend = false;
     uint32_t s = 0;
     if (valid) {
-      s = hash_slot(x, mask);
-      const int32_t y = tab[s];
-      hit = y == x;
-      pend = y != x && y != -1;
+      s = hash_home<S>(x, mask);
+      bool stop;
+      hit = bucket_has<S>(tab, s, x, &stop);
+      pend = !hit && !stop;
     }
-    push(pend, x, ((s + 1) & mask) | (1u << 16));
+    push(pend, x, ((s + S) & mask) | (1u << 16));
     while (n >= 32) hit += step();
     return hit;
   }
@@ -489,12 +521,12 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
 }
 
 // nitems_dev (nullable): the item count read from device memory instead of `nitems`.
-template <class Items>
+template <class Items, int S = 1>
 __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                   Items items, int nitems,
                                                                   const int* nitems_dev, int* next, GraphTags tags,
                                                                   unsigned long long* out) {
-  __shared__ int32_t tab[kBgWarps][kWarpSlots];
+  __shared__ __align__(16) int32_t tab[kBgWarps][kWarpSlots];
   __shared__ int32_t qx[kBgWarps][64];
   __shared__ uint32_t qs[kBgWarps][64];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -533,12 +565,12 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
       uint32_t cap = 64;
       while (cap < 4u * (uint32_t)dh) cap <<= 1;
       const uint32_t mask = cap - 1;
-      for (int j = lane; j < dh; j += 32) hash_insert(T, mask, __ldg(g.cols + hb + j));
+      for (int j = lane; j < dh; j += 32) hash_insert<S>(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();
-      HashQueueProber pr{T, mask, qx[w], qs[w], 0, lane};
+      HashQueueProber<S> pr{T, mask, qx[w], qs[w], 0, lane};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncwarp();
-      for (int j = lane; j < dh; j += 32) hash_erase(T, mask, __ldg(g.cols + hb + j));
+      for (int j = lane; j < dh; j += 32) hash_erase<S>(T, mask, __ldg(g.cols + hb + j));
     }
     __syncwarp();
     if (tags.counts) add_item_to_graph(tags, gi.h, cnt);
@@ -547,12 +579,12 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
   warp_add_count(total, out);
 }
 
-template <class Items>
+template <class Items, int S = 1>
 __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                    Items items, int nitems,
                                                                    const int* nitems_dev, int* next, uint32_t tab_words,
                                                                    GraphTags tags, unsigned long long* out) {
-  extern __shared__ int32_t tab[];  // tab_words
+  extern __shared__ __align__(16) int32_t tab[];  // tab_words
   __shared__ int32_t qx[kBgWarps][64];
   __shared__ uint32_t qs[kBgWarps][64];
   __shared__ int cur_item;
@@ -584,12 +616,12 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       uint32_t cap = 64;
       while (cap < 4u * (uint32_t)dh) cap <<= 1;
       const uint32_t mask = cap - 1;
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert(tab, mask, Nh[j]);
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert<S>(tab, mask, Nh[j]);
       __syncthreads();
-      HashQueueProber pr{tab, mask, qx[w], qs[w], 0, lane};
+      HashQueueProber<S> pr{tab, mask, qx[w], qs[w], 0, lane};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncthreads();
-      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase(tab, mask, Nh[j]);
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase<S>(tab, mask, Nh[j]);
     } else if (gi.mode == 1) {
       const int32_t lo = Nh[0], hi = Nh[dh - 1];
       const int words = ((hi - lo) >> 5) + 1;

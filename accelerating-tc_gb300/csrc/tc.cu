@@ -2,15 +2,17 @@
 // re-designed for sm_103a.  All count sum_u sum_{v in N+(u)} |N+(u) ∩ N+(v)| exactly in
 // uint64; every warp reduces its lanes with shuffles and adds once to a 64-bit counter.
 //
-//   Hu-style      Hu/tc.cu:22-201       CTA per balanced vertex range; runs of
-//                                        consecutive N+(u) staged in shared memory; a
-//                                        warp per edge streams N+(v) (coalesced) and
-//                                        binary-searches each element in the staged N+(u).
-//   Bisson-style  Bisson/tc.cu:18-104   out-degree > cutover: CTA per row, N+(u) as a
-//                                        bitmap (shared memory over [min,max] of the
-//                                        row, or a per-CTA global bitmap), one bit test
-//                                        per candidate; smaller rows: warp per row, row
-//                                        in shared memory, binary search.
+//   Hu-style      Hu/tc.cu:22-201       wedge walk: N+(u) staged in shared memory once
+//                                        per work item (chunk of N+(u)), every N+(v),
+//                                        v in N+(u), streamed through it (W tests);
+//                                        sorted copy + branch-free search for short
+//                                        N+(u), hash table above.
+//   Bisson-style  Bisson/tc.cu:18-104   every edge handed to the endpoint h with the
+//                                        longer list (grouping passes); N+(h) as a hash
+//                                        table, bitmap or sorted copy in shared memory,
+//                                        the partner's shorter list streamed through it
+//                                        (sum of min(d+u, d+v) tests).  Kernels in
+//                                        bisson.cuh.
 //   Fox-style     Fox/tc.cu:18-125,     per-edge work min*log2(max+2); edges binned on
 //                 316-384                the device into 1,2,4,...,32 threads per edge;
 //                                        each thread searches a slice of the shorter list
@@ -194,70 +196,6 @@ __global__ void fox_deal_kernel(const uint64_t* keys, const int64_t* list, int64
   }
 }
 
-// ============================== Hu-style ===========================================
-constexpr int kHuWarps = 8;
-constexpr int kHuStage = 6144;  // ints of N+(u) staged per CTA (24 KB)
-
-// Per-vertex work used to cut the vertex range into CTAs of equal work: the wedges
-// u -> v -> w it opens plus its own list (a balanced form of Hu/tc.cu:22-35).
-__global__ void hu_work_kernel(CsrView g, int64_t* work) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < g.n; u += stride) {
-    int64_t b = g.off[u], e = g.off[u + 1];
-    int64_t s = (e - b) + 1;
-    for (int64_t j = b; j < e; ++j) {
-      int32_t v = g.cols[j];
-      s += g.off[v + 1] - g.off[v];
-    }
-    work[u] = s;
-  }
-}
-
-// start[b] = first vertex whose work prefix reaches b * total / nb (Hu/tc.cu:292-301).
-__global__ void hu_cut_kernel(const int64_t* prefix, int64_t n, int64_t total, int nb, int32_t* start) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b > nb) return;
-  if (b == nb) { start[b] = (int32_t)n; return; }
-  int64_t target = (int64_t)((__int128)total * b / nb);
-  int64_t lo = 0, hi = n;
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if (prefix[mid] < target) lo = mid + 1; else hi = mid;
-  }
-  start[b] = (int32_t)lo;
-}
-
-__global__ void __launch_bounds__(kHuWarps * 32) hu_kernel(CsrView g, const int32_t* start, unsigned long long* out) {
-  __shared__ int32_t stage[kHuStage];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned long long cnt = 0;
-  int32_t u0 = start[blockIdx.x], uend = start[blockIdx.x + 1];
-  while (u0 < uend) {
-    // the run [u0, u1): consecutive lists that fit the stage together (at least one)
-    int64_t E0 = g.off[u0];
-    int32_t u1 = u0 + 1;
-    while (u1 < uend && g.off[u1 + 1] - E0 <= kHuStage) ++u1;
-    int64_t E1 = g.off[u1];
-    bool staged = E1 - E0 <= kHuStage;
-    if (staged) {
-      for (int64_t j = threadIdx.x; j < E1 - E0; j += blockDim.x) stage[j] = g.cols[E0 + j];
-    }
-    __syncthreads();
-    for (int64_t e = E0 + w; e < E1; e += kHuWarps) {
-      int32_t u = g.esrc[e];
-      int32_t v = staged ? stage[e - E0] : g.cols[e];
-      int64_t ub = g.off[u], ud = g.off[u + 1] - ub;
-      const int32_t* Nu = staged ? stage + (ub - E0) : g.cols + ub;
-      int64_t vb = g.off[v], vd = g.off[v + 1] - vb;
-      for (int64_t j = lane; j < vd; j += 32) cnt += bsearch_has(Nu, ud, g.cols[vb + j]);
-    }
-    __syncthreads();
-    u0 = u1;
-  }
-  warp_add_count(cnt, out);
-}
-
-
 }  // namespace
 
 // ---- family drivers ----------------------------------------------------------------
@@ -356,40 +294,96 @@ static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long l
   return ATC_OK;
 }
 
+// Launches the block and warp kernels over work items; S = hash slots per bucket.
+// hc = {warp items, block items, -, longest hashed block list}.
+template <int S>
+static atc_status launch_bisson(const CsrView& g, const int32_t* plist, const GroupItem* witems,
+                                const GroupItem* bitems, const int* hc, int* counters, unsigned long long* ctr,
+                                cudaStream_t s, int* launches) {
+  if (hc[1]) {
+    // block table: enough slots for the longest hashed list at load factor 1/4, or the
+    // full bitmap when some list needs it
+    uint32_t words = 64;
+    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
+    if (words > (uint32_t)kTabWords) words = kTabWords;
+    size_t smem = sizeof(int32_t) * words;
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems, S>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems, S>, kBgWarps * 32, smem);
+    int grid = std::min(hc[1], sm_count() * bps);
+    bisson_block_kernel<FullItems, S><<<grid, kBgWarps * 32, smem, s>>>(
+        g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, words, GraphTags{nullptr, 0, nullptr}, ctr);
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  if (hc[0]) {
+    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems, S>, kBgWarps * 32, 0);
+    int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
+    bisson_warp_kernel<FullItems, S><<<grid, kBgWarps * 32, 0, s>>>(g, plist, FullItems{witems}, hc[0], nullptr,
+                                                                   counters + 4, GraphTags{nullptr, 0, nullptr}, ctr);
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  return ATC_OK;
+}
+
+static atc_status launch_slots(int slots, const CsrView& g, const int32_t* plist, const GroupItem* witems,
+                               const GroupItem* bitems, const int* hc, int* counters, unsigned long long* ctr,
+                               cudaStream_t s, int* launches) {
+  if (slots == 1) return launch_bisson<1>(g, plist, witems, bitems, hc, counters, ctr, s, launches);
+  if (slots == 2) return launch_bisson<2>(g, plist, witems, bitems, hc, counters, ctr, s, launches);
+  return launch_bisson<4>(g, plist, witems, bitems, hc, counters, ctr, s, launches);
+}
+
+// Item shape: the defaults, overridden field by field by the tuning (chunks >= 32 partners).
+static atc_status item_shape(const atc_tuning* t, ItemShape* sh, int* slots) {
+  *sh = default_shape(32);
+  *slots = kDefaultSlots;
+  if (!t) return ATC_OK;
+  ATC_CHECK_ARG(t->bisson_slots == 0 || t->bisson_slots == 1 || t->bisson_slots == 2 || t->bisson_slots == 4,
+                "bisson_slots must be 0, 1, 2 or 4");
+  if (t->bisson_cutover > 0) sh->cutover = std::min(t->bisson_cutover, kWarpMax);
+  if (t->bisson_warp_max > 0) sh->warp_max = std::min(t->bisson_warp_max, kWarpMax);
+  if (t->bisson_warp_chunk > 0) sh->warp_chunk = std::max(t->bisson_warp_chunk, 32);
+  if (t->bisson_block_chunk > 0) sh->block_chunk = std::max(t->bisson_block_chunk, 32);
+  if (t->bisson_slots > 0) *slots = t->bisson_slots;
+  return ATC_OK;
+}
+
+// Hu-style (Hu/tc.cu:69-201): every wedge u -> v -> w is tested against N+(u), which a
+// work item stages in shared memory once and which every N+(v), v in N+(u), streams
+// through: W tests in all.  The reference binary-searches a sorted run of N+(u); here the
+// staged set is the sorted copy searched branch-free for d+(u) <= 32 and a hash table
+// above (the Bisson-style kernels' sets).  The reference's 30 000 vertex ranges of equal
+// wedge work (Hu/tc.cu:22-67,263-301) become chunks of N+(u) drained from a device queue,
+// which balances dynamically.  No grouping pass: the items index the CSR itself.
 static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                          int* launches) {
-  int nb = t && t->hu_blocks > 0 ? t->hu_blocks
-                                 : sm_count() * blocks_per_sm((const void*)hu_kernel, kHuWarps * 32, 0) * 4;
-  DevBuf<int64_t> work, prefix;
-  DevBuf<int32_t> start;
-  ATC_TRY(work.alloc(g.n + 1, s));
-  ATC_TRY(prefix.alloc(g.n + 1, s));
-  ATC_TRY(start.alloc(nb + 1, s));
-  hu_work_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, work.p);
+  ItemShape sh;
+  int slots;
+  ATC_TRY(item_shape(t, &sh, &slots));
+  DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
+  ATC_TRY(counters.alloc(8, s));
+  ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
+  const int64_t mi = max_items(g.n, g.m, std::min(sh.warp_chunk, sh.block_chunk));
+  DevBuf<GroupItem> witems, bitems;
+  ATC_TRY(witems.alloc(mi, s));
+  ATC_TRY(bitems.alloc(mi, s));
+  // the partner range of u is its own CSR row
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, g.off, witems.p, bitems.p, counters.p, sh);
   ATC_CK(cudaGetLastError());
-  ATC_CK(cudaMemsetAsync(work.p + g.n, 0, sizeof(int64_t), s));
-  ATC_TRY(exclusive_scan_i64(work.p, prefix.p, g.n + 1, s));
-  int64_t total = 0;
-  ATC_CK(cudaMemcpyAsync(&total, prefix.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  int hc[4];
+  ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
-  hu_cut_kernel<<<(nb + 1 + 255) / 256, 256, 0, s>>>(prefix.p, g.n, total, nb, start.p);
-  ATC_CK(cudaGetLastError());
-  hu_kernel<<<nb, kHuWarps * 32, 0, s>>>(g, start.p, ctr);
-  ATC_CK(cudaGetLastError());
-  *launches += 4;
-  return ATC_OK;
+  *launches += 1;
+  return launch_slots(slots, g, g.cols, witems.p, bitems.p, hc, counters.p, ctr, s, launches);
 }
 
 static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                              int* launches) {
-  // item shape: defaults, overridden field by field by the tuning (chunks >= 32 partners)
-  ItemShape sh = default_shape(32);
-  if (t) {
-    if (t->bisson_cutover > 0) sh.cutover = std::min(t->bisson_cutover, kWarpMax);
-    if (t->bisson_warp_max > 0) sh.warp_max = std::min(t->bisson_warp_max, kWarpMax);
-    if (t->bisson_warp_chunk > 0) sh.warp_chunk = std::max(t->bisson_warp_chunk, 32);
-    if (t->bisson_block_chunk > 0) sh.block_chunk = std::max(t->bisson_block_chunk, 32);
-  }
+  ItemShape sh;
+  int slots;
+  ATC_TRY(item_shape(t, &sh, &slots));
   DevBuf<int32_t> cnt, cur, plist;
   DevBuf<int64_t> gstart;
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
@@ -420,31 +414,7 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   *launches += 4;
-  if (hc[1]) {
-    // block table: enough slots for the longest hashed list at load factor 1/4, or the
-    // full bitmap when some list needs it
-    uint32_t words = 64;
-    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
-    if (words > (uint32_t)kTabWords) words = kTabWords;
-    size_t smem = sizeof(int32_t) * words;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems>, kBgWarps * 32, smem);
-    int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist.p, FullItems{bitems.p}, hc[1], nullptr, counters.p + 5, words,
-                                                          GraphTags{nullptr, 0, nullptr}, ctr);
-    ATC_CK(cudaGetLastError());
-    *launches += 1;
-  }
-  if (hc[0]) {
-    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems>, kBgWarps * 32, 0);
-    int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
-    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist.p, FullItems{witems.p}, hc[0], nullptr, counters.p + 4,
-                                                      GraphTags{nullptr, 0, nullptr}, ctr);
-    ATC_CK(cudaGetLastError());
-    *launches += 1;
-  }
-  return ATC_OK;
+  return launch_slots(slots, g, plist.p, witems.p, bitems.p, hc, counters.p, ctr, s, launches);
 }
 
 // ---- counting without device allocation ------------------------------------------
@@ -595,18 +565,18 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
     while (words < 4u * (uint32_t)hc[3]) words <<= 1;
     if (words > (uint32_t)kTabWords) words = kTabWords;
     size_t smem = sizeof(int32_t) * words;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems, kDefaultSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems>, kBgWarps * 32, smem);
+    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems, kDefaultSlots>, kBgWarps * 32, smem);
     int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<<<grid, kBgWarps * 32, smem, s>>>(g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, words,
+    bisson_block_kernel<FullItems, kDefaultSlots><<<grid, kBgWarps * 32, smem, s>>>(g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, words,
                                                           GraphTags{nullptr, 0, nullptr}, total_ctr);
     ATC_CK(cudaGetLastError());
   }
   if (hc[0]) {
-    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems>, kBgWarps * 32, 0);
+    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems, kDefaultSlots>, kBgWarps * 32, 0);
     int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
-    bisson_warp_kernel<<<grid, kBgWarps * 32, 0, s>>>(g, plist, FullItems{witems}, hc[0], nullptr, counters + 4,
+    bisson_warp_kernel<FullItems, kDefaultSlots><<<grid, kBgWarps * 32, 0, s>>>(g, plist, FullItems{witems}, hc[0], nullptr, counters + 4,
                                                       GraphTags{nullptr, 0, nullptr}, total_ctr);
     ATC_CK(cudaGetLastError());
   }

@@ -87,7 +87,7 @@ typedef enum atc_relabel_kind {
 
 typedef enum atc_kernel {
   ATC_KERNEL_AUTO = 0,    /* library default for the graph */
-  ATC_KERNEL_HU = 1,      /* vertex-range wedge walk, staged N+(u) (Hu/tc.cu:69-201) */
+  ATC_KERNEL_HU = 1,      /* wedge walk, N+(u) staged in shared memory (Hu/tc.cu:69-201) */
   ATC_KERNEL_BISSON = 2,  /* bitmap for large N+(u), search otherwise (Bisson/tc.cu:18-104) */
   ATC_KERNEL_FOX = 3,     /* edge bins with 1..32 threads per edge (Fox/tc.cu:64-125,316-384) */
   ATC_KERNEL_TRICORE = 4  /* warp per edge, 32 pivots + binary search (tricount_gpu.cu:215-290) */
@@ -97,16 +97,18 @@ typedef enum atc_kernel {
    #defines (Hu/tc.cu:6-8, Bisson/tc.cu:5-6, Fox/tc.cu:318-319, tricount_gpu.cu:24-25). */
 typedef struct atc_tuning {
   int32_t prune_deg1;        /* drop degree<=1 vertices, compact ids (Hu/preTC.cu:135-169) */
-  int32_t hu_blocks;         /* CTAs of the Hu-style kernel (0: 8 per SM) */
-  int32_t hu_stage_ints;     /* ints of N+(u) staged in shared memory per CTA */
-  int32_t bisson_cutover;    /* out-degree above which the bitmap path is taken (32) */
+  int32_t hu_blocks;         /* unused: the Hu-style kernel drains a work queue (layout kept) */
+  int32_t hu_stage_ints;     /* unused: N+(u) is staged per work item (layout kept) */
+  int32_t bisson_cutover;    /* warp items: sorted copy up to this out-degree, hash above (32) */
   int32_t fox_rearrange;     /* interleave each bin's edges (Fox/tc.cu:127-183) */
   int32_t fox_work_per_thread; /* bin base of the threads-per-edge bins (8) */
   int32_t tricore_blocks;    /* CTAs of the TriCore-style kernel (0: auto) */
   int32_t bisson_warp_max;   /* longest list a warp item handles, <= 256 (256) */
   int32_t bisson_warp_chunk; /* partners per warp item (512) */
   int32_t bisson_block_chunk; /* partners per block item (2048) */
-  int32_t reserved[6];
+  int32_t bisson_slots;      /* hash slots per bucket of the tables: 1, 2 or 4 (0: default) */
+  /* the bisson_* item shape applies to the Hu-style kernel too */
+  int32_t reserved[5];
 } atc_tuning;
 
 /* Oriented CSR on the device (the reference's edgeOffset/edgeRow/adjLength globals,
