@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <new>
+#include <thread>
 #include <vector>
 
 #include "internal.cuh"
@@ -367,24 +369,31 @@ atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uin
 }
 
 atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int32_t* lookup,
-                         int2* oriented, cudaStream_t s) {
+                         int2* oriented, cudaStream_t s, const int32_t* known_deg,
+                         const std::function<atc_status()>* overlap) {
   if (n_v <= 0) {
     set_error("A-order needs at least one edge");
     return ATC_ERR_UNSUPPORTED;
   }
   DevBuf<int32_t> deg, rt;
   DevBuf<int> mx;
-  ATC_TRY(deg.alloc(n_v, s));
   ATC_TRY(rt.alloc(n_v, s));
   ATC_TRY(mx.alloc(1, s));
-  ATC_CK(cudaMemsetAsync(deg.p, 0, sizeof(int32_t) * n_v, s));
   ATC_CK(cudaMemsetAsync(rt.p, 0, sizeof(int32_t) * n_v, s));
   ATC_CK(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
+  const int32_t* degp = known_deg;
+  if (!degp) {
+    ATC_TRY(deg.alloc(n_v, s));
+    ATC_CK(cudaMemsetAsync(deg.p, 0, sizeof(int32_t) * n_v, s));
+    if (ne) {
+      if (pairs) deg_pairs_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, ne, deg.p);
+      else deg_keys_kernel<<<grid_for(ne, 256), 256, 0, s>>>(keys, ne, bits, deg.p);
+      ATC_CK(cudaGetLastError());
+    }
+    degp = deg.p;
+  }
   if (ne) {
-    if (pairs) deg_pairs_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, ne, deg.p);
-    else deg_keys_kernel<<<grid_for(ne, 256), 256, 0, s>>>(keys, ne, bits, deg.p);
-    ATC_CK(cudaGetLastError());
-    rt_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, keys, bits, ne, deg.p, rt.p, oriented);
+    rt_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, keys, bits, ne, degp, rt.p, oriented);
     ATC_CK(cudaGetLastError());
   }
   rt_hist_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(rt.p, n_v, nullptr, mx.p);
@@ -429,7 +438,25 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
   ATC_TRY(sort_keys_u64(a, b, n_v, 0, B + rb, s));
 
   std::vector<uint32_t> log, rank;
-  bucket_heap(hist, maxrt, S, mdp, log, rank);
+  if (overlap) {
+    bool heap_ok = true;
+    std::thread heap([&] {
+      try {
+        bucket_heap(hist, maxrt, S, mdp, log, rank);
+      } catch (const std::bad_alloc&) {
+        heap_ok = false;
+      }
+    });
+    const atc_status st = (*overlap)();
+    heap.join();
+    ATC_TRY(st);
+    if (!heap_ok) {
+      set_error("A-order: host allocation failed");
+      return ATC_ERR_OOM;
+    }
+  } else {
+    bucket_heap(hist, maxrt, S, mdp, log, rank);
+  }
   const int64_t total = nb * kBucket;
   DevBuf<uint32_t> dlog, drank;
   DevBuf<int32_t> dpos;

@@ -48,7 +48,7 @@ constexpr int kWarpChunk = 512;     // partners per warp item
 constexpr int kBlockChunk = 2048;   // partners per block item
 constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
 constexpr int kHashMax = kTabWords / 4;
-constexpr int kDefaultSlots = 1;  // hash slots per bucket unless tuned
+constexpr int kDefaultSlots = 4;  // hash slots per bucket unless tuned (one 16-byte shared load)
 
 struct GroupItem {
   int32_t h;

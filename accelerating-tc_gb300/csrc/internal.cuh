@@ -1,6 +1,8 @@
 // Declarations shared between libatc translation units (not part of the ABI).
 #pragma once
 
+#include <functional>
+
 #include "common.cuh"
 
 namespace atc {
@@ -57,9 +59,12 @@ atc_status approx_peel(const SimpleEdges& e, const int32_t* deg, uint32_t* flags
 // non-null).  n_v = max id + 1 over the edges.  lookup: n_v ints (device).  If
 // oriented != nullptr (pairs input only) it receives the degree-oriented pairs (the
 // "normal" file).  Returns ATC_ERR_UNSUPPORTED where the reference reads outside its
-// arrays.
+// arrays.  deg (nullable, device): the degrees of the edges when the caller has them.
+// overlap (nullable): device work that does not depend on the lookup, run on the calling
+// thread while the host part of A-order runs on another.
 atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v,
-                         int32_t* lookup, int2* oriented, cudaStream_t s);
+                         int32_t* lookup, int2* oriented, cudaStream_t s, const int32_t* deg = nullptr,
+                         const std::function<atc_status()>* overlap = nullptr);
 
 // Rank relabellings (vertex_ordering/A-order/A-order-v2.cpp, relabel-naive.cpp,
 // relabel4lpOut.cpp) of an edge list with repeats counted: lookup (n_v ints, device);

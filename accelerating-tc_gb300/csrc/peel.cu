@@ -20,14 +20,29 @@ namespace atc {
 
 namespace {
 
+// Symmetric adjacency from the sorted keys (a < b).  Keys of one smaller endpoint are
+// contiguous, so a warp reserves each run's slots with one atomic (the loop is padded to
+// whole warps for __match_any_sync); the larger endpoints are scattered one by one.
 __global__ void sym_scatter_kernel(const uint64_t* keys, int64_t m, int B, unsigned long long* cur, int32_t* adj) {
-  uint64_t mask = (1ull << B) - 1;
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
-    uint64_t k = keys[i];
-    int32_t a = (int32_t)(k >> B), b = (int32_t)(k & mask);
-    adj[atomicAdd(&cur[a], 1ull)] = b;
-    adj[atomicAdd(&cur[b], 1ull)] = a;
+  const uint64_t mask = (1ull << B) - 1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t m_pad = (m + 31) & ~31ll;
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m_pad; i += stride) {
+    int64_t a = -1;
+    int32_t b = 0;
+    if (i < m) {
+      const uint64_t k = keys[i];
+      a = (int64_t)(k >> B);
+      b = (int32_t)(k & mask);
+      adj[atomicAdd(&cur[b], 1ull)] = (int32_t)a;
+    }
+    const unsigned same = __match_any_sync(0xffffffffu, a);
+    const int lead = __ffs(same) - 1;
+    unsigned long long base = 0;
+    if (a >= 0 && lane == lead) base = atomicAdd(&cur[a], (unsigned long long)__popc(same));
+    base = __shfl_sync(0xffffffffu, base, lead);
+    if (a >= 0) adj[base + __popc(same & ((1u << lane) - 1))] = b;
   }
 }
 

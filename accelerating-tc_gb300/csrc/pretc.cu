@@ -51,13 +51,23 @@ __global__ void canon_kernel(const int2* p, uint64_t np, int B, uint64_t* keys) 
   }
 }
 
+// Degrees of the simple graph from its sorted keys.  Keys of one smaller endpoint are
+// contiguous, so a warp adds each run of them with one atomic (the loop is padded to whole
+// warps for __match_any_sync); the larger endpoints are scattered.
 __global__ void degree_kernel(const uint64_t* keys, int64_t m, int B, int32_t* deg) {
-  uint64_t mask = (1ull << B) - 1;
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
-    uint64_t k = keys[i];
-    atomicAdd(&deg[k >> B], 1);
-    atomicAdd(&deg[k & mask], 1);
+  const uint64_t mask = (1ull << B) - 1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t m_pad = (m + 31) & ~31ll;
+  const int lane = threadIdx.x & 31;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m_pad; i += stride) {
+    int64_t lo = -1;
+    if (i < m) {
+      const uint64_t k = keys[i];
+      lo = (int64_t)(k >> B);
+      atomicAdd(&deg[k & mask], 1);
+    }
+    const unsigned same = __match_any_sync(0xffffffffu, lo);
+    if (lo >= 0 && lane == __ffs(same) - 1) atomicAdd(&deg[lo], __popc(same));
   }
 }
 
@@ -296,6 +306,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   int64_t n_in = e.n_in;
   DevBuf<int32_t> deg, prio, perm, cmap;
   DevBuf<uint32_t> minor;
+  bool peeled = false;  // A-direction priorities computed already
   ATC_TRY(deg.alloc(n_in, s));
   ATC_TRY(simple_degrees(e, deg.p, s));
   if (order != ATC_ORDER_NONE) {
@@ -317,14 +328,22 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
       ATC_CK(cudaStreamSynchronize(s));
       n_v = (int64_t)h + 1;
     }
-    if (order == ATC_ORDER_AORDER)
-      ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s));
-    else
+    if (order == ATC_ORDER_AORDER && dir == ATC_DIR_ADIRECTION) {
+      // the peel does not depend on the relabelling: it runs on the device while the
+      // host part of A-order runs
+      ATC_TRY(prio.alloc(n_in, s));
+      int waves = 0;
+      const std::function<atc_status()> peel = [&] { return peel_priorities(e, deg.p, prio.p, &waves, s); };
+      ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s, deg.p, &peel));
+      peeled = true;
+    } else if (order == ATC_ORDER_AORDER) {
+      ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s, deg.p));
+    } else
       ATC_TRY(relabel_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v,
                              order == ATC_ORDER_DEGREE_DESC ? ATC_RELABEL_DEGREE_DESC : ATC_RELABEL_AORDER_V2, perm.p,
                              nullptr, s));
   }
-  if (dir == ATC_DIR_ADIRECTION) {
+  if (dir == ATC_DIR_ADIRECTION && !peeled) {
     ATC_TRY(prio.alloc(n_in, s));
     int waves = 0;
     ATC_TRY(peel_priorities(e, deg.p, prio.p, &waves, s));
