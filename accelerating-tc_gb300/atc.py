@@ -151,6 +151,8 @@ _SIGS = {
     "atc_relabel": (C.c_int, [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]),
     "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_tc_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_uint64), _P]),
+    "atc_tc_part": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.c_uint32, C.c_uint32,
+                              C.POINTER(C.c_uint64), C.POINTER(C.c_int64), C.POINTER(StatsStruct), _P]),
     "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "atc_batch_reserve": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _P]),
@@ -367,6 +369,16 @@ def tc(csr: CSR, kernel=Kernel.AUTO, tuning=None, stream=None):
     st = StatsStruct()
     _check(lib().atc_tc(C.byref(csr.struct), int(kernel), _tuning(tuning), C.byref(cnt), C.byref(st), stream))
     return cnt.value, _stats(st)
+
+
+def tc_part(csr: CSR, part, nparts, kernel=Kernel.AUTO, tuning=None, stream=None):
+    """atc_tc_part: (count of part `part` of `nparts` work-balanced edge ranges, (first, last) edge, stats)."""
+    cnt = C.c_uint64(0)
+    rng = (C.c_int64 * 2)()
+    st = StatsStruct()
+    _check(lib().atc_tc_part(C.byref(csr.struct), int(kernel), _tuning(tuning), part, nparts, C.byref(cnt), rng,
+                             C.byref(st), stream))
+    return cnt.value, (rng[0], rng[1]), _stats(st)
 
 
 def tc_noalloc(offsets_dev_ptr, cols_dev_ptr, n, m, stream=None):

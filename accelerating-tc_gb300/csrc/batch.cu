@@ -229,7 +229,7 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   const int grid_block = sm_count() * blocks_per_sm((const void*)bisson_block_kernel<CompactItems, kDefaultSlots>, kBgWarps * 32, smem);
   const int grid_warp = sm_count() * blocks_per_sm((const void*)bisson_warp_kernel<CompactItems, kDefaultSlots>, kBgWarps * 32, 0);
 
-  CsrView g{b->off, b->cols, nullptr, n, m};
+  CsrView g = csr_view(b->off, b->cols, nullptr, n, m);
   GraphTags tags{b->vbase_d, ng, b->gcounts};
   CompactItems witems{b->items, b->gstart, cap_items, false, sh};
   CompactItems bitems{b->items, b->gstart, cap_items, true, sh};

@@ -12,7 +12,12 @@ struct CsrView {
   const int32_t* cols;
   const int32_t* esrc;
   int64_t n, m;
+  int64_t e0, e1;  // edge window [e0, e1) of the per-edge passes (0, m: every edge)
 };
+
+inline CsrView csr_view(const int64_t* off, const int32_t* cols, const int32_t* esrc, int64_t n, int64_t m) {
+  return CsrView{off, cols, esrc, n, m, 0, m};
+}
 
 namespace {
 
@@ -64,10 +69,11 @@ __device__ __forceinline__ bool longer_is_u(int32_t u, int32_t v, int64_t du, in
 // contiguous, so runs of one h are common).
 __global__ void group_count_kernel(CsrView g, int32_t* cnt) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t m_pad = (g.m + 31) & ~31ll;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
+  int64_t w_pad = (g.e1 - g.e0 + 31) & ~31ll;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < w_pad; i += stride) {
+    const int64_t e = g.e0 + i;
     int32_t h = -1;
-    if (e < g.m) {
+    if (e < g.e1) {
       int32_t u = g.esrc[e], v = g.cols[e];
       int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
       if (du > 0 && dv > 0) h = longer_is_u(u, v, du, dv) ? u : v;
@@ -81,11 +87,12 @@ __global__ void group_count_kernel(CsrView g, int32_t* cnt) {
 // Pass 2: scatter partners into their group (order inside a group is irrelevant).
 __global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t m_pad = (g.m + 31) & ~31ll;
+  int64_t w_pad = (g.e1 - g.e0 + 31) & ~31ll;
   const int lane = threadIdx.x & 31;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m_pad; e += stride) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < w_pad; i += stride) {
+    const int64_t e = g.e0 + i;
     int32_t h = -1, p = 0;
-    if (e < g.m) {
+    if (e < g.e1) {
       int32_t u = g.esrc[e], v = g.cols[e];
       int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
       if (du > 0 && dv > 0) {
@@ -143,15 +150,16 @@ __device__ __forceinline__ int warp_reserve(int* ctr, int k) {
 
 // One lane per vertex h; the loop bound is padded to whole warps so that every lane of a
 // warp takes part in warp_reserve.
+// The partner range of h is [gstart[h], gstart[h+1]) clipped to [clip0, clip1).
 __global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* witems, GroupItem* bitems,
-                                   int* counters, ItemShape sh) {
+                                   int* counters, ItemShape sh, int64_t clip0, int64_t clip1) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t n_pad = (g.n + 31) & ~31ll;
   for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < n_pad; h += stride) {
     int64_t b = 0, e = 0, hb = 0, dh = 0;
     if (h < g.n) {
-      b = gstart[h];
-      e = gstart[h + 1];
+      b = max(gstart[h], clip0);
+      e = min(gstart[h + 1], clip1);
       hb = g.off[h];
       dh = g.off[h + 1] - hb;
     }

@@ -53,6 +53,40 @@ __device__ __forceinline__ bool bsearch_has32(const int32_t* a, int n, int32_t x
   return lo < n && a[lo] == x;
 }
 
+// ============================== part split ===========================================
+// Work of edge e for cutting the edges into parts: the shorter list it streams, plus one.
+// work[m] = 0, so that an exclusive scan of m + 1 entries ends with the total.
+__global__ void edge_work_kernel(CsrView g, int64_t* work) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e <= g.m; e += stride) {
+    int64_t w = 0;
+    if (e < g.m) {
+      const int32_t u = g.esrc[e], v = g.cols[e];
+      const int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      w = (du < dv ? du : dv) + 1;
+    }
+    work[e] = w;
+  }
+}
+
+// bounds[t] (t = 0, 1) = the first edge whose work prefix reaches total * (part + t) / nparts.
+__global__ void part_bounds_kernel(const int64_t* prefix, int64_t m, uint32_t part, uint32_t nparts, int64_t* bounds) {
+  const int t = threadIdx.x;
+  if (t > 1) return;
+  const uint32_t k = part + t;
+  if (k == 0 || k >= nparts) {
+    bounds[t] = k == 0 ? 0 : m;
+    return;
+  }
+  const int64_t target = (int64_t)((__int128)prefix[m] * k / nparts);
+  int64_t lo = 0, hi = m;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (prefix[mid] < target) lo = mid + 1; else hi = mid;
+  }
+  bounds[t] = lo;
+}
+
 // ============================== TriCore-style ======================================
 constexpr int kTriWarps = 8;
 
@@ -61,7 +95,7 @@ __global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsi
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned long long cnt = 0;
   const int64_t warps = (int64_t)gridDim.x * kTriWarps;
-  for (int64_t e = (int64_t)blockIdx.x * kTriWarps + w; e < g.m; e += warps) {
+  for (int64_t e = g.e0 + (int64_t)blockIdx.x * kTriWarps + w; e < g.e1; e += warps) {
     int32_t u = g.esrc[e], v = g.cols[e];
     int64_t au = g.off[u], du = g.off[u + 1] - au;
     int64_t av = g.off[v], dv = g.off[v + 1] - av;
@@ -101,7 +135,7 @@ __device__ __forceinline__ int fox_work(int64_t du, int64_t dv) {
 __global__ void fox_maxwork_kernel(CsrView g, int* maxw) {
   int best = 0;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.m; e += stride) {
+  for (int64_t e = g.e0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.e1; e += stride) {
     int32_t u = g.esrc[e], v = g.cols[e];
     best = max(best, fox_work(g.off[u + 1] - g.off[u], g.off[v + 1] - g.off[v]));
   }
@@ -125,7 +159,7 @@ __global__ void fox_hist_kernel(CsrView g, FoxBins fb, unsigned long long* hist)
   if (threadIdx.x < 6) h[threadIdx.x] = 0;
   __syncthreads();
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.m; e += stride) {
+  for (int64_t e = g.e0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.e1; e += stride) {
     int32_t u = g.esrc[e], v = g.cols[e];
     atomicAdd(&h[fox_bin(fb, fox_work(g.off[u + 1] - g.off[u], g.off[v + 1] - g.off[v]))], 1u);
   }
@@ -135,7 +169,7 @@ __global__ void fox_hist_kernel(CsrView g, FoxBins fb, unsigned long long* hist)
 
 __global__ void fox_scatter_kernel(CsrView g, FoxBins fb, unsigned long long* cursor, int64_t* list) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.m; e += stride) {
+  for (int64_t e = g.e0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.e1; e += stride) {
     int32_t u = g.esrc[e], v = g.cols[e];
     int b = fox_bin(fb, fox_work(g.off[u + 1] - g.off[u], g.off[v + 1] - g.off[v]));
     list[atomicAdd(&cursor[b], 1ull)] = e;
@@ -218,7 +252,7 @@ static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long l
   ATC_TRY(cursor.alloc(6, s));
   ATC_CK(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
   ATC_CK(cudaMemsetAsync(hist.p, 0, sizeof(unsigned long long) * 6, s));
-  fox_maxwork_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, mx.p);
+  fox_maxwork_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, mx.p);
   ATC_CK(cudaGetLastError());
   int maxw = 0;
   ATC_CK(cudaMemcpyAsync(&maxw, mx.p, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -236,7 +270,7 @@ static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long l
     fb.bound[k] = pp > 2147483647.0L ? 2147483647 : (int)pp;
   }
   fb.bound[6] = INT32_MAX;
-  fox_hist_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, fb, hist.p);
+  fox_hist_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, fb, hist.p);
   ATC_CK(cudaGetLastError());
   unsigned long long h[6];
   ATC_CK(cudaMemcpyAsync(h, hist.p, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -246,13 +280,13 @@ static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long l
   for (int b = 0; b < 6; ++b) start[b + 1] = start[b] + h[b];
   ATC_CK(cudaMemcpyAsync(cursor.p, start, sizeof(unsigned long long) * 6, cudaMemcpyHostToDevice, s));
   DevBuf<int64_t> list, list2;
-  ATC_TRY(list.alloc(g.m, s));
-  fox_scatter_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, fb, cursor.p, list.p);
+  ATC_TRY(list.alloc(g.e1 - g.e0, s));
+  fox_scatter_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, fb, cursor.p, list.p);
   ATC_CK(cudaGetLastError());
   *launches += 3;
   const int64_t* L = list.p;
   if (t && t->fox_rearrange) {
-    ATC_TRY(list2.alloc(g.m, s));
+    ATC_TRY(list2.alloc(g.e1 - g.e0, s));
     for (int b = 0; b < 6; ++b) {
       int64_t nb = (int64_t)h[b];
       if (nb == 0) continue;
@@ -365,12 +399,12 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
   ATC_TRY(counters.alloc(8, s));
   ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
-  const int64_t mi = max_items(g.n, g.m, std::min(sh.warp_chunk, sh.block_chunk));
+  const int64_t mi = max_items(g.n, g.e1 - g.e0, std::min(sh.warp_chunk, sh.block_chunk));
   DevBuf<GroupItem> witems, bitems;
   ATC_TRY(witems.alloc(mi, s));
   ATC_TRY(bitems.alloc(mi, s));
   // the partner range of u is its own CSR row
-  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, g.off, witems.p, bitems.p, counters.p, sh);
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, g.off, witems.p, bitems.p, counters.p, sh, g.e0, g.e1);
   ATC_CK(cudaGetLastError());
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
@@ -394,21 +428,22 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (g.n + 1), s));
   ATC_CK(cudaMemsetAsync(cur.p, 0, sizeof(int32_t) * g.n, s));
   ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
-  group_count_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, cnt.p);
+  group_count_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, cnt.p);
   ATC_CK(cudaGetLastError());
   ATC_TRY(exclusive_scan_i32_to_i64(cnt.p, gstart.p, g.n + 1, s));
   int64_t total = 0;
   ATC_CK(cudaMemcpyAsync(&total, gstart.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   ATC_TRY(plist.alloc(total + 32, s));
-  group_scatter_kernel<<<grid_for(g.m, 256), 256, 0, s>>>(g, gstart.p, cur.p, plist.p);
+  group_scatter_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gstart.p, cur.p, plist.p);
   ATC_CK(cudaGetLastError());
   // items: at most one per group plus one per chunk boundary
   int64_t max_items = g.n + total / std::min(sh.warp_chunk, sh.block_chunk) + 1;
   DevBuf<GroupItem> witems, bitems;
   ATC_TRY(witems.alloc(max_items, s));
   ATC_TRY(bitems.alloc(max_items, s));
-  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p, sh);
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p, sh, 0,
+                                                         INT64_MAX);
   ATC_CK(cudaGetLastError());
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
@@ -551,11 +586,12 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
   }
   esrc_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(off, n, esrc);
   ATC_CK(cudaGetLastError());
-  CsrView g{off, cols, esrc, n, m};
+  CsrView g = csr_view(off, cols, esrc, n, m);
   group_count_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, cnt);
   scan_one_block_kernel<<<1, 1024, 0, s>>>(cnt, n + 1, gstart);
   group_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, gstart, cur, plist);
-  group_items_kernel<<<grid_for(n, 256), 256, 0, s>>>(g, gstart, witems, bitems, counters, default_shape(32));
+  group_items_kernel<<<grid_for(n, 256), 256, 0, s>>>(g, gstart, witems, bitems, counters, default_shape(32), 0,
+                                                       INT64_MAX);
   ATC_CK(cudaGetLastError());
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
@@ -591,19 +627,17 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
 
 using namespace atc;
 
-extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint64_t* count,
-                             atc_stats* stats, atc_stream st) {
-  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
-  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
-  ATC_CHECK_ARG(kernel >= ATC_KERNEL_AUTO && kernel <= ATC_KERNEL_TRICORE, "unknown atc_kernel");
-  cudaStream_t s = as_stream(st);
-  *count = 0;
+// Counts the edges [e0, e1) of the CSR (every edge for the whole count).
+static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, int64_t e0, int64_t e1,
+                            uint64_t* count, atc_stats* stats, cudaStream_t s) {
   if (kernel == ATC_KERNEL_AUTO) kernel = ATC_KERNEL_BISSON;
   CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
   int launches = 0;
   EventTimer tm;
-  if (csr->m > 0) {
-    CsrView g{csr->offsets, csr->cols, pv->esrc, csr->n, csr->m};
+  if (e1 > e0) {
+    CsrView g = csr_view(csr->offsets, csr->cols, pv->esrc, csr->n, csr->m);
+    g.e0 = e0;
+    g.e1 = e1;
     unsigned long long* ctr = pv->counter;
     tm.start(s);
     ATC_CK(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
@@ -620,7 +654,7 @@ extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tu
     *count = h;
   }
   if (stats) {
-    stats->kernel_ms = csr->m > 0 ? tm.ms() : 0.0f;
+    stats->kernel_ms = e1 > e0 ? tm.ms() : 0.0f;
     stats->total_ms = stats->kernel_ms;
     stats->wedges = (uint64_t)csr->wedges;
     stats->alg_bytes = 4ull * (uint64_t)(csr->n + 1) + 4ull * (uint64_t)csr->m + 4ull * (uint64_t)csr->wedges + 8ull;
@@ -630,6 +664,47 @@ extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tu
     stats->launches = launches;
   }
   return ATC_OK;
+}
+
+extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint64_t* count,
+                             atc_stats* stats, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
+  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  ATC_CHECK_ARG(kernel >= ATC_KERNEL_AUTO && kernel <= ATC_KERNEL_TRICORE, "unknown atc_kernel");
+  *count = 0;
+  return tc_window(csr, kernel, tuning, 0, csr->m, count, stats, as_stream(st));
+}
+
+extern "C" atc_status atc_tc_part(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint32_t part,
+                                  uint32_t nparts, uint64_t* count, int64_t* edge_range, atc_stats* stats,
+                                  atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
+  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  ATC_CHECK_ARG(kernel >= ATC_KERNEL_AUTO && kernel <= ATC_KERNEL_TRICORE, "unknown atc_kernel");
+  ATC_CHECK_ARG(nparts >= 1 && part < nparts, "part must be in [0, nparts)");
+  cudaStream_t s = as_stream(st);
+  *count = 0;
+  int64_t b[2] = {0, csr->m};
+  if (nparts > 1 && csr->m > 0) {
+    CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+    CsrView g = csr_view(csr->offsets, csr->cols, pv->esrc, csr->n, csr->m);
+    DevBuf<int64_t> work, prefix, bounds;
+    ATC_TRY(work.alloc(csr->m + 1, s));
+    ATC_TRY(prefix.alloc(csr->m + 1, s));
+    ATC_TRY(bounds.alloc(2, s));
+    edge_work_kernel<<<grid_for(csr->m + 1, 256), 256, 0, s>>>(g, work.p);
+    ATC_CK(cudaGetLastError());
+    ATC_TRY(exclusive_scan_i64(work.p, prefix.p, csr->m + 1, s));
+    part_bounds_kernel<<<1, 32, 0, s>>>(prefix.p, csr->m, part, nparts, bounds.p);
+    ATC_CK(cudaGetLastError());
+    ATC_CK(cudaMemcpyAsync(b, bounds.p, sizeof(b), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+  }
+  if (edge_range) {
+    edge_range[0] = b[0];
+    edge_range[1] = b[1];
+  }
+  return tc_window(csr, kernel, tuning, b[0], b[1], count, stats, s);
 }
 
 extern "C" atc_status atc_tc_noalloc(const int64_t* offsets, const int32_t* cols, int64_t n, int64_t m,

@@ -254,6 +254,16 @@ atc_status atc_aorder(const int32_t* pairs, uint64_t n_pairs, int32_t* lookup, i
    Bisson/tc.cu:198-204, Fox/tc.cu:334-384, tricount_gpu.cu:337-408. */
 atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning,
                   uint64_t* count, atc_stats* stats, atc_stream s);
+/* One part of the triangle count: the edges of the CSR are cut into `nparts` contiguous
+   ranges of equal work (sum over the edges of min(outdeg u, outdeg v) + 1) and this call
+   counts the triangles sum_{(u,v) in part} |N+(u) ∩ N+(v)| of range `part`, so the counts
+   of parts 0..nparts-1 add up to atc_tc's.  It is the sharding unit of a count spread over
+   several GPUs (each holding the CSR, one uint64 sum at the end), the partitioned
+   counting the reference leaves to TriCore's vertex-range parts
+   (tricore/src/tricount_gpu.cu:347-406).  edge_range (nullable, 2 entries) receives
+   [first, last) edge of the part.  stats describe the whole CSR except kernel_ms. */
+atc_status atc_tc_part(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint32_t part,
+                       uint32_t nparts, uint64_t* count, int64_t* edge_range, atc_stats* stats, atc_stream s);
 /* Triangle count of an oriented CSR given as plain device arrays, computed without
    allocating any device memory.  No counterpart in the reference: it is for callers
    that cannot call cudaMalloc (capture of a CUDA graph in a mode that forbids

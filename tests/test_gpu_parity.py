@@ -135,9 +135,17 @@ def test_tuning_knobs_do_not_change_counts():
     want = oracle.tc_count(g)
     csr = atc.pretc(g, atc.Dir.ID)  # id orientation: long lists, hubs
     for t in ({"bisson_cutover": 8}, {"bisson_cutover": 64}, {"fox_rearrange": 1}, {"fox_work_per_thread": 4},
-              {"hu_blocks": 7}, {"tricore_blocks": 3}, {"hu_blocks": 2000}):
+              {"hu_blocks": 7}, {"tricore_blocks": 3}, {"hu_blocks": 2000}, {"bisson_slots": 1},
+              {"bisson_slots": 2}, {"bisson_slots": 4}, {"bisson_slots": 2, "bisson_warp_max": 64, "bisson_cutover": 4}):
         for k in KERNELS:
             assert atc.tc(csr, k, tuning=t)[0] == want, (t, k.name)
+
+
+def test_bad_slot_count_rejected():
+    csr = atc.pretc(atc.rmat_graph(8, 8, 1), atc.Dir.DEGREE)
+    for k in (atc.Kernel.BISSON, atc.Kernel.HU):
+        with pytest.raises(atc.ATCError):
+            atc.tc(csr, k, tuning={"bisson_slots": 3})
 
 
 # ---- CSR layout ----------------------------------------------------------------------------
