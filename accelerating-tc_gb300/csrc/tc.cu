@@ -20,8 +20,7 @@
 //   TriCore-style tricount_gpu.cu:215-290  warp per edge; 32 pivots of the longer list
 //                                        in shared memory bracket each element of the
 //                                        shorter list, then a binary search inside the
-//                                        bracket (in a shared-memory copy of the longer
-//                                        list when it fits).
+//                                        bracket.
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -89,60 +88,38 @@ __global__ void part_bounds_kernel(const int64_t* prefix, int64_t m, uint32_t pa
 }
 
 // ============================== TriCore-style ======================================
-// A warp per edge (tricount_gpu.cu:215-290): 32 pivots of the longer list A sit in the
-// warp's shared slot and bracket each element of the shorter list, which is then found by
-// a binary search inside its bracket.  The warp also copies A into its shared stage when
-// A fits (at most `stage` ints), so the bracket searches run in shared memory instead of
-// as chains of dependent global loads; a warp walks chunks of kTriChunk consecutive
-// edges, which mostly share their source, and keeps A staged while it stays the same list.
 constexpr int kTriWarps = 8;
-constexpr int kTriChunk = 16;
-constexpr int kTriStageMax = 2048;  // ints of A staged per warp at most (8 KB)
 
-__global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, int stage, unsigned long long* out) {
-  extern __shared__ int32_t tri_stage[];  // kTriWarps * stage
+__global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsigned long long* out) {
   __shared__ int32_t piv[kTriWarps][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int32_t* S = tri_stage + (size_t)w * stage;
-  const int32_t* staged = nullptr;  // global list held in S
   unsigned long long cnt = 0;
   const int64_t warps = (int64_t)gridDim.x * kTriWarps;
-  const int64_t chunks = (g.e1 - g.e0 + kTriChunk - 1) / kTriChunk;
-  for (int64_t c = (int64_t)blockIdx.x * kTriWarps + w; c < chunks; c += warps) {
-    const int64_t eb = g.e0 + c * kTriChunk, ee = min(eb + kTriChunk, g.e1);
-    for (int64_t e = eb; e < ee; ++e) {
-      const int32_t u = g.esrc[e], v = g.cols[e];
-      const int64_t au = g.off[u], du = g.off[u + 1] - au;
-      const int64_t av = g.off[v], dv = g.off[v + 1] - av;
-      const int32_t* A = g.cols + (du >= dv ? au : av);
-      const int32_t* Bl = g.cols + (du >= dv ? av : au);
-      const int64_t da = du >= dv ? du : dv, db = du >= dv ? dv : du;
-      if (db == 0) continue;
-      const bool fits = da <= stage;
-      if (fits && A != staged) {
-        __syncwarp();
-        for (int64_t j = lane; j < da; j += 32) S[j] = __ldg(A + j);
-        staged = A;
+  for (int64_t e = g.e0 + (int64_t)blockIdx.x * kTriWarps + w; e < g.e1; e += warps) {
+    int32_t u = g.esrc[e], v = g.cols[e];
+    int64_t au = g.off[u], du = g.off[u + 1] - au;
+    int64_t av = g.off[v], dv = g.off[v + 1] - av;
+    const int32_t* A = g.cols + (du >= dv ? au : av);
+    const int32_t* Bl = g.cols + (du >= dv ? av : au);
+    int64_t da = du >= dv ? du : dv, db = du >= dv ? dv : du;
+    if (db == 0) continue;
+    piv[w][lane] = A[(int64_t)lane * da / 32];
+    __syncwarp();
+    for (int64_t j = lane; j < db; j += 32) {
+      int32_t x = Bl[j];
+      // k = number of pivots <= x
+      int lo = 0, hi = 32;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (piv[w][mid] <= x) lo = mid + 1; else hi = mid;
       }
-      const int32_t* Aq = fits ? S : A;
-      __syncwarp();
-      piv[w][lane] = Aq[(int64_t)lane * da / 32];
-      __syncwarp();
-      for (int64_t j = lane; j < db; j += 32) {
-        const int32_t x = __ldg(Bl + j);
-        // k = number of pivots <= x
-        int lo = 0, hi = 32;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (piv[w][mid] <= x) lo = mid + 1; else hi = mid;
-        }
-        if (lo == 0) continue;  // x < A[0]
-        if (piv[w][lo - 1] == x) { ++cnt; continue; }
-        const int64_t b = (int64_t)(lo - 1) * da / 32 + 1;  // strictly inside the bracket
-        const int64_t e2 = lo == 32 ? da : (int64_t)lo * da / 32;
-        if (b < e2 && bsearch_has(Aq + b, e2 - b, x)) ++cnt;
-      }
+      if (lo == 0) continue;                 // x < A[0]
+      if (piv[w][lo - 1] == x) { ++cnt; continue; }
+      int64_t b = (int64_t)(lo - 1) * da / 32 + 1;  // strictly inside the bracket
+      int64_t e2 = lo == 32 ? da : (int64_t)lo * da / 32;
+      if (b < e2 && bsearch_has(A + b, e2 - b, x)) ++cnt;
     }
+    __syncwarp();
   }
   warp_add_count(cnt, out);
 }
@@ -256,15 +233,11 @@ __global__ void fox_deal_kernel(const uint64_t* keys, const int64_t* list, int64
 }  // namespace
 
 // ---- family drivers ----------------------------------------------------------------
-static atc_status run_tricore(const CsrView& g, const atc_tuning* t, int64_t max_outdeg, unsigned long long* ctr,
-                              cudaStream_t s, int* launches) {
-  // stage: the longest list, rounded to whole warps, up to kTriStageMax ints per warp
-  const int stage = (int)std::min<int64_t>((std::max<int64_t>(max_outdeg, 1) + 31) & ~31ll, kTriStageMax);
-  const size_t smem = sizeof(int32_t) * (size_t)stage * kTriWarps;
-  ATC_CK(cudaFuncSetAttribute((const void*)tricore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+static atc_status run_tricore(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
+                              int* launches) {
   int grid = t && t->tricore_blocks > 0 ? t->tricore_blocks
-                                        : sm_count() * blocks_per_sm((const void*)tricore_kernel, kTriWarps * 32, smem);
-  tricore_kernel<<<grid, kTriWarps * 32, smem, s>>>(g, stage, ctr);
+                                        : sm_count() * blocks_per_sm((const void*)tricore_kernel, kTriWarps * 32, 0);
+  tricore_kernel<<<grid, kTriWarps * 32, 0, s>>>(g, ctr);
   ATC_CK(cudaGetLastError());
   *launches += 1;
   return ATC_OK;
@@ -672,7 +645,7 @@ static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tun
       case ATC_KERNEL_HU: ATC_TRY(run_hu(g, tuning, ctr, s, &launches)); break;
       case ATC_KERNEL_BISSON: ATC_TRY(run_bisson(g, tuning, ctr, s, &launches)); break;
       case ATC_KERNEL_FOX: ATC_TRY(run_fox(g, tuning, ctr, s, &launches)); break;
-      default: ATC_TRY(run_tricore(g, tuning, csr->max_outdeg, ctr, s, &launches)); break;
+      default: ATC_TRY(run_tricore(g, tuning, ctr, s, &launches)); break;
     }
     tm.stop(s);
     unsigned long long h = 0;
