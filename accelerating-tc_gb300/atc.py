@@ -146,6 +146,8 @@ _SIGS = {
     "atc_read_edges": (C.c_int, [C.c_char_p, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "atc_csr_save": (C.c_int, [C.POINTER(CSRStruct), C.c_char_p, _P]),
     "atc_csr_load": (C.c_int, [C.c_char_p, C.POINTER(CSRStruct), _P]),
+    "atc_csr_load_host": (C.c_int, [C.c_char_p, C.POINTER(CSRStruct), _P]),
+    "atc_csr_host_resident": (C.c_int, [C.POINTER(CSRStruct), _P]),
     "atc_adirection": (C.c_int, [_P, C.c_uint64, _P, C.POINTER(C.c_uint64), _P, _P]),
     "atc_aorder": (C.c_int, [_P, C.c_uint64, _P, _P, _P, _P]),
     "atc_relabel": (C.c_int, [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]),
@@ -305,10 +307,17 @@ class CSR:
         _check(lib().atc_csr_save(C.byref(self._st), os.fsencode(path), stream))
 
     @staticmethod
-    def load(path, stream=None):
+    def load(path, stream=None, host_resident=False):
+        """Loads a CSR cache file; host_resident: edge arrays in mapped host memory."""
         st = CSRStruct()
-        _check(lib().atc_csr_load(os.fsencode(path), C.byref(st), stream))
+        f = lib().atc_csr_load_host if host_resident else lib().atc_csr_load
+        _check(f(os.fsencode(path), C.byref(st), stream))
         return CSR(st)
+
+    def to_host_resident(self, stream=None):
+        """Moves the edge arrays to pinned host memory read by the kernels in place."""
+        _check(lib().atc_csr_host_resident(C.byref(self._st), stream))
+        return self
 
     def free(self):
         if self._st is not None and self._st.offsets is not None:

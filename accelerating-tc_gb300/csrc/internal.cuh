@@ -77,6 +77,10 @@ struct CsrPriv {
   int32_t* esrc = nullptr;       // m: source vertex of every edge, in edge order
   unsigned long long* counter = nullptr;  // 2 x u64 scratch for counting kernels
   int bits = 1;
+  // cols and esrc live in pinned host memory mapped into the device's address space
+  // (atc_csr_host_resident / atc_csr_load_host); these are the host allocations
+  int32_t* host_cols = nullptr;
+  int32_t* host_esrc = nullptr;
 };
 
 }  // namespace atc

@@ -469,18 +469,24 @@ extern "C" atc_status atc_csr_to_host(const atc_csr* csr, int64_t* offsets, int3
   ATC_CHECK_ARG(csr != nullptr && offsets != nullptr && cols != nullptr, "NULL argument");
   cudaStream_t st = as_stream(s);
   ATC_CK(cudaMemcpyAsync(offsets, csr->offsets, sizeof(int64_t) * (csr->n + 1), cudaMemcpyDeviceToHost, st));
-  if (csr->m) ATC_CK(cudaMemcpyAsync(cols, csr->cols, sizeof(int32_t) * csr->m, cudaMemcpyDeviceToHost, st));
+  if (csr->m) ATC_CK(cudaMemcpyAsync(cols, csr->cols, sizeof(int32_t) * csr->m, cudaMemcpyDefault, st));
   ATC_CK(cudaStreamSynchronize(st));
   return ATC_OK;
 }
 
 extern "C" atc_status atc_csr_free(atc_csr* csr) {
   if (!csr) return ATC_OK;
+  CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+  const bool host = pv && pv->host_cols;
   if (csr->offsets) cudaFree(csr->offsets);
-  if (csr->cols) cudaFree(csr->cols);
-  if (csr->priv) {
-    CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
-    if (pv->esrc) cudaFree(pv->esrc);
+  if (host) {
+    cudaFreeHost(pv->host_cols);
+    if (pv->host_esrc) cudaFreeHost(pv->host_esrc);
+  } else {
+    if (csr->cols) cudaFree(csr->cols);
+    if (pv && pv->esrc) cudaFree(pv->esrc);
+  }
+  if (pv) {
     if (pv->counter) cudaFree(pv->counter);
     delete pv;
   }
@@ -653,6 +659,39 @@ __global__ void csr_fill_esrc_kernel(const int64_t* off, int64_t n, int32_t* esr
     for (int64_t j = off[u] + lane; j < off[u + 1]; j += 32) esrc[j] = (int32_t)u;
 }
 static const char kCsrMagic[8] = {'A', 'T', 'C', 'C', 'S', 'R', '0', '1'};
+
+// int32 array in pinned host memory mapped into the device's address space: `host` for
+// the CPU, `dev` for kernels (the same address under unified addressing).
+struct HostMapped {
+  int32_t* host = nullptr;
+  int32_t* dev = nullptr;
+  atc_status alloc(int64_t count) {
+    void* p = nullptr;
+    cudaError_t e = cudaHostAlloc(&p, sizeof(int32_t) * (size_t)std::max<int64_t>(count, 1),
+                                  cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      set_error("cudaHostAlloc of %lld ints: %s", (long long)count, cudaGetErrorString(e));
+      return ATC_ERR_OOM;
+    }
+    host = static_cast<int32_t*>(p);
+    void* d = nullptr;
+    e = cudaHostGetDevicePointer(&d, p, 0);
+    if (e != cudaSuccess) {
+      set_error("cudaHostGetDevicePointer: %s", cudaGetErrorString(e));
+      return ATC_ERR_CUDA;
+    }
+    dev = static_cast<int32_t*>(d);
+    return ATC_OK;
+  }
+  int32_t* release() {
+    int32_t* p = host;
+    host = dev = nullptr;
+    return p;
+  }
+  ~HostMapped() {
+    if (host) cudaFreeHost(host);
+  }
+};
 }  // namespace atc
 
 extern "C" atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_stream st) {
@@ -678,9 +717,8 @@ extern "C" atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_str
   return ATC_OK;
 }
 
-extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st) {
+static atc_status csr_load_impl(const char* path, bool host_resident, atc_csr* out, cudaStream_t s) {
   ATC_CHECK_ARG(path != nullptr && out != nullptr, "NULL argument");
-  cudaStream_t s = as_stream(st);
   *out = atc_csr{};
   FILE* f = fopen(path, "rb");
   if (!f) {
@@ -717,24 +755,45 @@ extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st
   DevBuf<int64_t> doff;
   DevBuf<int32_t> dcols, desrc;
   DevBuf<unsigned long long> counter;
+  HostMapped hcols, hesrc;
   ATC_TRY(doff.alloc(n + 1, s));
-  ATC_TRY(dcols.alloc(m + 16, s));
-  ATC_TRY(desrc.alloc(m + 16, s));
   ATC_TRY(counter.alloc(4, s));
   ATC_CK(cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s));
-  ATC_CK(cudaMemsetAsync(dcols.p + m, 0, sizeof(int32_t) * 16, s));
-  if (m) ATC_CK(cudaMemcpyAsync(dcols.p, cols.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
-  if (n) atc::csr_fill_esrc_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(doff.p, n, desrc.p);
+  int32_t* cols_dev;
+  int32_t* esrc_dev;
+  if (host_resident) {
+    ATC_TRY(hcols.alloc(m + 16));
+    ATC_TRY(hesrc.alloc(m + 16));
+    std::copy(cols.begin(), cols.end(), hcols.host);
+    std::fill(hcols.host + m, hcols.host + m + 16, 0);
+    cols_dev = hcols.dev;
+    esrc_dev = hesrc.dev;
+  } else {
+    ATC_TRY(dcols.alloc(m + 16, s));
+    ATC_TRY(desrc.alloc(m + 16, s));
+    ATC_CK(cudaMemsetAsync(dcols.p + m, 0, sizeof(int32_t) * 16, s));
+    if (m) ATC_CK(cudaMemcpyAsync(dcols.p, cols.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
+    cols_dev = dcols.p;
+    esrc_dev = desrc.p;
+  }
+  if (n) atc::csr_fill_esrc_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(doff.p, n, esrc_dev);
   ATC_CK(cudaGetLastError());
   ATC_CK(cudaStreamSynchronize(s));
   CsrPriv* pv = new CsrPriv();
-  pv->esrc = desrc.detach();
+  if (host_resident) {
+    pv->host_cols = hcols.release();
+    pv->host_esrc = hesrc.release();
+    pv->esrc = esrc_dev;
+    out->cols = cols_dev;
+  } else {
+    pv->esrc = desrc.detach();
+    out->cols = dcols.detach();
+  }
   pv->counter = counter.detach();
   pv->bits = id_bits(n);
   out->n = n;
   out->m = m;
   out->offsets = doff.detach();
-  out->cols = dcols.detach();
   out->n_input = h64[2];
   out->wedges = h64[3];
   out->wedges_min = h64[4];
@@ -743,5 +802,35 @@ extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st
   out->pruned = h32[2];
   out->max_outdeg = h32[3];
   out->priv = pv;
+  return ATC_OK;
+}
+
+extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st) {
+  return csr_load_impl(path, false, out, as_stream(st));
+}
+
+extern "C" atc_status atc_csr_load_host(const char* path, atc_csr* out, atc_stream st) {
+  return csr_load_impl(path, true, out, as_stream(st));
+}
+
+extern "C" atc_status atc_csr_host_resident(atc_csr* csr, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr, "csr is NULL");
+  ATC_CHECK_ARG(csr->priv != nullptr, "csr was not built by atc_pretc or atc_csr_load");
+  CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+  if (pv->host_cols) return ATC_OK;
+  cudaStream_t s = as_stream(st);
+  const int64_t m = csr->m;
+  HostMapped hcols, hesrc;
+  ATC_TRY(hcols.alloc(m + 16));
+  ATC_TRY(hesrc.alloc(m + 16));
+  ATC_CK(cudaMemcpyAsync(hcols.host, csr->cols, sizeof(int32_t) * (m + 16), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaMemcpyAsync(hesrc.host, pv->esrc, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  cudaFree(csr->cols);
+  cudaFree(pv->esrc);
+  csr->cols = hcols.dev;
+  pv->esrc = hesrc.dev;
+  pv->host_cols = hcols.release();
+  pv->host_esrc = hesrc.release();
   return ATC_OK;
 }

@@ -204,6 +204,16 @@ atc_status atc_read_edges(const char* path, int32_t* pairs, uint64_t cap, uint64
    atc_csr_load validates the arrays (ATC_ERR_INVALID for a file that is not a CSR). */
 atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_stream s);
 atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream s);
+/* Graphs larger than device memory (TriCore's out-of-core parts,
+   tricore/src/tricount_gpu.cu:337-408, copy vertex-range parts of the CSR to the device
+   pair by pair).  Here the CSR's edge arrays (cols and the per-edge source array, 8 bytes
+   per edge) move into pinned host memory mapped into the device's address space, only the
+   offsets stay on the device, and every kernel reads the lists over the CPU-GPU link
+   (NVLink-C2C on Grace-Blackwell) in place; atc_tc_part bounds the counting scratch.
+   atc_csr_host_resident moves a CSR built on the device; atc_csr_load_host loads a cache
+   file straight into host memory.  atc_csr_free releases either kind. */
+atc_status atc_csr_host_resident(atc_csr* csr, atc_stream s);
+atc_status atc_csr_load_host(const char* path, atc_csr* out, atc_stream s);
 
 /* ---- orientation and ordering as drop-ins for the reference programs ------------ */
 /* A-direction-seri <file> (edge_directing/A-direction-seri.cpp:170-288): writes the
