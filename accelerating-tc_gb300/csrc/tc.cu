@@ -177,7 +177,8 @@ __global__ void fox_scatter_kernel(CsrView g, FoxBins fb, unsigned long long* cu
 }
 
 // T threads per edge (Fox/tc.cu:64-125): each thread takes every T-th element of the
-// shorter list and binary-searches it in the longer list.
+// shorter list and searches it in the longer list (exponential search from the previous
+// element's position, then binary search).
 template <int T>
 __global__ void __launch_bounds__(256) fox_kernel(CsrView g, const int64_t* list, int64_t cnt_edges,
                                                   unsigned long long* out) {
@@ -193,7 +194,25 @@ __global__ void __launch_bounds__(256) fox_kernel(CsrView g, const int64_t* list
     const int32_t* L = g.cols + (du >= dv ? au : av);   // longer
     const int32_t* S = g.cols + (du >= dv ? av : au);   // shorter
     int64_t dl = du >= dv ? du : dv, ds = du >= dv ? dv : du;
-    for (int64_t j = sub; j < ds; j += T) cnt += bsearch_has(L, dl, S[j]);
+    // a thread's elements ascend, so each search resumes where the previous one ended:
+    // gallop forward from there, then binary-search the last step
+    int64_t lo = 0;
+    for (int64_t j = sub; j < ds; j += T) {
+      const int32_t x = __ldg(S + j);
+      int64_t a = lo, b = lo, step = 1;  // every L[i], i < a, is < x
+      while (b < dl && __ldg(L + b) < x) {
+        a = b + 1;
+        b = a + step;
+        step <<= 1;
+      }
+      if (b > dl) b = dl;
+      while (a < b) {  // L[b] >= x or b == dl
+        const int64_t mid = (a + b) >> 1;
+        if (__ldg(L + mid) < x) a = mid + 1; else b = mid;
+      }
+      cnt += a < dl && __ldg(L + a) == x;
+      lo = a;
+    }
   }
   warp_add_count(cnt, out);
 }
