@@ -105,8 +105,11 @@ __global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsi
     if (db == 0) continue;
     piv[w][lane] = A[(int64_t)lane * da / 32];
     __syncwarp();
+    // a lane's elements ascend: `prev` = where its previous element's search ended, a
+    // lower bound for the next one inside any bracket
+    int64_t prev = 0;
     for (int64_t j = lane; j < db; j += 32) {
-      int32_t x = Bl[j];
+      int32_t x = __ldg(Bl + j);
       // k = number of pivots <= x
       int lo = 0, hi = 32;
       while (lo < hi) {
@@ -117,7 +120,13 @@ __global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsi
       if (piv[w][lo - 1] == x) { ++cnt; continue; }
       int64_t b = (int64_t)(lo - 1) * da / 32 + 1;  // strictly inside the bracket
       int64_t e2 = lo == 32 ? da : (int64_t)lo * da / 32;
-      if (b < e2 && bsearch_has(A + b, e2 - b, x)) ++cnt;
+      if (prev > b) b = prev;
+      while (b < e2) {  // lower bound of x in A[b, e2)
+        const int64_t mid = (b + e2) >> 1;
+        if (__ldg(A + mid) < x) b = mid + 1; else e2 = mid;
+      }
+      cnt += b < da && __ldg(A + b) == x;
+      prev = b;
     }
     __syncwarp();
   }
