@@ -218,53 +218,71 @@ struct CompactItems {
   }
 };
 
-// Vertex-centric grouping passes for a CSR without the per-edge source array: a warp
-// per source vertex, lanes over its out-edges (same grouping rule as above).
-__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt) {
+// Grouping passes for a CSR without the per-edge source array.  A warp takes a block of
+// 32 consecutive rows, whose edges are contiguous in cols, and deals them 32 per round;
+// each lane finds the row of its edge by a 5-step search over the lanes' row starts,
+// done with shuffles.  Every lane has an edge in every round but the last, whatever the
+// row lengths (a warp per row would leave most lanes idle on short rows).  Same grouping
+// rule as the per-edge passes.  f(u, v, du, dv, valid) is called by all 32 lanes.
+template <class F>
+__device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < g.n; u += warps) {
-    const int64_t ub = g.off[u], du = g.off[u + 1] - ub;
-    if (du == 0) continue;
-    for (int64_t base = 0; base < du; base += 32) {
-      int32_t h = -1;
-      if (base + lane < du) {
-        int32_t v = g.cols[ub + base + lane];
-        int64_t dv = g.off[v + 1] - g.off[v];
-        if (dv > 0) h = longer_is_u((int32_t)u, v, du, dv) ? (int32_t)u : v;
+  const int64_t blocks = (g.n + 31) >> 5;
+  for (int64_t rb = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; rb < blocks; rb += warps) {
+    const int64_t u0 = rb << 5;
+    const int64_t row = u0 + lane;
+    const int64_t last = min(u0 + 32, g.n);
+    const int64_t start = __ldg(g.off + min(row, last));  // rows past the end start at the block's end
+    const int64_t stop = __shfl_sync(0xffffffffu, __ldg(g.off + last), 0);
+    const int64_t first = __shfl_sync(0xffffffffu, start, 0);
+    for (int64_t t0 = first; t0 < stop; t0 += 32) {
+      const int64_t e = t0 + lane;
+      // k = the last lane whose row starts at or before e
+      int k = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int64_t sk = __shfl_sync(0xffffffffu, start, k + step);
+        if (sk <= e) k += step;
       }
-      unsigned same = __match_any_sync(0xffffffffu, h);
-      int lead = __ffs(same) - 1;
-      if (h >= 0 && lane == lead) atomicAdd(&cnt[h], __popc(same));
+      const int64_t su = __shfl_sync(0xffffffffu, start, k);
+      const int64_t eu = __shfl_sync(0xffffffffu, start, (k + 1) & 31);
+      const bool valid = e < stop;
+      int32_t u = (int32_t)(u0 + k), v = 0;
+      int64_t du = (k == 31 ? stop : eu) - su, dv = 0;
+      if (valid) {
+        v = __ldg(g.cols + e);
+        dv = __ldg(g.off + v + 1) - __ldg(g.off + v);
+      }
+      f(u, v, du, dv, valid && du > 0 && dv > 0);
     }
   }
 }
 
+__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt) {
+  for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
+    const int32_t h = ok ? (longer_is_u(u, v, du, dv) ? u : v) : -1;
+    const unsigned same = __match_any_sync(0xffffffffu, h);
+    if (h >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&cnt[h], __popc(same));
+  });
+}
+
 __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < g.n; u += warps) {
-    const int64_t ub = g.off[u], du = g.off[u + 1] - ub;
-    if (du == 0) continue;
-    for (int64_t base = 0; base < du; base += 32) {
-      int32_t h = -1, p = 0;
-      if (base + lane < du) {
-        int32_t v = g.cols[ub + base + lane];
-        int64_t dv = g.off[v + 1] - g.off[v];
-        if (dv > 0) {
-          bool hu = longer_is_u((int32_t)u, v, du, dv);
-          h = hu ? (int32_t)u : v;
-          p = hu ? v : (int32_t)u;
-        }
-      }
-      unsigned same = __match_any_sync(0xffffffffu, h);
-      int lead = __ffs(same) - 1;
-      int at = 0;
-      if (h >= 0 && lane == lead) at = atomicAdd(&cur[h], __popc(same));
-      at = __shfl_sync(0xffffffffu, at, lead);
-      if (h >= 0) plist[gstart[h] + at + __popc(same & ((1u << lane) - 1))] = p;
+  for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
+    int32_t h = -1, p = 0;
+    if (ok) {
+      const bool hu = longer_is_u(u, v, du, dv);
+      h = hu ? u : v;
+      p = hu ? v : u;
     }
-  }
+    const unsigned same = __match_any_sync(0xffffffffu, h);
+    const int lead = __ffs(same) - 1;
+    int at = 0;
+    if (h >= 0 && lane == lead) at = atomicAdd(&cur[h], __popc(same));
+    at = __shfl_sync(0xffffffffu, at, lead);
+    if (h >= 0) plist[gstart[h] + at + __popc(same & ((1u << lane) - 1))] = p;
+  });
 }
 
 // Compact items: counters[0] warp items (front), counters[1] block items (back),

@@ -424,6 +424,9 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
   ItemShape sh;
   int slots;
   ATC_TRY(item_shape(t, &sh, &slots));
+  // the sorted copy only for N+(u) of at most 8 (every N+(v) is searched in it; the hash
+  // takes one probe): 4 % faster than 32 at R-MAT scale 24
+  if (!t || t->bisson_cutover <= 0) sh.cutover = 8;
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
   ATC_TRY(counters.alloc(8, s));
   ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
