@@ -53,6 +53,7 @@ constexpr int kWarpChunk = 512;     // partners per warp item
 constexpr int kBlockChunk = 2048;   // partners per block item
 constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
 constexpr int kHashMax = kTabWords / 4;
+constexpr int kWarpGrab = 4;     // warp items taken per atomic
 constexpr int kDefaultSlots = 4;  // hash slots per bucket unless tuned (one 16-byte shared load)
 
 struct GroupItem {
@@ -191,11 +192,13 @@ __global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* 
 // warp items from the front of one array and block items from its back, decoded with
 // the group starts and the item shape.
 struct FullItems {
+  static constexpr bool kBatch = false;  // one graph: counts go to the kernel's counter
   const GroupItem* p;
   __device__ __forceinline__ GroupItem get(const CsrView&, int i) const { return p[i]; }
 };
 
 struct CompactItems {
+  static constexpr bool kBatch = true;  // a batch: counts go to each item's graph
   const int2* p;
   const int64_t* gstart;
   int64_t cap;
@@ -328,12 +331,33 @@ __device__ __forceinline__ int graph_of(const GraphTags& t, int64_t v) {
   return lo;
 }
 
-// Adds a warp's per-lane partial of one item to its graph (all 32 lanes call this).
-__device__ __forceinline__ void add_item_to_graph(const GraphTags& t, int64_t h, unsigned part) {
-  unsigned long long c = part;
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&t.counts[graph_of(t, h)], c);
-}
+// Per-warp attribution of counts to the graphs of a batch.  The warp keeps the graph of
+// its last item and that graph's vertex range, adds its lanes' hits to a running partial,
+// and flushes the partial (one shuffle reduction, one atomic) only when an item of another
+// graph comes or the kernel ends.  A warp takes items in increasing index order, which is
+// vertex order, so the graph lookup (a binary search over the graph starts) runs about
+// once per graph instead of once per item.  All 32 lanes call add/flush; h is the same
+// on every lane.
+struct GraphAcc {
+  int g = -1;
+  int64_t lo = 0, hi = 0;
+  unsigned long long part = 0;
+  __device__ __forceinline__ void flush(const GraphTags& t) {
+    unsigned long long c = part;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c && g >= 0) atomicAdd(&t.counts[g], c);
+    part = 0;
+  }
+  __device__ __forceinline__ void add(const GraphTags& t, int64_t h, unsigned c) {
+    if (h < lo || h >= hi) {
+      flush(t);
+      g = graph_of(t, h);
+      lo = t.vbase[g];
+      hi = t.vbase[g + 1];
+    }
+    part += c;
+  }
+};
 
 // Hash tables of N+(h): linear probing over buckets of S slots (S = 1, 2 or 4; 4-, 8- or
 // 16-byte aligned), empty slots hold -1.  The home bucket of x is given by Fibonacci
@@ -559,14 +583,21 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
   for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
   __syncwarp();
   unsigned long long total = 0;
+  GraphAcc acc;
   int32_t* T = tab[w];
   if (nitems_dev) nitems = *nitems_dev;
+  // batch items are taken kWarpGrab at a time (one atomic): most of them are tiny
+  constexpr int grab = Items::kBatch ? kWarpGrab : 1;
+  int it = 0, it_end = 0;
   for (;;) {
-    int it = 0;
-    if (lane == 0) it = atomicAdd(next, 1);
-    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it == it_end) {
+      int first = 0;
+      if (lane == 0) first = atomicAdd(next, grab);
+      it = __shfl_sync(0xffffffffu, first, 0);
+      it_end = min(it + grab, nitems);
+    }
     if (it >= nitems) break;
-    const GroupItem gi = items.get(g, it);
+    const GroupItem gi = items.get(g, it++);
     const int64_t hb = g.off[gi.h];
     const int dh = (int)(g.off[gi.h + 1] - hb);
     int64_t cur = gi.b;
@@ -599,9 +630,10 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
       for (int j = lane; j < dh; j += 32) hash_erase<S>(T, mask, __ldg(g.cols + hb + j));
     }
     __syncwarp();
-    if (tags.counts) add_item_to_graph(tags, gi.h, cnt);
+    if constexpr (Items::kBatch) acc.add(tags, gi.h, cnt);
     else total += cnt;
   }
+  if constexpr (Items::kBatch) acc.flush(tags);
   warp_add_count(total, out);
 }
 
@@ -618,6 +650,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t j = threadIdx.x; j < tab_words; j += blockDim.x) tab[j] = -1;
   unsigned long long total = 0;
+  GraphAcc acc;
   if (nitems_dev) nitems = *nitems_dev;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -679,9 +712,10 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
     }
     __syncthreads();
-    if (tags.counts) add_item_to_graph(tags, gi.h, cnt);
+    if constexpr (Items::kBatch) acc.add(tags, gi.h, cnt);
     else total += cnt;
   }
+  if constexpr (Items::kBatch) acc.flush(tags);
   warp_add_count(total, out);
 }
 
