@@ -77,7 +77,8 @@ class Tuning(C.Structure):
         ("bisson_warp_chunk", C.c_int32),
         ("bisson_block_chunk", C.c_int32),
         ("bisson_slots", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("group_by_source", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 

@@ -171,7 +171,7 @@ namespace {
 
 bool same_shape(const ItemShape& a, const ItemShape& b) {
   return a.cutover == b.cutover && a.warp_max == b.warp_max && a.warp_chunk == b.warp_chunk &&
-         a.block_chunk == b.block_chunk;
+         a.block_chunk == b.block_chunk && a.by_source == b.by_source;
 }
 
 ItemShape shape_from(const atc_tuning* t, const ItemShape& base) {
@@ -181,6 +181,7 @@ ItemShape shape_from(const atc_tuning* t, const ItemShape& base) {
   if (t->bisson_warp_max > 0) sh.warp_max = std::min(t->bisson_warp_max, kWarpMax);
   if (t->bisson_warp_chunk > 0) sh.warp_chunk = t->bisson_warp_chunk;
   if (t->bisson_block_chunk > 0) sh.block_chunk = t->bisson_block_chunk;
+  if (t->group_by_source > 0) sh.by_source = 1;
   if (sh.cutover > sh.warp_max) sh.cutover = sh.warp_max;
   return sh;
 }
@@ -242,9 +243,10 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   cudaMemsetAsync(b->cur, 0, sizeof(int32_t) * (n + 1), c);
   cudaMemsetAsync(b->counters, 0, sizeof(int) * 8, c);
   cudaMemsetAsync(b->gcounts, 0, sizeof(unsigned long long) * ng, c);
-  group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt);
+  group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt, sh.by_source);
   exclusive_scan_i32_to_i64_tmp(b->scan_tmp, &bytes, b->cnt, b->gstart, (size_t)n + 1, c);
-  group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist);
+  group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist,
+                                                                     sh.by_source);
   group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->gstart, b->items, cap_items, b->counters, sh);
   bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(g, b->plist, bitems, 0, b->counters + 1,
                                                                             b->counters + 5, words, tags, b->gcounts);
@@ -297,7 +299,7 @@ extern "C" atc_status atc_batch_run(atc_batch* b, const atc_tuning* t, uint64_t*
     memset(stats, 0, sizeof(*stats));
     stats->kernel_ms = ms;
     stats->total_ms = ms;
-    stats->kernel_used = ATC_KERNEL_BISSON;
+    stats->kernel_used = sh.by_source ? ATC_KERNEL_HU : ATC_KERNEL_BISSON;
     stats->launches = 6;
   }
   return ATC_OK;

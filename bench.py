@@ -521,7 +521,7 @@ def run_batch(a):
     ng, n_all, m_all = batch.info()
     cands = [{}, {"bisson_warp_max": 128}, {"bisson_warp_max": 64, "bisson_cutover": 16},
              {"bisson_warp_chunk": 256, "bisson_block_chunk": 1024}, {"bisson_warp_chunk": 2048, "bisson_block_chunk": 8192},
-             {"bisson_cutover": 64}]
+             {"bisson_cutover": 64}, {"group_by_source": 1}, {"group_by_source": 1, "bisson_cutover": 8}]
     best, tune_ms = batch.tune(cands, stream=sp)
     counts, _ = batch.run(stream=sp)
     assert counts.tolist() == plain_counts, "batched and per-graph counts differ"
