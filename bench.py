@@ -487,12 +487,17 @@ def run_batch(a):
     plain_counts = []
     dirs = []
     wmin_adir = wmin_sel = 0
+    # the per-graph calls are timed with L2 flushed before each (a graph counted right after
+    # it was built or warmed would otherwise be read from L2, which a pass over many graphs,
+    # and the batch, cannot do)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     t_setup = time.perf_counter()
     for i, (n, gamma, d) in enumerate(params):
         pairs = atc.gen_chunglu_device(n, gamma, d, a.seed * 100003 + i, stream=sp)
         csr = atc.pretc_device(pairs.data_ptr(), pairs.shape[0], atc.Dir.ADIRECTION, stream=sp)
         for j, kf in enumerate(kfixed):
             atc.tc(csr, kf, stream=sp)  # warm
+            flush.fill_(j)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             c, _ = atc.tc(csr, kf, stream=sp)
@@ -537,7 +542,8 @@ def run_batch(a):
         "graphs": ng, "vertices": n_all, "edges": m_all, "triangles": int(sum(plain_counts)),
         "plain": {kf.name.lower(): {"ms_total": sum(ms), "graphs_per_s": ng / (sum(ms) * 1e-3),
                                     "edges_per_s": m_all / (sum(ms) * 1e-3)} for kf, ms in zip(kfixed, plain_ms)},
-        "plain_note": "atc_tc per graph on its resident A-direction CSR, host-synchronised per call",
+        "plain_note": "atc_tc per graph on its resident A-direction CSR, host-synchronised per call, L2 flushed "
+                      "(256 MB written) before each timed call",
         "batched": {"ms_per_replay": batch_ms, "graphs_per_s": ng / (batch_ms * 1e-3),
                     "edges_per_s": m_all / (batch_ms * 1e-3), "tuned": cands[best],
                     "tune_ms": [float(x) for x in tune_ms], "selection": "work estimate" if a.batch_select else "none",
