@@ -232,8 +232,12 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
 
   CsrView g = csr_view(b->off, b->cols, nullptr, n, m);
   GraphTags tags{b->vbase_d, ng, b->gcounts};
-  CompactItems witems{b->items, b->gstart, cap_items, false, sh};
-  CompactItems bitems{b->items, b->gstart, cap_items, true, sh};
+  // grouped at the source, a vertex's partners are its own row: the items index the CSR
+  // itself and the grouping passes are skipped
+  const int64_t* gstart = sh.by_source ? b->off : b->gstart;
+  const int32_t* plist = sh.by_source ? b->cols : b->plist;
+  CompactItems witems{b->items, gstart, cap_items, false, sh};
+  CompactItems bitems{b->items, gstart, cap_items, true, sh};
   cudaStream_t c = b->cap_stream;
   size_t bytes = 0;
   ATC_TRY(exclusive_scan_i32_to_i64_tmp(nullptr, &bytes, b->cnt, b->gstart, (size_t)n + 1, s));
@@ -243,14 +247,15 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   cudaMemsetAsync(b->cur, 0, sizeof(int32_t) * (n + 1), c);
   cudaMemsetAsync(b->counters, 0, sizeof(int) * 8, c);
   cudaMemsetAsync(b->gcounts, 0, sizeof(unsigned long long) * ng, c);
-  group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt, sh.by_source);
-  exclusive_scan_i32_to_i64_tmp(b->scan_tmp, &bytes, b->cnt, b->gstart, (size_t)n + 1, c);
-  group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist,
-                                                                     sh.by_source);
-  group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->gstart, b->items, cap_items, b->counters, sh);
-  bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(g, b->plist, bitems, 0, b->counters + 1,
+  if (!sh.by_source) {
+    group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt);
+    exclusive_scan_i32_to_i64_tmp(b->scan_tmp, &bytes, b->cnt, b->gstart, (size_t)n + 1, c);
+    group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist);
+  }
+  group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, gstart, b->items, cap_items, b->counters, sh);
+  bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(g, plist, bitems, 0, b->counters + 1,
                                                                             b->counters + 5, words, tags, b->gcounts);
-  bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(g, b->plist, witems, 0, b->counters,
+  bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(g, plist, witems, 0, b->counters,
                                                                        b->counters + 4, tags, b->gcounts);
   cudaError_t launch_err = cudaGetLastError();
   cudaError_t end_err = cudaStreamEndCapture(c, &b->graph);

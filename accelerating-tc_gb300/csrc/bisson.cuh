@@ -120,7 +120,8 @@ struct ItemShape {
   int warp_max;
   int warp_chunk;
   int block_chunk;
-  int by_source;    // batch grouping: 1 = every edge at its source (h = u, partner v)
+  int by_source;    // batches: 1 = every edge at its source (h = u, partners = its row: the
+                    // Hu-style wedge walk, no grouping passes), 0 = at the longer endpoint
 };
 
 __host__ __device__ inline ItemShape default_shape(int cutover) {
@@ -263,23 +264,20 @@ __device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f) {
   }
 }
 
-// by_source: every edge goes to its source (the Hu-style wedge walk: N+(v) streamed
-// through N+(u) for every edge, no choice of endpoint), which keeps the scatter in row order.
-__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt, int by_source) {
+__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt) {
   for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
-    const int32_t h = ok ? (by_source || longer_is_u(u, v, du, dv) ? u : v) : -1;
+    const int32_t h = ok ? (longer_is_u(u, v, du, dv) ? u : v) : -1;
     const unsigned same = __match_any_sync(0xffffffffu, h);
     if (h >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&cnt[h], __popc(same));
   });
 }
 
-__global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist,
-                                        int by_source) {
+__global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
   const int lane = threadIdx.x & 31;
   for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
     int32_t h = -1, p = 0;
     if (ok) {
-      const bool hu = by_source || longer_is_u(u, v, du, dv);
+      const bool hu = longer_is_u(u, v, du, dv);
       h = hu ? u : v;
       p = hu ? v : u;
     }

@@ -108,8 +108,9 @@ typedef struct atc_tuning {
   int32_t bisson_block_chunk; /* partners per block item (2048) */
   int32_t bisson_slots;      /* hash slots per bucket of the tables: 1, 2 or 4 (0: default) */
   /* the bisson_* item shape applies to the Hu-style kernel too */
-  int32_t group_by_source;   /* batches: 1 = group every edge at its source (Hu-style wedge
-                                tests, no scatter), 0 = at the endpoint with the longer list */
+  int32_t group_by_source;   /* batches: 1 = every edge at its source, the items index the
+                                CSR rows (Hu-style wedge tests, no grouping passes); 0 = at
+                                the endpoint with the longer list (Bisson-style) */
   int32_t reserved[4];
 } atc_tuning;
 
