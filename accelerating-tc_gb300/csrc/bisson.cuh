@@ -195,12 +195,14 @@ __global__ void group_items_kernel(CsrView g, const int64_t* gstart, GroupItem* 
 // the group starts and the item shape.
 struct FullItems {
   static constexpr bool kBatch = false;  // one graph: counts go to the kernel's counter
+  static constexpr int kMinBlocks = 0;  // no occupancy hint (the register choice measured fastest)
   const GroupItem* p;
   __device__ __forceinline__ GroupItem get(const CsrView&, int i) const { return p[i]; }
 };
 
 struct CompactItems {
   static constexpr bool kBatch = true;  // a batch: counts go to each item's graph
+  static constexpr int kMinBlocks = 6;    // 40 registers: 6 CTAs of 256 threads per SM
   const int2* p;
   const int64_t* gstart;
   int64_t cap;
@@ -334,32 +336,39 @@ __device__ __forceinline__ int graph_of(const GraphTags& t, int64_t v) {
 }
 
 // Per-warp attribution of counts to the graphs of a batch.  The warp keeps the graph of
-// its last item and that graph's vertex range, adds its lanes' hits to a running partial,
-// and flushes the partial (one shuffle reduction, one atomic) only when an item of another
-// graph comes or the kernel ends.  A warp takes items in increasing index order, which is
-// vertex order, so the graph lookup (a binary search over the graph starts) runs about
-// once per graph instead of once per item.  All 32 lanes call add/flush; h is the same
-// on every lane.
-struct GraphAcc {
-  int g = -1;
-  int64_t lo = 0, hi = 0;
-  unsigned long long part = 0;
-  __device__ __forceinline__ void flush(const GraphTags& t) {
-    unsigned long long c = part;
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if ((threadIdx.x & 31) == 0 && c && g >= 0) atomicAdd(&t.counts[g], c);
-    part = 0;
-  }
-  __device__ __forceinline__ void add(const GraphTags& t, int64_t h, unsigned c) {
-    if (h < lo || h >= hi) {
-      flush(t);
-      g = graph_of(t, h);
-      lo = t.vbase[g];
-      hi = t.vbase[g + 1];
-    }
-    part += c;
-  }
+// its last item, that graph's vertex range and its running count in shared memory (no
+// registers held across the item), and flushes the count (one atomic) only when an item
+// of another graph comes or the kernel ends.  A warp takes items in increasing index
+// order, which is vertex order, so the graph lookup (a binary search over the graph
+// starts) runs about once per graph instead of once per item.  All 32 lanes call add and
+// flush; h is the same on every lane.
+struct GraphAccSlot {
+  int g;
+  int32_t lo, hi;
+  unsigned long long part;
 };
+__device__ __forceinline__ void graph_acc_init(GraphAccSlot* a) {
+  if ((threadIdx.x & 31) == 0) *a = GraphAccSlot{-1, 0, 0, 0ull};
+  __syncwarp();
+}
+__device__ __forceinline__ void graph_acc_flush(const GraphTags& t, GraphAccSlot* a) {
+  if ((threadIdx.x & 31) == 0 && a->part && a->g >= 0) atomicAdd(&t.counts[a->g], a->part);
+  __syncwarp();
+}
+__device__ __forceinline__ void graph_acc_add(const GraphTags& t, GraphAccSlot* a, int64_t h, unsigned c) {
+  unsigned long long w = c;
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  if ((threadIdx.x & 31) == 0) {
+    if (h < a->lo || h >= a->hi) {
+      if (a->part && a->g >= 0) atomicAdd(&t.counts[a->g], a->part);
+      const int g = graph_of(t, h);
+      *a = GraphAccSlot{g, (int32_t)t.vbase[g], (int32_t)t.vbase[g + 1], 0ull};
+    }
+    a->part += w;
+  }
+  __syncwarp();
+}
+
 
 // Hash tables of N+(h): linear probing over buckets of S slots (S = 1, 2 or 4; 4-, 8- or
 // 16-byte aligned), empty slots hold -1.  The home bucket of x is given by Fibonacci
@@ -574,7 +583,7 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
 
 // nitems_dev (nullable): the item count read from device memory instead of `nitems`.
 template <class Items, int S = 1>
-__global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
+__global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                   Items items, int nitems,
                                                                   const int* nitems_dev, int* next, GraphTags tags,
                                                                   unsigned long long* out) {
@@ -585,7 +594,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
   for (int j = lane; j < kWarpSlots; j += 32) tab[w][j] = -1;
   __syncwarp();
   unsigned long long total = 0;
-  GraphAcc acc;
+  __shared__ GraphAccSlot acc[kBgWarps];
+  if constexpr (Items::kBatch) graph_acc_init(&acc[w]);
   int32_t* T = tab[w];
   if (nitems_dev) nitems = *nitems_dev;
   // batch items are taken kWarpGrab at a time (one atomic): most of them are tiny
@@ -632,15 +642,15 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_warp_kernel(CsrView g, c
       for (int j = lane; j < dh; j += 32) hash_erase<S>(T, mask, __ldg(g.cols + hb + j));
     }
     __syncwarp();
-    if constexpr (Items::kBatch) acc.add(tags, gi.h, cnt);
+    if constexpr (Items::kBatch) graph_acc_add(tags, &acc[w], gi.h, cnt);
     else total += cnt;
   }
-  if constexpr (Items::kBatch) acc.flush(tags);
+  if constexpr (Items::kBatch) graph_acc_flush(tags, &acc[w]);
   warp_add_count(total, out);
 }
 
 template <class Items, int S = 1>
-__global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
+__global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_block_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                    Items items, int nitems,
                                                                    const int* nitems_dev, int* next, uint32_t tab_words,
                                                                    GraphTags tags, unsigned long long* out) {
@@ -652,7 +662,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (uint32_t j = threadIdx.x; j < tab_words; j += blockDim.x) tab[j] = -1;
   unsigned long long total = 0;
-  GraphAcc acc;
+  __shared__ GraphAccSlot acc[kBgWarps];
+  if constexpr (Items::kBatch) graph_acc_init(&acc[w]);
   if (nitems_dev) nitems = *nitems_dev;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -714,10 +725,10 @@ __global__ void __launch_bounds__(kBgWarps * 32) bisson_block_kernel(CsrView g, 
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
     }
     __syncthreads();
-    if constexpr (Items::kBatch) acc.add(tags, gi.h, cnt);
+    if constexpr (Items::kBatch) graph_acc_add(tags, &acc[w], gi.h, cnt);
     else total += cnt;
   }
-  if constexpr (Items::kBatch) acc.flush(tags);
+  if constexpr (Items::kBatch) graph_acc_flush(tags, &acc[w]);
   warp_add_count(total, out);
 }
 
