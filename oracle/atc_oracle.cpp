@@ -226,6 +226,133 @@ struct IdSort {    // A-order.cpp:56-60
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// GRO's gain list (vertex_ordering/other_order/linkedlist_heap.cpp:3-254), restated:
+// every key sits in one doubly linked list ordered by non-increasing gain; per gain
+// value a header marks the first and last key with that gain.  Gains from an earlier
+// window are stale (their state label differs) and read as 0.  inc() only records the
+// key's first change since the last adjust(); adjust() then moves the recorded keys in
+// recording order (up()), which fixes how keys of equal gain are ordered.
+// ---------------------------------------------------------------------------
+class GroGainList {
+ public:
+  explicit GroGainList(int cap) : nodes_(cap), heads_(2 * (size_t)cap + 2, Head{-1, -1, 0}), pend_() {
+    for (int i = 0; i < cap; ++i) nodes_[i] = Node{0, 0, i - 1, i + 1};
+    if (cap) {
+      nodes_[cap - 1].next = -1;
+      heads_[0] = Head{0, cap - 1, 0};
+      head_ = 0;
+      tail_ = cap - 1;
+    }
+  }
+  bool has(int key) const { return nodes_[key].val != -1; }  // :141-144
+  int max_gain() const { return max_gain_; }
+  void inc(int key) {                                         // :25-41
+    Node& x = nodes_[key];
+    if ((x.state & kLabelMask) != label_) {
+      x.val = 0;
+      x.state = label_;
+    }
+    ++x.val;
+    if (x.val > max_gain_) max_gain_ = x.val;
+    if ((x.state & kPending) == 0) {
+      pend_.push_back({key, x.val - 1});
+      x.state |= kPending;
+    }
+  }
+  int pop() {  // :49-71
+    adjust();
+    Node& x = nodes_[head_];
+    const int val = x.state != label_ ? 0 : x.val;
+    const int key = head_;
+    x.val = -1;
+    head_ = x.next;
+    if (x.next == -1) tail_ = -1;
+    else nodes_[x.next].prev = -1;
+    Head& h = heads_[val];
+    if (h.first == h.last) h.first = h.last = -1;
+    else h.first = head_;
+    return key;
+  }
+  void del(int key) {  // :73-98
+    adjust();
+    Node& x = nodes_[key];
+    if (x.val == -1) return;
+    const int val = x.state != label_ ? 0 : x.val;
+    x.val = -1;
+    unlink(key);
+    Head& h = heads_[val];
+    if (h.first == h.last) h.first = h.last = -1;
+    else if (h.first == key) h.first = x.next;
+    else if (h.last == key) h.last = x.prev;
+  }
+  void reset() {  // :100-105
+    ++label_;
+    pend_.clear();
+    heads_[0] = Head{head_, tail_, label_};
+  }
+
+ private:
+  static constexpr int kLabelMask = 0x7fffffff;
+  static constexpr int kPending = (int)0x80000000u;
+  struct Node { int state, val, prev, next; };
+  struct Head { int first, last, label; };
+  std::vector<Node> nodes_;
+  std::vector<Head> heads_;
+  std::vector<std::pair<int, int>> pend_;  // (key, gain before its first change)
+  int label_ = 0, head_ = -1, tail_ = -1, max_gain_ = 0;
+
+  void unlink(int key) {
+    const Node& x = nodes_[key];
+    if (x.prev == -1) head_ = x.next;
+    else nodes_[x.prev].next = x.next;
+    if (x.next == -1) tail_ = x.prev;
+    else nodes_[x.next].prev = x.prev;
+  }
+  void adjust() {  // :107-113
+    for (const auto& p : pend_) up(p.first, p.second);
+    pend_.clear();
+  }
+  void up(int key, int old_val) {  // :162-216
+    Node& x = nodes_[key];
+    Head& oh = heads_[old_val];
+    if (oh.first == oh.last) oh.first = oh.last = -1;
+    else if (oh.first == key) oh.first = x.next;
+    else if (oh.last == key) oh.last = x.prev;
+    unlink(key);
+    Head& nh = heads_[x.val];
+    if (nh.label != label_ || nh.first == -1) {  // no key has this gain yet
+      nh.first = nh.last = key;
+      nh.label = label_;
+      int r = x.val - 1;  // the nearest smaller gain that has keys, down to old_val
+      while (r > old_val && (heads_[r].label != label_ || heads_[r].first == -1)) --r;
+      const Head& rh = heads_[r];
+      if (rh.first == -1) {  // back into its old place
+        if (x.prev == -1) head_ = key;
+        else nodes_[x.prev].next = key;
+        if (x.next == -1) tail_ = key;
+        else nodes_[x.next].prev = key;
+      } else {  // just before the first key of gain r
+        const int right = rh.first, left = nodes_[right].prev;
+        x.prev = left;
+        x.next = right;
+        if (left == -1) head_ = key;
+        else nodes_[left].next = key;
+        nodes_[right].prev = key;
+      }
+    } else {  // after the last key with this gain
+      const int left = nh.last, right = nodes_[left].next;
+      x.prev = left;
+      x.next = right;
+      nodes_[left].next = key;
+      if (right == -1) tail_ = key;
+      else nodes_[right].prev = key;
+      nh.last = key;
+    }
+    x.state -= kPending;
+  }
+};
+
 extern "C" {
 
 // Status codes shared by the oracle entry points.
@@ -892,6 +1019,88 @@ void orc_mlp_grad(const float* params, int I, int H, int O, const float* mean, c
     }
   }
   *loss = 0.5 * L / msum;
+}
+
+
+// GRO order (vertex_ordering/other_order/porder.cpp:141-226, POrder::greedy_mheap) of the
+// directed edges `edges` (uint64 words, source in the high half: util.cpp:56-67).  Edges
+// are sorted as POrder::build sorts them (porder.cpp:94-123, repeats kept); vertices are
+// taken in windows of 32 (PACK_WIDTH, util.hpp:21-27): a window opens with the first
+// unplaced vertex in (degree desc, id asc) order, and each next vertex is the head of
+// the gain list, where every placed u adds one to each unplaced w that shares an
+// in-neighbour's out-list or an out-neighbour's in-list with u (each neighbour once per
+// window).  new_id (v_num = max id + 1 ints) receives the order: org2newid of the
+// program's _GRO_newID.txt.  Returns v_num.  *max_gain (nullable) = the largest gain any
+// key reached: the program's gain headers hold 2 * v_num entries of which only the first
+// v_num are initialised (linkedlist_heap.cpp:9-18), so its output is defined only while
+// max_gain < v_num.
+int32_t orc_gro(const uint64_t* edges, uint64_t ne, int32_t* new_id, int32_t* max_gain) {
+  std::vector<std::pair<int, int>> ev(ne);
+  int vn = 0;
+  for (uint64_t i = 0; i < ne; ++i) {
+    ev[i] = {(int)(edges[i] >> 32), (int)(edges[i] & 0xffffffffu)};
+    vn = std::max(vn, std::max(ev[i].first, ev[i].second));
+  }
+  if (ne == 0) return 0;
+  ++vn;
+  if (!new_id) return vn;
+  std::sort(ev.begin(), ev.end());
+  std::vector<int> od(vn, 0), id(vn, 0), os(vn + 1, 0), is(vn + 1, 0), oe(ne), ie(ne);
+  for (const auto& e : ev) {
+    ++od[e.first];
+    ++id[e.second];
+  }
+  for (int v = 0; v < vn; ++v) {
+    os[v + 1] = os[v] + od[v];
+    is[v + 1] = is[v] + id[v];
+  }
+  std::vector<int> ipos(is.begin(), is.end() - 1);
+  for (uint64_t i = 0; i < ne; ++i) {
+    oe[i] = ev[i].second;
+    ie[ipos[ev[i].second]++] = ev[i].first;
+  }
+  std::vector<int> by_deg(vn);
+  for (int v = 0; v < vn; ++v) by_deg[v] = v;
+  std::sort(by_deg.begin(), by_deg.end(), [&](int a, int b) {
+    const int da = od[a] + id[a], db = od[b] + id[b];
+    return da == db ? a < b : da > db;
+  });
+  std::vector<char> placed(vn, 0);
+  size_t cursor = 0;  // the first vertex of by_deg not yet placed (doublelinked_list.cpp pop_head)
+  GroGainList gains(vn);
+  std::vector<int> out_mark(vn, -1), in_mark(vn, -1);
+  const int kWindow = 32;
+  int window = -1;
+  for (int idx = 0; idx < vn; ++idx) {
+    int u;
+    if (idx % kWindow == 0) {
+      while (placed[by_deg[cursor]]) ++cursor;
+      u = by_deg[cursor];
+      gains.reset();
+      gains.del(u);
+      ++window;
+    } else {
+      u = gains.pop();
+    }
+    placed[u] = 1;
+    new_id[u] = idx;
+    for (int j = is[u]; j < is[u + 1]; ++j) {
+      const int v = ie[j];
+      if (out_mark[v] == window) continue;
+      out_mark[v] = window;
+      for (int k = os[v]; k < os[v + 1]; ++k)
+        if (gains.has(oe[k])) gains.inc(oe[k]);
+    }
+    for (int j = os[u]; j < os[u + 1]; ++j) {
+      const int v = oe[j];
+      if (in_mark[v] == window) continue;
+      in_mark[v] = window;
+      for (int k = is[v]; k < is[v + 1]; ++k)
+        if (gains.has(ie[k])) gains.inc(ie[k]);
+    }
+  }
+  if (max_gain) *max_gain = gains.max_gain();
+  return vn;
 }
 
 }  // extern "C"

@@ -48,6 +48,8 @@ def lib():
                                    C.POINTER(C.c_double)]
         L.orc_core_numbers.argtypes = [_P, C.c_uint64, _P]
         L.orc_relabel.argtypes = [_P, C.c_uint64, C.c_int, _P, _P]
+        L.orc_gro.restype = C.c_int32
+        L.orc_gro.argtypes = [_P, C.c_uint64, _P, _P]
         L.orc_adirection_par.argtypes = [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]
         L.orc_costfunc.argtypes = [_P, C.c_uint64, C.c_int, _P]
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
@@ -181,6 +183,17 @@ def relabel(pairs, kind):
     lib().orc_relabel(_ptr(p), p.shape[0], int(kind), _ptr(lookup), _ptr(normal))
     normal = normal[: p.shape[0]]
     return lookup, normal, lookup[normal] if normal.size else normal.copy()
+
+
+def gro(edges_u64):
+    """(new_id, max_gain) of other_order's GRO order (porder.cpp:141-226) on packed
+    uint64 directed edges (source in the high half)."""
+    e = np.ascontiguousarray(edges_u64, dtype=np.uint64)
+    vn = lib().orc_gro(_ptr(e), e.size, None, None)
+    new_id = np.empty(max(vn, 1), dtype=np.int32)
+    mg = C.c_int32(0)
+    lib().orc_gro(_ptr(e), e.size, _ptr(new_id), C.byref(mg))
+    return new_id[:vn], mg.value
 
 
 def adirection_par(edges_u64, compat=False):

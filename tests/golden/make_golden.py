@@ -15,6 +15,10 @@ case the script records what the reference programs output:
   costfunc     costFuncCal lpBasedGraph.bin k -> three printed floats, k = 1, 2
   verification verification lpBasedGraph    -> two printed floats (text input)
   triangles    OrgTriangleCount on E symmetrised (x86 only; int result, small graphs)
+  gro_sym      other_order reorder (GRO) on E symmetrised, packed uint64 -> _GRO_newID.txt
+  gro_lp       the same on the A-direction output (directed edges)
+               (x86 only; recorded only where its gain headers stay initialised:
+               max gain < vertex count, see orc_gro)
 
 Small outputs are stored in full, larger ones as (count, sha256).
 
@@ -67,6 +71,30 @@ def record(arr: np.ndarray):
     if arr.size // 2 <= INLINE_MAX:
         d["pairs"] = arr.reshape(-1).tolist()
     return d
+
+
+def record_ids(arr: np.ndarray):
+    arr = np.ascontiguousarray(arr, dtype=np.int32)
+    d = {"count": int(arr.size), "sha256": sha(arr.tobytes())}
+    if arr.size <= 2 * INLINE_MAX:
+        d["ids"] = arr.tolist()
+    return d
+
+
+def gro_case(d, pairs):
+    """GRO newID of the directed pairs through the reference reorder program."""
+    if not pairs.size:
+        return {"unsupported": True, "reason": "empty"}
+    u64 = (pairs[:, 0].astype(np.uint64) << np.uint64(32)) | pairs[:, 1].astype(np.uint32).astype(np.uint64)
+    new_id, max_gain = oracle.gro(u64)
+    if max_gain >= new_id.size:
+        return {"unsupported": True, "reason": "max gain %d >= %d vertices" % (max_gain, new_id.size)}
+    u64.tofile(os.path.join(d, "G.bin"))
+    r = run([os.path.join(REF, "reorder"), "G.bin"], d)
+    assert r.returncode == 0, r.stdout
+    ids = np.loadtxt(os.path.join(d, "G_GRO_newID.txt"), dtype=np.int64, ndmin=2)
+    assert np.array_equal(ids[:, 0], np.arange(ids.shape[0]))
+    return record_ids(ids[:, 1])
 
 
 def run(args, cwd):
@@ -138,6 +166,10 @@ def case(name, pairs):
             r = run([os.path.join(REF, "orgtc"), os.path.join(d, "E.u64")], d)
             assert r.returncode == 0, r.stdout
             out["triangles"] = int(grab(r.stdout, "triangles="))
+        if os.path.exists(os.path.join(REF, "reorder")):
+            sym = atc.simplify(pairs, symmetric=True) if pairs.size else pairs
+            out["gro_sym"] = gro_case(d, sym)
+            out["gro_lp"] = gro_case(d, lp)
     return out
 
 

@@ -71,6 +71,37 @@ def test_relabel(golden, name, which, kind):
     assert np.array_equal(np.sort(lookup), np.arange(lookup.size))
 
 
+def pack_u64(pairs):
+    pairs = np.asarray(pairs, dtype=np.int32).reshape(-1, 2)
+    return (pairs[:, 0].astype(np.uint64) << np.uint64(32)) | pairs[:, 1].astype(np.uint32).astype(np.uint64)
+
+
+def check_ids(got, rec):
+    got = np.ascontiguousarray(got, dtype=np.int32)
+    assert got.size == rec["count"]
+    if "ids" in rec:
+        assert got.tolist() == rec["ids"]
+    assert hashlib.sha256(got.tobytes()).hexdigest() == rec["sha256"]
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("which", ["gro_sym", "gro_lp"])
+def test_gro(golden, name, which):
+    """other_order's GRO order (reorder program, _GRO_newID.txt) on the symmetrised input and on
+    the A-direction output, where the program's output is defined (max gain < vertex count)."""
+    c = golden["cases"][name]
+    rec = c.get(which)
+    if rec is None or rec.get("unsupported"):
+        pytest.skip("no GRO fixture for this case")
+    g = golden_input(c)
+    import atc
+    src = atc.simplify(g, symmetric=True) if which == "gro_sym" else oracle.adirection(g)
+    new_id, max_gain = oracle.gro(pack_u64(src))
+    assert max_gain < new_id.size
+    check_ids(new_id, rec)
+    assert np.array_equal(np.sort(new_id), np.arange(new_id.size))
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_costfunc(golden, name):
     c = golden["cases"][name]
