@@ -48,12 +48,14 @@ class Order(enum.IntEnum):
     AORDER = 1
     DEGREE_DESC = 2
     AORDER_V2 = 3
+    GRO = 4
 
 
 class Relabel(enum.IntEnum):
     DEGREE_DESC = 0
     AORDER_V2 = 1
     OUTDEG_DESC = 2
+    GRO = 3
 
 
 class Kernel(enum.IntEnum):

@@ -44,6 +44,7 @@ CLI_PROGRAMS = {
     "cost_func_cal": "order_main.cpp",
     "kcore_direction": "order_main.cpp",
     "Peel": "order_main.cpp",
+    "reorder": "order_main.cpp",
 }
 
 

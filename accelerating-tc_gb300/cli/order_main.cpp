@@ -11,10 +11,16 @@
 //        edges, src = x >> 32; --compat keeps the program's minor-priority term, peel.cu:49)
 //   kcore_direction <in> <out>       edge_directing/kcore_direction.cpp:12-146 (uint64 edges,
 //        src = x >> 32; writes the oriented uint64 edges to <out>)
+//   reorder <edges.u64>              vertex_ordering/other_order/reorder.cpp:6-97, its default
+//        GRO order (uint64 edges, src = x >> 32); writes <name>_GRO.txt (the edges sorted,
+//        relabelled, "src dst" lines) and <name>_GRO_newID.txt ("old new" lines)
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <string>
+#include <utility>
 #include <vector>
 
 #include "atc.h"
@@ -108,6 +114,35 @@ int main(int argc, char** argv) {
   std::cout << "the edge num is " << np << std::endl;
   std::cout << "the node num is " << nv << std::endl;
   if (!write_pairs(argv[2], reinterpret_cast<const int32_t*>(out.data()), np)) return 1;
+#elif defined(ATC_PROGRAM_REORDER)
+  // the file's uint64 words hold the source in the high half (other_order/util.cpp:56-67)
+  std::vector<int32_t> directed(pairs.size());
+  int32_t mx = -1;
+  for (uint64_t i = 0; i < np; ++i) {
+    directed[2 * i] = pairs[2 * i + 1];
+    directed[2 * i + 1] = pairs[2 * i];
+    mx = std::max(mx, std::max(directed[2 * i], directed[2 * i + 1]));
+  }
+  std::vector<int32_t> lookup((size_t)std::max(mx, 0) + 1);
+  s = atc_relabel(directed.data(), np, ATC_RELABEL_GRO, lookup.data(), nullptr, nullptr, nullptr);
+  if (s != ATC_OK) return fail("atc_relabel", s);
+  std::string name(argv[1]);
+  size_t slash = name.find_last_of('/');
+  if (slash != std::string::npos) name = name.substr(slash + 1);
+  size_t dot = name.find_last_of('.');
+  if (dot != std::string::npos) name = name.substr(0, dot);
+  std::vector<std::pair<int32_t, int32_t>> sorted(np);
+  for (uint64_t i = 0; i < np; ++i) sorted[i] = {directed[2 * i], directed[2 * i + 1]};
+  std::sort(sorted.begin(), sorted.end());
+  FILE* g = fopen((name + "_GRO.txt").c_str(), "w");
+  FILE* ids = fopen((name + "_GRO_newID.txt").c_str(), "w");
+  if (!g || !ids) return 1;
+  for (const auto& e : sorted) fprintf(g, "%d %d\n", lookup[e.first], lookup[e.second]);
+  const int32_t nv = std::max(mx, 0) + 1;  // the program counts one vertex for an empty list
+  for (int32_t i = 0; i < nv; ++i) fprintf(ids, "%d %d\n", i, lookup[i]);
+  fclose(g);
+  fclose(ids);
+  printf("order_algo=gro graph_file=%s\n", name.c_str());
 #else
 #error "define one ATC_PROGRAM_*"
 #endif

@@ -516,7 +516,7 @@ extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel
                                   int32_t* normal, int32_t* relabeled, atc_stream st) {
   ATC_CHECK_ARG(lookup != nullptr, "lookup is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
-  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_OUTDEG_DESC, "unknown atc_relabel_kind");
+  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_GRO, "unknown atc_relabel_kind");
   cudaStream_t s = as_stream(st);
   int maxid = 0;  // the programs start maxNodeId at 0, so an empty list has one vertex
   for (uint64_t i = 0; i < 2 * np; ++i) {
@@ -530,7 +530,12 @@ extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel
   ATC_TRY(o.alloc(np + 1, s));
   ATC_TRY(lk.alloc(n_v, s));
   if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, s));
-  ATC_TRY(relabel_lookup(d.p, nullptr, 1, np, n_v, kind, lk.p, o.p, s));
+  if (kind == ATC_RELABEL_GRO) {
+    ATC_TRY(gro_lookup(d.p, np, n_v, lk.p, s));
+    if (np) ATC_CK(cudaMemcpyAsync(o.p, d.p, sizeof(int2) * np, cudaMemcpyDeviceToDevice, s));
+  } else {
+    ATC_TRY(relabel_lookup(d.p, nullptr, 1, np, n_v, kind, lk.p, o.p, s));
+  }
   ATC_CK(cudaMemcpyAsync(lookup, lk.p, sizeof(int32_t) * n_v, cudaMemcpyDeviceToHost, s));
   if (normal && np) ATC_CK(cudaMemcpyAsync(normal, o.p, sizeof(int2) * np, cudaMemcpyDeviceToHost, s));
   if (relabeled && np) {

@@ -71,6 +71,16 @@ __global__ void degree_kernel(const uint64_t* keys, int64_t m, int B, int32_t* d
   }
 }
 
+// Both directions of every simple edge (a < b): (a, b) at 2i, (b, a) at 2i+1.
+__global__ void both_directions_kernel(const uint64_t* keys, int64_t m, int B, int2* out) {
+  const uint64_t mask = (1ull << B) - 1;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t a = (int32_t)(keys[i] >> B), b = (int32_t)(keys[i] & mask);
+    out[2 * i] = make_int2(a, b);
+    out[2 * i + 1] = make_int2(b, a);
+  }
+}
+
 struct OrientArgs {
   const int32_t* deg;   // simple degree, by input id
   const int32_t* prio;  // A-direction priority / core number / peel flag, by input id
@@ -298,7 +308,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
                              atc_csr* out, int32_t* perm_out, cudaStream_t s) {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION_PAR, "unknown atc_dir");
-  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_AORDER_V2, "unknown atc_order");
+  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_GRO, "unknown atc_order");
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
   SimpleEdges e;
@@ -338,6 +348,15 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
       peeled = true;
     } else if (order == ATC_ORDER_AORDER) {
       ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s, deg.p));
+    } else if (order == ATC_ORDER_GRO) {
+      // GRO of the undirected graph: both directions of every simple edge
+      DevBuf<int2> sym;
+      ATC_TRY(sym.alloc(2 * (size_t)e.m + 1, s));
+      if (e.m) {
+        both_directions_kernel<<<grid_for(e.m, 256), 256, 0, s>>>(e.keys.p, e.m, e.bits, sym.p);
+        ATC_CK(cudaGetLastError());
+      }
+      ATC_TRY(gro_lookup(sym.p, 2 * (uint64_t)e.m, n_v, perm.p, s));
     } else
       ATC_TRY(relabel_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v,
                              order == ATC_ORDER_DEGREE_DESC ? ATC_RELABEL_DEGREE_DESC : ATC_RELABEL_AORDER_V2, perm.p,

@@ -68,7 +68,10 @@ typedef enum atc_order {
      relabelling of vertex_ordering/A-order/relabel-naive.cpp:67-74 (ATC_RELABEL_DEGREE_DESC) */
   ATC_ORDER_DEGREE_DESC = 2,
   /* A-order-v2's 40-column mix of that list (A-order-v2.cpp:102-146, ATC_RELABEL_AORDER_V2) */
-  ATC_ORDER_AORDER_V2 = 3
+  ATC_ORDER_AORDER_V2 = 3,
+  /* other_order's GRO order of the simple graph, both directions of every edge
+     (vertex_ordering/other_order/porder.cpp:141-226, ATC_RELABEL_GRO) */
+  ATC_ORDER_GRO = 4
 } atc_order;
 
 /* Rank relabellings of vertex_ordering/A-order (atc_relabel). */
@@ -82,7 +85,13 @@ typedef enum atc_relabel_kind {
   ATC_RELABEL_AORDER_V2 = 1,
   /* rt = out-degree of the pairs as given ("good" of relabel4lpOut.cpp:27-54, whose
      input is already oriented) */
-  ATC_RELABEL_OUTDEG_DESC = 2
+  ATC_RELABEL_OUTDEG_DESC = 2,
+  /* GRO order of the other_order library on the pairs as directed edges, repeats kept
+     (vertex_ordering/other_order/porder.cpp:141-226 with linkedlist_heap.cpp, the
+     _GRO_newID.txt of its reorder program); `normal` = the pairs as given.  The program
+     reads uninitialised memory once a vertex's gain reaches the vertex count; this
+     build reads those gains as unset. */
+  ATC_RELABEL_GRO = 3
 } atc_relabel_kind;
 
 typedef enum atc_kernel {

@@ -78,6 +78,40 @@ def test_relabel_matches_reference(golden, name, which, kind):
     assert np.array_equal(lookup, olookup) and np.array_equal(normal, onormal)
 
 
+def pack_u64(pairs):
+    pairs = np.asarray(pairs, dtype=np.int32).reshape(-1, 2)
+    return (pairs[:, 0].astype(np.uint64) << np.uint64(32)) | pairs[:, 1].astype(np.uint32).astype(np.uint64)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("which", ["gro_sym", "gro_lp"])
+def test_gro_matches_reference(golden, name, which):
+    """other_order's GRO order (the reorder program's _GRO_newID.txt)."""
+    c = golden["cases"][name]
+    g = golden_input(c)
+    src = atc.simplify(g, symmetric=True) if which == "gro_sym" else oracle.adirection(g)
+    lookup, normal, rel = atc.relabel(src, atc.Relabel.GRO)
+    onew, _ = oracle.gro(pack_u64(src))
+    assert np.array_equal(lookup[: onew.size], onew)
+    assert np.array_equal(normal, src) and np.array_equal(rel, lookup[src])
+    rec = c.get(which)
+    if rec and not rec.get("unsupported"):
+        got = np.ascontiguousarray(lookup[: rec["count"]], dtype=np.int32)
+        assert hashlib.sha256(got.tobytes()).hexdigest() == rec["sha256"]
+
+
+def test_gro_order_in_pretc():
+    g = atc.rmat_graph(12, 16, 4)
+    want = oracle.tc_count(g)
+    sym = atc.simplify(g, symmetric=True)
+    onew, _ = oracle.gro(pack_u64(sym))
+    for d in (atc.Dir.ADIRECTION, atc.Dir.DEGREE, atc.Dir.ID):
+        csr = atc.pretc(g, d, atc.Order.GRO, want_perm=True)
+        assert np.array_equal(csr.perm[: onew.size], onew)
+        for k in KERNELS:
+            assert atc.tc(csr, k)[0] == want, (d.name, k.name)
+
+
 @pytest.mark.parametrize("order", [atc.Order.DEGREE_DESC, atc.Order.AORDER_V2])
 def test_relabel_orders_in_pretc(order):
     g = atc.rmat_graph(13, 16, 6)
@@ -342,6 +376,17 @@ def test_cli_dropins(tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert np.array_equal(np.fromfile(tmp_path / "K.u64", dtype=np.uint64), atc.kcore_direction(u64))
+    # other_order's reorder (GRO): <name>_GRO_newID.txt and the sorted, relabelled edges
+    r = subprocess.run([os.path.join(bindir, "reorder"), str(tmp_path / "E.u64")], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ids = np.loadtxt(tmp_path / "E_GRO_newID.txt", dtype=np.int64, ndmin=2)
+    e = np.fromfile(tmp_path / "E.u64", dtype=np.uint64)
+    directed = np.stack([(e >> np.uint64(32)).astype(np.int32), (e & np.uint64(0xffffffff)).astype(np.int32)], 1)
+    onew, _ = oracle.gro(e)
+    assert np.array_equal(ids[:, 0], np.arange(onew.size)) and np.array_equal(ids[:, 1], onew)
+    srt = directed[np.lexsort((directed[:, 1], directed[:, 0]))]
+    assert np.array_equal(np.loadtxt(tmp_path / "E_GRO.txt", dtype=np.int64, ndmin=2), onew[srt])
     n = int(g.max()) + 1
     adj = [[] for _ in range(n)]
     for u, v in g:
