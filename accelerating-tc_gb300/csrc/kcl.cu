@@ -53,7 +53,10 @@ __device__ __forceinline__ int warp_intersect(const int32_t* P, int np, const in
 
 constexpr int kKcWarps = 8;
 constexpr int kMaxK = 16;
-constexpr int kMaskMax = 64;  // candidate sets up to this size use the bitmask path
+constexpr int kMaskMax = 64;     // candidate sets up to this size use the warp's bitmask path
+constexpr int kDenseMax = 1024;  // larger ones up to this size: a CTA per edge, bitmaps in shared memory
+constexpr int kDenseWords = kDenseMax / 64;
+constexpr int kDenseThreads = 256;
 
 // d-cliques inside `mask` of the DAG whose successor sets (within C0) are adj[]:
 // cliq(1, M) = |M|, cliq(d, M) = sum_{i in M} cliq(d-1, M & adj[i]).  Iterative, one
@@ -87,9 +90,11 @@ __device__ __forceinline__ unsigned long long mask_cliques(const unsigned long l
   return total;
 }
 
+// dense (nullable): edges whose C0 has kMaskMax < |C0| <= kDenseMax are appended to
+// dense[1 + ...] (count in dense[0]) for kcl_dense_kernel instead of being walked here.
 __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, const int32_t* cols, const int32_t* esrc,
                                                           int64_t m, int k, int cap, int32_t* scratch,
-                                                          unsigned long long* out) {
+                                                          unsigned long long* dense, unsigned long long* out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t gw = (int64_t)blockIdx.x * kKcWarps + w;
   const int64_t warps = (int64_t)gridDim.x * kKcWarps;
@@ -111,6 +116,11 @@ __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, 
       continue;
     }
     if (c0 < levels) continue;  // not enough candidates for k-2 more vertices
+    if (dense && c0 > kMaskMax && c0 <= kDenseMax) {
+      if (lane == 0) dense[1 + atomicAdd(dense, 1ull)] = (unsigned long long)e;
+      bytes -= 4ull * (unsigned long long)vd;  // the dense kernel reads N+(v) again and counts it
+      continue;
+    }
     if (c0 <= kMaskMax) {
       // bitmask path: adjm[w][i] = members of C0 that are successors of C0[i]
       for (int i = 0; i < c0; ++i) {
@@ -172,6 +182,140 @@ __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, 
   }
 }
 
+// (d)-cliques of the DAG whose successor bitmaps are A (rows of `words` uint64) among
+// the members in `mask`: cliq(1, M) = |M|, cliq(d, M) = sum_{i in M} cliq(d-1, M & A[i]).
+// One thread, an explicit stack of candidate masks.
+__device__ unsigned long long dense_cliques(const unsigned long long* A, int words, const unsigned long long* mask,
+                                            int d) {
+  unsigned long long stack[kMaxK][kDenseWords];
+  int pos[kMaxK];  // next member index to try at each depth
+  if (d == 1) {
+    unsigned long long c = 0;
+    for (int w = 0; w < words; ++w) c += __popcll(mask[w]);
+    return c;
+  }
+  for (int w = 0; w < words; ++w) stack[0][w] = mask[w];
+  pos[0] = 0;
+  int top = 0;
+  unsigned long long total = 0;
+  const int nbits = words * 64;
+  while (top >= 0) {
+    // next member i >= pos[top] of stack[top]
+    int i = -1;
+    for (int b = pos[top]; b < nbits;) {
+      const unsigned long long word = stack[top][b >> 6] >> (b & 63);
+      if (word) {
+        i = b + __ffsll(word) - 1;
+        break;
+      }
+      b = (b | 63) + 1;
+    }
+    if (i < 0) {
+      --top;
+      continue;
+    }
+    pos[top] = i + 1;
+    const unsigned long long* row = A + (size_t)i * words;
+    const int left = d - 1 - top;  // members still to choose after i
+    if (left == 1) {
+      for (int w = 0; w < words; ++w) total += __popcll(stack[top][w] & row[w]);
+    } else {
+      int c = 0;
+      for (int w = 0; w < words; ++w) {
+        stack[top + 1][w] = stack[top][w] & row[w];
+        c += __popcll(stack[top + 1][w]);
+      }
+      if (c >= left) {
+        ++top;
+        pos[top] = 0;
+      }
+    }
+  }
+  return total;
+}
+
+// Edges whose C0 = N+(u) ∩ N+(v) holds kMaskMax < |C0| <= kDenseMax members, a CTA per
+// edge: C0 in shared memory (sorted, as N+(u) is), the DAG induced on it as successor
+// bitmaps (row i: the members of N+(C0[i]), found by binary search in C0), then thread t
+// counts the (k-2)-cliques whose first vertex is C0[i] for i = t, t + 256, ... with
+// AND / popc over the rows: cliques are counted in words of 64 instead of listed.
+__global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t* off, const int32_t* cols,
+                                                                  const int32_t* esrc, const unsigned long long* dense,
+                                                                  int k, int cmax, unsigned long long* next,
+                                                                  unsigned long long* out) {
+  extern __shared__ unsigned long long dsm[];  // rows: cmax * words
+  __shared__ int32_t C[kDenseMax];
+  __shared__ int wcount[kDenseThreads / 32];
+  __shared__ int csize;
+  __shared__ unsigned long long item;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = kDenseThreads / 32;
+  const unsigned long long nitems = dense[0];
+  unsigned long long cnt = 0, bytes = 0;
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(next, 1ull);
+    __syncthreads();
+    const unsigned long long it = item;
+    if (it >= nitems) break;
+    const int64_t e = (int64_t)dense[1 + it];
+    const int32_t u = esrc[e], v = cols[e];
+    const int64_t ub = off[u], ud = off[u + 1] - ub, vb = off[v], vd = off[v + 1] - vb;
+    if (threadIdx.x == 0) {
+      csize = 0;
+      bytes += 4ull * (unsigned long long)vd;
+    }
+    __syncthreads();
+    // C0 in the order of N+(u): block-wide compaction of the hits, chunk by chunk
+    for (int64_t base = 0; base < ud; base += kDenseThreads) {
+      const int64_t j = base + threadIdx.x;
+      const int32_t x = j < ud ? cols[ub + j] : 0;
+      const bool hit = j < ud && kc_has(cols + vb, vd, x);
+      const unsigned b = __ballot_sync(0xffffffffu, hit);
+      if (lane == 0) wcount[w] = __popc(b);
+      __syncthreads();
+      int before = csize;
+      for (int q = 0; q < w; ++q) before += wcount[q];
+      if (hit) C[before + __popc(b & ((1u << lane) - 1))] = x;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int t = csize;
+        for (int q = 0; q < nw; ++q) t += wcount[q];
+        csize = t;
+      }
+      __syncthreads();
+    }
+    const int c = csize;
+    const int words = (c + 63) >> 6;
+    for (int t = threadIdx.x; t < c * words; t += kDenseThreads) dsm[t] = 0ull;
+    __syncthreads();
+    // row i = members of C that are in N+(C[i]); a warp per row, lanes over N+(C[i])
+    for (int i = w; i < c; i += nw) {
+      const int64_t xb = off[C[i]], xd = off[C[i] + 1] - xb;
+      if (lane == 0) bytes += 4ull * (unsigned long long)xd;
+      for (int64_t j = lane; j < xd; j += 32) {
+        const int32_t y = cols[xb + j];
+        int lo = 0, hi = c;  // y's position in C, if any
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (C[mid] < y) lo = mid + 1; else hi = mid;
+        }
+        if (lo < c && C[lo] == y) atomicOr(&dsm[(size_t)i * words + (lo >> 6)], 1ull << (lo & 63));
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < c; i += kDenseThreads)
+      cnt += dense_cliques(dsm, words, dsm + (size_t)i * words, k - 3);
+    __syncthreads();
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+  }
+  if (lane == 0) {
+    if (cnt) atomicAdd(out, cnt);
+    if (bytes) atomicAdd(out + 1, bytes);
+  }
+}
+
 }  // namespace
 
 }  // namespace atc
@@ -200,13 +344,32 @@ extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, a
     while (grid > sm_count() && grid * kKcWarps * per_warp > (4ll << 30)) grid /= 2;
     DevBuf<int32_t> scratch;
     ATC_TRY(scratch.alloc((size_t)grid * kKcWarps * levels * cap, s));
+    // edges with mid-sized C0 go to the dense kernel (k >= 4: C0 holds k-2 more vertices)
+    const bool use_dense = k >= 4 && cap > kMaskMax;
+    DevBuf<unsigned long long> dense;
+    if (use_dense) ATC_TRY(dense.alloc((size_t)csr->m + 2, s));
     tm.start(s);
     ATC_CK(cudaMemsetAsync(pv->counter, 0, 2 * sizeof(unsigned long long), s));
+    if (use_dense) ATC_CK(cudaMemsetAsync(dense.p, 0, 2 * sizeof(unsigned long long), s));
     kcl_kernel<<<(unsigned)grid, kKcWarps * 32, 0, s>>>(csr->offsets, csr->cols, pv->esrc, csr->m, (int)k, cap,
-                                                         scratch.p, pv->counter);
+                                                         scratch.p, use_dense ? dense.p + 1 : nullptr, pv->counter);
     ATC_CK(cudaGetLastError());
-    tm.stop(s);
     launches = 1;
+    if (use_dense) {
+      // rows for the largest C0 this graph can have
+      const int cmax = std::min(cap, kDenseMax);
+      const size_t smem = sizeof(unsigned long long) * (size_t)cmax * ((cmax + 63) / 64);
+      ATC_CK(cudaFuncSetAttribute((const void*)kcl_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+      int dbps = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dbps, kcl_dense_kernel, kDenseThreads, smem);
+      if (dbps < 1) dbps = 1;
+      kcl_dense_kernel<<<(unsigned)(sm_count() * dbps), kDenseThreads, smem, s>>>(
+          csr->offsets, csr->cols, pv->esrc, dense.p + 1, (int)k, cmax, dense.p, pv->counter);
+      ATC_CK(cudaGetLastError());
+      launches = 2;
+    }
+    tm.stop(s);
     ATC_CK(cudaMemcpyAsync(h, pv->counter, sizeof(h), cudaMemcpyDeviceToHost, s));
     ATC_CK(cudaStreamSynchronize(s));
     *count = h[0];

@@ -242,6 +242,22 @@ def test_kcl_complete_graphs():
             assert atc.kcl(csr, k)[0] == comb(n, k), (n, k)
 
 
+def test_kcl_dense_candidate_sets():
+    # C0 = N+(u) ∩ N+(v) above 64 members: the CTA-per-edge bitmap path
+    for n, ks in ((100, range(3, 9)), (300, range(3, 6))):
+        kn = np.array([(a, b) for a in range(n) for b in range(n) if a != b], dtype=np.int32)
+        csr = atc.pretc(kn, atc.Dir.DEGREE)
+        for k in ks:
+            assert atc.kcl(csr, k)[0] == comb(n, k), (n, k)
+    g = atc.rmat_graph(11, 64, 5)
+    for k in (4, 5):
+        want = oracle.kclique(g, k)
+        for d in (atc.Dir.ID, atc.Dir.ADIRECTION):
+            csr = atc.pretc(g, d)
+            assert csr.max_outdeg > 64
+            assert atc.kcl(csr, k)[0] == want, (d.name, k)
+
+
 def test_kcl_three_equals_triangles():
     g = atc.rmat_graph(13, 16, 2)
     csr = atc.pretc(g, atc.Dir.ADIRECTION)
