@@ -65,7 +65,7 @@ def parse():
                     help="fixed kernels timed in the per-graph loop (the first is the reference line)")
     ap.add_argument("--batch-select", action="store_true",
                     help="batched path picks each graph's orientation (degree or A-direction) by its work estimate")
-    ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-5,rmat:14:6-7",
+    ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-6,rmat:14:6-7",
                     help="comma list of kind:log2size:kmin-kmax (kind rmat or rgg)")
     return ap.parse_args()
 

@@ -249,8 +249,8 @@ def test_kcl_dense_candidate_sets():
         csr = atc.pretc(kn, atc.Dir.DEGREE)
         for k in ks:
             assert atc.kcl(csr, k)[0] == comb(n, k), (n, k)
-    g = atc.rmat_graph(11, 64, 5)
-    for k in (4, 5):
+    g = atc.rmat_graph(12, 32, 8)
+    for k in (4, 5, 6):
         want = oracle.kclique(g, k)
         for d in (atc.Dir.ID, atc.Dir.ADIRECTION):
             csr = atc.pretc(g, d)
