@@ -11,6 +11,10 @@ same metric through the public C ABI with host buffers: every step copies the ra
 int32 pairs from pinned host memory, builds the CSR (dedup, A-order, A-direction),
 counts and reads the count back.  Every kernel family is also timed ("kernels").
 
+With N > 1 ranks (torchrun, NCCL) every rank builds the same CSR, each step counts the rank's
+work-balanced part of the edges (atc_tc_part) and sums the parts with one all_reduce: the
+total work is fixed ("scaling": "strong") and `value` = edges / the slowest rank's step.
+
 --impl reference times the reference's CPU triangle count (the oracle restatement of
 OrgTriangleCount's scalar merge, all host threads) on a bounded vertex sample of the same
 graph and prints the same JSON line with "impl": "reference".
@@ -52,8 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernels", default="hu,bisson,fox,tricore", help="families timed besides the headline")
     ap.add_argument("--mode", default="tc", choices=["tc", "kcl", "batch", "select"],
-                    help="tc: the headline (BASELINE config 2); kcl: k-clique counts (config 3); "
-                         "batch: many Chung-Lu graphs, batched vs per-graph loop (config 4)")
+                    help="tc: the headline (R-MAT scale 24, every kernel family); kcl: k-clique counts; "
+                         "batch: many Chung-Lu graphs, batched vs per-graph loop; select: the learned selector")
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--select-train", type=int, default=2048, help="training graphs of the selector")
     ap.add_argument("--select-eval", type=int, default=512, help="held-out graphs of the selector")
@@ -390,7 +394,7 @@ def run_ours(a):
 
 
 def run_kcl(a):
-    """k-clique counting (BASELINE config 3): R-MAT and 2-D RGG graphs, A-direction."""
+    """k-clique counting, k = 4..7, on R-MAT and 2-D RGG graphs, A-direction orientation."""
     import ctypes as C
     import torch
     import atc
@@ -464,7 +468,7 @@ def batch_params(count, seed):
 
 
 def run_batch(a):
-    """Batched TC (BASELINE config 4): one CUDA-graph replay for all graphs vs a per-graph loop."""
+    """Batched TC of seeded Chung-Lu graphs: one CUDA-graph replay for all graphs vs a per-graph loop."""
     import ctypes as C
     import torch
     import atc
@@ -666,7 +670,7 @@ def selector_policies(train_t, eval_t, eval_costs, preds):
 
 
 def run_select(a):
-    """Learned (direction, ordering, kernel) selection (BASELINE config 5)."""
+    """Learned (direction, ordering, kernel) selection on seeded Chung-Lu / R-MAT graphs."""
     import torch
     import atc
     torch.cuda.set_device(0)
