@@ -90,28 +90,6 @@ __global__ void part_bounds_kernel(const int64_t* prefix, int64_t m, uint32_t pa
 // ============================== TriCore-style ======================================
 constexpr int kTriWarps = 8;
 
-// Finds x's bracket between the 32 pivots of A (da elements): returns false when x is
-// settled by the pivots alone (below A[0], or equal to a pivot: *cnt counts it), else sets
-// [*b, *e) = the part of the bracket strictly between two pivots, starting no lower than
-// `prev`.
-__device__ __forceinline__ bool tri_bracket(const int32_t* piv, int64_t da, int32_t x, int64_t prev, int64_t* b,
-                                            int64_t* e, unsigned long long* cnt) {
-  int lo = 0, hi = 32;  // lo = number of pivots <= x
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (piv[mid] <= x) lo = mid + 1; else hi = mid;
-  }
-  if (lo == 0) return false;
-  if (piv[lo - 1] == x) {
-    ++*cnt;
-    return false;
-  }
-  int64_t bb = (int64_t)(lo - 1) * da / 32 + 1;
-  *e = lo == 32 ? da : (int64_t)lo * da / 32;
-  *b = prev > bb ? prev : bb;
-  return true;
-}
-
 __global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsigned long long* out) {
   __shared__ int32_t piv[kTriWarps][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -127,35 +105,28 @@ __global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsi
     if (db == 0) continue;
     piv[w][lane] = A[(int64_t)lane * da / 32];
     __syncwarp();
-    // Each lane takes two elements per round (j and j + 32) and runs their bracket searches
-    // interleaved, so two chains of dependent loads are in flight.  A lane's elements of one
-    // chain ascend: prev0 / prev1 = where that chain's previous search ended, a lower bound
-    // for its next one inside any bracket.
-    int64_t prev0 = 0, prev1 = 0;
-    for (int64_t j = lane; j < db; j += 64) {
-      const bool has1 = j + 32 < db;
-      const int32_t x0 = __ldg(Bl + j), x1 = has1 ? __ldg(Bl + j + 32) : 0;
-      int64_t b0 = 0, e0 = 0, b1 = 0, e1 = 0;  // empty ranges: nothing to search
-      bool s0 = tri_bracket(piv[w], da, x0, prev0, &b0, &e0, &cnt);
-      bool s1 = has1 && tri_bracket(piv[w], da, x1, prev1, &b1, &e1, &cnt);
-      while (b0 < e0 || b1 < e1) {  // lower bounds of x0 in A[b0, e0) and x1 in A[b1, e1)
-        if (b0 < e0) {
-          const int64_t mid = (b0 + e0) >> 1;
-          if (__ldg(A + mid) < x0) b0 = mid + 1; else e0 = mid;
-        }
-        if (b1 < e1) {
-          const int64_t mid = (b1 + e1) >> 1;
-          if (__ldg(A + mid) < x1) b1 = mid + 1; else e1 = mid;
-        }
+    // a lane's elements ascend: `prev` = where its previous element's search ended, a
+    // lower bound for the next one inside any bracket
+    int64_t prev = 0;
+    for (int64_t j = lane; j < db; j += 32) {
+      int32_t x = __ldg(Bl + j);
+      // k = number of pivots <= x
+      int lo = 0, hi = 32;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (piv[w][mid] <= x) lo = mid + 1; else hi = mid;
       }
-      if (s0) {
-        cnt += b0 < da && __ldg(A + b0) == x0;
-        prev0 = b0;
+      if (lo == 0) continue;                 // x < A[0]
+      if (piv[w][lo - 1] == x) { ++cnt; continue; }
+      int64_t b = (int64_t)(lo - 1) * da / 32 + 1;  // strictly inside the bracket
+      int64_t e2 = lo == 32 ? da : (int64_t)lo * da / 32;
+      if (prev > b) b = prev;
+      while (b < e2) {  // lower bound of x in A[b, e2)
+        const int64_t mid = (b + e2) >> 1;
+        if (__ldg(A + mid) < x) b = mid + 1; else e2 = mid;
       }
-      if (s1) {
-        cnt += b1 < da && __ldg(A + b1) == x1;
-        prev1 = b1;
-      }
+      cnt += b < da && __ldg(A + b) == x;
+      prev = b;
     }
     __syncwarp();
   }
