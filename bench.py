@@ -233,10 +233,14 @@ def run_reference(a):
     steps, warm = max(1, a.steps), max(0, a.warmup)
     per_step = max(0.5, a.cpu_seconds * 2 / (steps + warm))
     stride = max(1, n // 1024)
-    t1 = time.perf_counter()
-    oracle.tc_count_lower_sample(loff, lcols, stride, 0, nthreads)
-    dt = time.perf_counter() - t1
-    stride = max(1, int(stride * dt / per_step)) if dt > 0 else stride
+    for _ in range(3):  # calibrate the stride to about per_step seconds (phase 1: vertex 0 is the top hub)
+        t1 = time.perf_counter()
+        oracle.tc_count_lower_sample(loff, lcols, stride, 1, nthreads)
+        dt = time.perf_counter() - t1
+        if dt > per_step / 4 or stride == 1:
+            break
+        stride = max(1, int(stride * dt / per_step * 1.2)) if dt > 0 else stride // 16
+    stride = max(1, int(round(stride * dt / per_step))) if dt > 0 else stride
     for i in range(warm):
         oracle.tc_count_lower_sample(loff, lcols, stride, i % stride, nthreads)
     edges, secs = 0, 0.0
