@@ -60,6 +60,18 @@ def test_argument_checks_without_gpu():
     assert lib.atc_gen_rmat_host(4, 1, 900000, 190000, 190000, 1, buf.ctypes.data, 1) == atc.Status.ERR_INVALID
     with pytest.raises(atc.ATCError):
         atc.simplify(np.array([[-1, 2]], dtype=np.int32))
+    # parts: a part outside [0, nparts) and zero parts are refused before any device work
+    rng = (C.c_int64 * 2)()
+    assert lib.atc_tc_part(C.byref(st), 0, None, 3, 3, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_tc_part(C.byref(st), 0, None, 0, 0, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_tc_part(None, 0, None, 0, 1, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_csr_host_resident(None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_csr_host_resident(C.byref(st), None) == atc.Status.ERR_INVALID  # not built by the library
+    assert lib.atc_csr_load_host(b"/nonexistent/g.atccsr", C.byref(st), None) == atc.Status.ERR_INVALID
+    # unknown relabel kind
+    pairs = np.array([[0, 1], [1, 2]], dtype=np.int32)
+    lookup = np.zeros(3, dtype=np.int32)
+    assert lib.atc_relabel(pairs.ctypes.data, 2, 9, lookup.ctypes.data, None, None, None) == atc.Status.ERR_INVALID
 
 
 def test_csr_free_is_idempotent():
