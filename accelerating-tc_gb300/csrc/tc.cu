@@ -673,9 +673,22 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
 using namespace atc;
 
 // Counts the edges [e0, e1) of the CSR (every edge for the whole count).
+// ATC_KERNEL_AUTO: the Bisson-style or the Hu-style count, whichever this cost model of
+// their GB300 times predicts is faster for the CSR.  Bisson-style: 1.232 ps per probe of the
+// shorter lists (W_min) + 117.5 ps per edge (grouping, items) + 0.3 ms per call (two more
+// passes and one more host synchronisation); Hu-style: 1.097 ps per wedge (W) + 103.5 ps per
+// edge.  Fitted to R-MAT scale 24 (117 / 231 ms) and Chung-Lu graphs of 4M-46M edges; the
+// learned selector (atc_select) chooses among all kernels and pipelines instead.
+static atc_kernel auto_kernel(const atc_csr* csr) {
+  const double m = (double)csr->m, w = (double)csr->wedges, wmin = (double)csr->wedges_min;
+  const double bisson_ps = 1.232 * wmin + 117.5 * m + 3.0e8;
+  const double hu_ps = 1.097 * w + 103.5 * m;
+  return hu_ps < bisson_ps ? ATC_KERNEL_HU : ATC_KERNEL_BISSON;
+}
+
 static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, int64_t e0, int64_t e1,
                             uint64_t* count, atc_stats* stats, cudaStream_t s) {
-  if (kernel == ATC_KERNEL_AUTO) kernel = ATC_KERNEL_BISSON;
+  if (kernel == ATC_KERNEL_AUTO) kernel = auto_kernel(csr);
   CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
   int launches = 0;
   EventTimer tm;

@@ -95,7 +95,8 @@ typedef enum atc_relabel_kind {
 } atc_relabel_kind;
 
 typedef enum atc_kernel {
-  ATC_KERNEL_AUTO = 0,    /* library default for the graph */
+  ATC_KERNEL_AUTO = 0,    /* Bisson- or Hu-style, whichever a cost model of their GB300 times
+                             (W, W_min and m of the CSR) predicts is faster */
   ATC_KERNEL_HU = 1,      /* wedge walk, N+(u) staged in shared memory (Hu/tc.cu:69-201) */
   ATC_KERNEL_BISSON = 2,  /* bitmap for large N+(u), search otherwise (Bisson/tc.cu:18-104) */
   ATC_KERNEL_FOX = 3,     /* edge bins with 1..32 threads per edge (Fox/tc.cu:64-125,316-384) */
