@@ -33,26 +33,6 @@ namespace atc {
 namespace {
 
 
-// Number of elements < x in a sorted list (lower bound), list in any address space.
-__device__ __forceinline__ bool bsearch_has(const int32_t* a, int64_t n, int32_t x) {
-  int64_t lo = 0, hi = n;
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    int32_t y = a[mid];
-    if (y < x) lo = mid + 1; else hi = mid;
-  }
-  return lo < n && a[lo] == x;
-}
-
-__device__ __forceinline__ bool bsearch_has32(const int32_t* a, int n, int32_t x) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (a[mid] < x) lo = mid + 1; else hi = mid;
-  }
-  return lo < n && a[lo] == x;
-}
-
 // ============================== part split ===========================================
 // Work of edge e for cutting the edges into parts: the shorter list it streams, plus one.
 // work[m] = 0, so that an exclusive scan of m + 1 entries ends with the total.
