@@ -83,26 +83,23 @@ __global__ void __launch_bounds__(kTriWarps * 32) tricore_kernel(CsrView g, unsi
     const int32_t* Bl = g.cols + (du >= dv ? av : au);
     int64_t da = du >= dv ? du : dv, db = du >= dv ? dv : du;
     if (db == 0) continue;
-    // P pivots: 32, or for a shorter list than 32 the power of two that covers it (each of its
-    // elements needs no finer bracket than one pivot gap)
-    const int P = db >= 32 ? 32 : 1 << (32 - __clz((int)db - 1 | 1));
-    if (lane < P) piv[w][lane] = A[(int64_t)lane * da / P];
+    piv[w][lane] = A[(int64_t)lane * da / 32];
     __syncwarp();
     // a lane's elements ascend: `prev` = where its previous element's search ended, a
     // lower bound for the next one inside any bracket
     int64_t prev = 0;
     for (int64_t j = lane; j < db; j += 32) {
       int32_t x = __ldg(Bl + j);
-      // lo = number of pivots <= x
-      int lo = 0, hi = P;
+      // k = number of pivots <= x
+      int lo = 0, hi = 32;
       while (lo < hi) {
         int mid = (lo + hi) >> 1;
         if (piv[w][mid] <= x) lo = mid + 1; else hi = mid;
       }
       if (lo == 0) continue;                 // x < A[0]
       if (piv[w][lo - 1] == x) { ++cnt; continue; }
-      int64_t b = (int64_t)(lo - 1) * da / P + 1;  // strictly inside the bracket
-      int64_t e2 = lo == P ? da : (int64_t)lo * da / P;
+      int64_t b = (int64_t)(lo - 1) * da / 32 + 1;  // strictly inside the bracket
+      int64_t e2 = lo == 32 ? da : (int64_t)lo * da / 32;
       if (prev > b) b = prev;
       while (b < e2) {  // lower bound of x in A[b, e2)
         const int64_t mid = (b + e2) >> 1;
