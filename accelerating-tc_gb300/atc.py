@@ -156,6 +156,8 @@ _SIGS = {
     "atc_relabel": (C.c_int, [_P, C.c_uint64, C.c_int, _P, _P, _P, _P]),
     "atc_tc": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_tc_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_uint64), _P]),
+    "atc_kcl_part": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint64),
+                               C.POINTER(C.c_int64), C.POINTER(StatsStruct), _P]),
     "atc_tc_part": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.c_uint32, C.c_uint32,
                               C.POINTER(C.c_uint64), C.POINTER(C.c_int64), C.POINTER(StatsStruct), _P]),
     "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
@@ -390,6 +392,15 @@ def tc_part(csr: CSR, part, nparts, kernel=Kernel.AUTO, tuning=None, stream=None
     st = StatsStruct()
     _check(lib().atc_tc_part(C.byref(csr.struct), int(kernel), _tuning(tuning), part, nparts, C.byref(cnt), rng,
                              C.byref(st), stream))
+    return cnt.value, (rng[0], rng[1]), _stats(st)
+
+
+def kcl_part(csr: CSR, k, part, nparts, stream=None):
+    """atc_kcl_part: (k-cliques of part `part` of `nparts` edge ranges, (first, last) edge, stats)."""
+    cnt = C.c_uint64(0)
+    rng = (C.c_int64 * 2)()
+    st = StatsStruct()
+    _check(lib().atc_kcl_part(C.byref(csr.struct), k, part, nparts, C.byref(cnt), rng, C.byref(st), stream))
     return cnt.value, (rng[0], rng[1]), _stats(st)
 
 

@@ -72,6 +72,10 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
 atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int kind,
                           int32_t* lookup, int2* oriented, cudaStream_t s);
 
+// Edge range [range[0], range[1]) of part `part` of `nparts` contiguous ranges of equal work
+// (sum over the edges of min(outdeg u, outdeg v) + 1) of a CSR built by the library.
+atc_status part_edge_range(const atc_csr* csr, uint32_t part, uint32_t nparts, int64_t* range, cudaStream_t s);
+
 // GRO order (vertex_ordering/other_order/porder.cpp:141-226) of the directed pairs (device):
 // lookup (n_v ints, device) = new id of every id in [0, n_v).
 atc_status gro_lookup(const int2* pairs, uint64_t ne, int64_t n_v, int32_t* lookup, cudaStream_t s);

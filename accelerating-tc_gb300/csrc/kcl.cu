@@ -93,7 +93,7 @@ __device__ __forceinline__ unsigned long long mask_cliques(const unsigned long l
 // dense (nullable): edges whose C0 has kMaskMax < |C0| <= kDenseMax are appended to
 // dense[1 + ...] (count in dense[0]) for kcl_dense_kernel instead of being walked here.
 __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, const int32_t* cols, const int32_t* esrc,
-                                                          int64_t m, int k, int cap, int32_t* scratch,
+                                                          int64_t e0, int64_t e1, int k, int cap, int32_t* scratch,
                                                           unsigned long long* dense, unsigned long long* out) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t gw = (int64_t)blockIdx.x * kKcWarps + w;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, 
   unsigned long long cnt = 0, bytes = 0;
   int size[kMaxK];
   int idx[kMaxK];
-  for (int64_t e = gw; e < m; e += warps) {
+  for (int64_t e = e0 + gw; e < e1; e += warps) {
     int32_t u = esrc[e], v = cols[e];
     int64_t ub = off[u], ud = off[u + 1] - ub;
     int64_t vb = off[v], vd = off[v + 1] - vb;
@@ -322,16 +322,14 @@ __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t*
 
 using namespace atc;
 
-extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream st) {
-  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
-  ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
-  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
-  cudaStream_t s = as_stream(st);
+// k-cliques whose first two vertices (in orientation order) form an edge of [e0, e1).
+static atc_status kcl_window(const atc_csr* csr, uint32_t k, int64_t e0, int64_t e1, uint64_t* count, atc_stats* stats,
+                             cudaStream_t s) {
   *count = 0;
   unsigned long long h[2] = {0, 0};
   EventTimer tm;
   int launches = 0;
-  if (csr->m > 0) {
+  if (e1 > e0) {
     CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
     int cap = std::max(csr->max_outdeg, 1);
     int levels = (int)k - 2;
@@ -353,7 +351,7 @@ extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, a
     tm.start(s);
     ATC_CK(cudaMemsetAsync(pv->counter, 0, 2 * sizeof(unsigned long long), s));
     if (use_dense) ATC_CK(cudaMemsetAsync(dense.p, 0, 2 * sizeof(unsigned long long), s));
-    kcl_kernel<<<(unsigned)grid, kKcWarps * 32, 0, s>>>(csr->offsets, csr->cols, pv->esrc, csr->m, (int)k, cap,
+    kcl_kernel<<<(unsigned)grid, kKcWarps * 32, 0, s>>>(csr->offsets, csr->cols, pv->esrc, e0, e1, (int)k, cap,
                                                          scratch.p, use_dense ? dense.p + 1 : nullptr, pv->counter);
     ATC_CK(cudaGetLastError());
     launches = 1;
@@ -377,7 +375,7 @@ extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, a
     *count = h[0];
   }
   if (stats) {
-    stats->kernel_ms = csr->m > 0 ? tm.ms() : 0.0f;
+    stats->kernel_ms = e1 > e0 ? tm.ms() : 0.0f;
     stats->total_ms = stats->kernel_ms;
     stats->alg_bytes = h[1];
     stats->wedges = (uint64_t)csr->wedges;
@@ -386,4 +384,28 @@ extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, a
     stats->launches = launches;
   }
   return ATC_OK;
+}
+
+extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
+  ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
+  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  return kcl_window(csr, k, 0, csr->m, count, stats, as_stream(st));
+}
+
+extern "C" atc_status atc_kcl_part(const atc_csr* csr, uint32_t k, uint32_t part, uint32_t nparts, uint64_t* count,
+                                   int64_t* edge_range, atc_stats* stats, atc_stream st) {
+  ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
+  ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
+  ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  ATC_CHECK_ARG(nparts >= 1 && part < nparts, "part must be in [0, nparts)");
+  cudaStream_t s = as_stream(st);
+  *count = 0;
+  int64_t b[2];
+  ATC_TRY(part_edge_range(csr, part, nparts, b, s));
+  if (edge_range) {
+    edge_range[0] = b[0];
+    edge_range[1] = b[1];
+  }
+  return kcl_window(csr, k, b[0], b[1], count, stats, s);
 }

@@ -652,6 +652,26 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
 
 using namespace atc;
 
+atc_status atc::part_edge_range(const atc_csr* csr, uint32_t part, uint32_t nparts, int64_t* range, cudaStream_t s) {
+  range[0] = 0;
+  range[1] = csr->m;
+  if (nparts <= 1 || csr->m == 0) return ATC_OK;
+  CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
+  CsrView g = csr_view(csr->offsets, csr->cols, pv->esrc, csr->n, csr->m);
+  DevBuf<int64_t> work, prefix, bounds;
+  ATC_TRY(work.alloc(csr->m + 1, s));
+  ATC_TRY(prefix.alloc(csr->m + 1, s));
+  ATC_TRY(bounds.alloc(2, s));
+  edge_work_kernel<<<grid_for(csr->m + 1, 256), 256, 0, s>>>(g, work.p);
+  ATC_CK(cudaGetLastError());
+  ATC_TRY(exclusive_scan_i64(work.p, prefix.p, csr->m + 1, s));
+  part_bounds_kernel<<<1, 32, 0, s>>>(prefix.p, csr->m, part, nparts, bounds.p);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaMemcpyAsync(range, bounds.p, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  return ATC_OK;
+}
+
 // Counts the edges [e0, e1) of the CSR (every edge for the whole count).
 // ATC_KERNEL_AUTO: the Bisson-style or the Hu-style count, whichever this cost model of
 // their GB300 times predicts is faster for the CSR.  Bisson-style: 1.232 ps per probe of the
@@ -722,22 +742,8 @@ extern "C" atc_status atc_tc_part(const atc_csr* csr, atc_kernel kernel, const a
   ATC_CHECK_ARG(nparts >= 1 && part < nparts, "part must be in [0, nparts)");
   cudaStream_t s = as_stream(st);
   *count = 0;
-  int64_t b[2] = {0, csr->m};
-  if (nparts > 1 && csr->m > 0) {
-    CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
-    CsrView g = csr_view(csr->offsets, csr->cols, pv->esrc, csr->n, csr->m);
-    DevBuf<int64_t> work, prefix, bounds;
-    ATC_TRY(work.alloc(csr->m + 1, s));
-    ATC_TRY(prefix.alloc(csr->m + 1, s));
-    ATC_TRY(bounds.alloc(2, s));
-    edge_work_kernel<<<grid_for(csr->m + 1, 256), 256, 0, s>>>(g, work.p);
-    ATC_CK(cudaGetLastError());
-    ATC_TRY(exclusive_scan_i64(work.p, prefix.p, csr->m + 1, s));
-    part_bounds_kernel<<<1, 32, 0, s>>>(prefix.p, csr->m, part, nparts, bounds.p);
-    ATC_CK(cudaGetLastError());
-    ATC_CK(cudaMemcpyAsync(b, bounds.p, sizeof(b), cudaMemcpyDeviceToHost, s));
-    ATC_CK(cudaStreamSynchronize(s));
-  }
+  int64_t b[2];
+  ATC_TRY(part_edge_range(csr, part, nparts, b, s));
   if (edge_range) {
     edge_range[0] = b[0];
     edge_range[1] = b[1];

@@ -303,6 +303,11 @@ atc_status atc_tc_noalloc(const int64_t* offsets_dev, const int32_t* cols_dev, i
 /* k-clique count (k >= 3) of the oriented CSR, exact in uint64.  Replaces
    kcl_gpu_solver(std::string, unsigned k, AccType& total, size_t) (k-clique/kcl.h:6-7). */
 atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream s);
+/* One part of the k-clique count: the cliques whose first two vertices (in orientation order)
+   form an edge of part `part` of the work-balanced edge ranges of atc_tc_part; the counts of
+   parts 0..nparts-1 add up to atc_kcl's (sharding by the clique's first edge). */
+atc_status atc_kcl_part(const atc_csr* csr, uint32_t k, uint32_t part, uint32_t nparts, uint64_t* count,
+                        int64_t* edge_range, atc_stats* stats, atc_stream s);
 
 /* ---- batched counting --------------------------------------------------------------
    Many graphs of uneven sizes counted together.  No counterpart in the reference, which

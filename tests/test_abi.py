@@ -65,6 +65,10 @@ def test_argument_checks_without_gpu():
     assert lib.atc_tc_part(C.byref(st), 0, None, 3, 3, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
     assert lib.atc_tc_part(C.byref(st), 0, None, 0, 0, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
     assert lib.atc_tc_part(None, 0, None, 0, 1, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_kcl_part(C.byref(st), 4, 3, 3, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_kcl_part(C.byref(st), 4, 0, 0, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_kcl_part(C.byref(st), 2, 0, 1, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
+    assert lib.atc_kcl_part(None, 4, 0, 1, C.byref(cnt), rng, None, None) == atc.Status.ERR_INVALID
     assert lib.atc_csr_host_resident(None, None) == atc.Status.ERR_INVALID
     assert lib.atc_csr_host_resident(C.byref(st), None) == atc.Status.ERR_INVALID  # not built by the library
     assert lib.atc_csr_load_host(b"/nonexistent/g.atccsr", C.byref(st), None) == atc.Status.ERR_INVALID

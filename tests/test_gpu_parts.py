@@ -1,5 +1,5 @@
-"""Counting in parts (atc_tc_part): the work-balanced edge ranges of a CSR tile it, and the
-part counts add up to the whole count for every kernel family.  This is the sharding
+"""Counting in parts (atc_tc_part, atc_kcl_part): the work-balanced edge ranges of a CSR tile
+it, and the part counts add up to the whole count for every kernel family and for k-cliques.  This is the sharding
 unit of a count spread over several GPUs; here the parts run one after another on one GPU.
 """
 import pytest
@@ -64,3 +64,26 @@ def test_more_parts_than_edges_and_bad_arguments():
         atc.tc_part(csr, 3, 3)
     with pytest.raises(atc.ATCError):
         atc.tc_part(csr, 0, 0)
+
+
+def test_kclique_parts_add_up():
+    # R-MAT s12 with 32 edges a vertex has candidate sets above 64 (the dense path at k >= 5)
+    g = atc.rmat_graph(12, 32, 8)
+    csr = atc.pretc(g, atc.Dir.ADIRECTION, atc.Order.AORDER)
+    tc_ranges = [atc.tc_part(csr, p, 5)[1] for p in range(5)]
+    for k in (3, 4, 5):
+        want = atc.kcl(csr, k)[0]
+        assert want == oracle.kclique(g, k)
+        for nparts in (1, 2, 5):
+            total, prev = 0, 0
+            for p in range(nparts):
+                c, (e0, e1), _ = atc.kcl_part(csr, k, p, nparts)
+                assert e0 == prev and e1 >= e0
+                if nparts == 5:
+                    assert (e0, e1) == tc_ranges[p]
+                prev = e1
+                total += c
+            assert prev == csr.m
+            assert total == want, (k, nparts)
+    with pytest.raises(atc.ATCError):
+        atc.kcl_part(csr, 4, 2, 2)
