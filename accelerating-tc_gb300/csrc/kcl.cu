@@ -182,52 +182,77 @@ __global__ void __launch_bounds__(kKcWarps * 32) kcl_kernel(const int64_t* off, 
   }
 }
 
-// (d)-cliques of the DAG whose successor bitmaps are A (rows of `words` uint64) among
-// the members in `mask`: cliq(1, M) = |M|, cliq(d, M) = sum_{i in M} cliq(d-1, M & A[i]).
-// One thread, an explicit stack of candidate masks.
-__device__ unsigned long long dense_cliques(const unsigned long long* A, int words, const unsigned long long* mask,
-                                            int d) {
-  unsigned long long stack[kMaxK][kDenseWords];
-  int pos[kMaxK];  // next member index to try at each depth
+// Position of the r-th (from 0) set bit of x; x has more than r set bits.
+__device__ __forceinline__ int select_bit(unsigned long long x, int r) {
+  int pos = 0;
+#pragma unroll
+  for (int s = 32; s > 0; s >>= 1) {
+    const int c = __popcll(x & ((1ull << s) - 1));
+    if (r >= c) {
+      r -= c;
+      x >>= s;
+      pos += s;
+    }
+  }
+  return pos;
+}
+
+// d-cliques (d >= 1) among the common higher neighbours of members i < j of C0, in the
+// graph whose rows U (`words` uint64 each) hold every member's higher-indexed neighbours:
+// cliq(1, M) = |M|, cliq(d, M) = sum_{x in M} cliq(d-1, M & U[x]).  Every set below holds
+// members above the last one chosen only, so the word loops start at that member's word.
+// One thread, an explicit stack of candidate sets.
+__device__ unsigned long long pair_cliques(const unsigned long long* U, int words, int i, int j, int d) {
+  const unsigned long long* Ri = U + (size_t)i * words;
+  const unsigned long long* Rj = U + (size_t)j * words;
+  const int w0 = (j + 1) >> 6;
   if (d == 1) {
     unsigned long long c = 0;
-    for (int w = 0; w < words; ++w) c += __popcll(mask[w]);
+    for (int w = w0; w < words; ++w) c += __popcll(Ri[w] & Rj[w]);
     return c;
   }
-  for (int w = 0; w < words; ++w) stack[0][w] = mask[w];
-  pos[0] = 0;
+  unsigned long long st[kMaxK - 4][kDenseWords];
+  int pos[kMaxK - 4];
+  int n0 = 0;
+  for (int w = w0; w < words; ++w) {
+    st[0][w] = Ri[w] & Rj[w];
+    n0 += __popcll(st[0][w]);
+  }
+  if (n0 < d) return 0;
+  pos[0] = j + 1;
   int top = 0;
   unsigned long long total = 0;
   const int nbits = words * 64;
   while (top >= 0) {
-    // next member i >= pos[top] of stack[top]
-    int i = -1;
+    // next member x >= pos[top] of st[top]
+    int x = -1;
     for (int b = pos[top]; b < nbits;) {
-      const unsigned long long word = stack[top][b >> 6] >> (b & 63);
+      const unsigned long long word = st[top][b >> 6] >> (b & 63);
       if (word) {
-        i = b + __ffsll(word) - 1;
+        x = b + __ffsll(word) - 1;
         break;
       }
       b = (b | 63) + 1;
     }
-    if (i < 0) {
+    if (x < 0) {
       --top;
       continue;
     }
-    pos[top] = i + 1;
-    const unsigned long long* row = A + (size_t)i * words;
-    const int left = d - 1 - top;  // members still to choose after i
+    pos[top] = x + 1;
+    const unsigned long long* Rx = U + (size_t)x * words;
+    const int wx = (x + 1) >> 6;
+    const int left = d - 1 - top;  // members still to choose after x
     if (left == 1) {
-      for (int w = 0; w < words; ++w) total += __popcll(stack[top][w] & row[w]);
+      for (int w = wx; w < words; ++w) total += __popcll(st[top][w] & Rx[w]);
     } else {
       int c = 0;
-      for (int w = 0; w < words; ++w) {
-        stack[top + 1][w] = stack[top][w] & row[w];
-        c += __popcll(stack[top + 1][w]);
+      for (int w = wx; w < words; ++w) {
+        st[top + 1][w] = st[top][w] & Rx[w];
+        c += __popcll(st[top + 1][w]);
       }
       if (c >= left) {
         ++top;
-        pos[top] = 0;
+        pos[top] = x + 1;
       }
     }
   }
@@ -235,16 +260,22 @@ __device__ unsigned long long dense_cliques(const unsigned long long* A, int wor
 }
 
 // Edges whose C0 = N+(u) ∩ N+(v) holds kMaskMax < |C0| <= kDenseMax members, a CTA per
-// edge: C0 in shared memory (sorted, as N+(u) is), the DAG induced on it as successor
-// bitmaps (row i: the members of N+(C0[i]), found by binary search in C0), then thread t
-// counts the (k-2)-cliques whose first vertex is C0[i] for i = t, t + 256, ... with
-// AND / popc over the rows: cliques are counted in words of 64 instead of listed.
+// edge.  C0 goes to shared memory (sorted by id, as N+(u) is) and the graph induced on it
+// to bitmap rows: row i = the members above i adjacent to C0[i] (each oriented edge
+// x -> y inside C0 found by a binary search of y in C0, recorded at the lower index of the
+// two).  A (k-2)-clique of C0 is then counted once, from its two lowest members i < j:
+// the CTA deals the adjacent pairs (i, j) over its threads by a prefix sum of the row
+// popcounts, and each thread counts the (k-4)-cliques of row i AND row j with AND / popc
+// over 64-member words.  The pairs, not the rows, are the unit, so a dense core's few
+// heavy rows are spread over every thread.
+static_assert(kDenseMax == 4 * kDenseThreads, "the row scan gives each thread four rows");
 __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t* off, const int32_t* cols,
                                                                   const int32_t* esrc, const unsigned long long* dense,
                                                                   int k, int cmax, unsigned long long* next,
                                                                   unsigned long long* out) {
   extern __shared__ unsigned long long dsm[];  // rows: cmax * words
   __shared__ int32_t C[kDenseMax];
+  __shared__ int pre[kDenseMax + 1];
   __shared__ int wcount[kDenseThreads / 32];
   __shared__ int csize;
   __shared__ unsigned long long item;
@@ -287,7 +318,7 @@ __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t*
     const int words = (c + 63) >> 6;
     for (int t = threadIdx.x; t < c * words; t += kDenseThreads) dsm[t] = 0ull;
     __syncthreads();
-    // row i = members of C that are in N+(C[i]); a warp per row, lanes over N+(C[i])
+    // the edges inside C0: a warp per member x = C[i], lanes over N+(x)
     for (int i = w; i < c; i += nw) {
       const int64_t xb = off[C[i]], xd = off[C[i] + 1] - xb;
       if (lane == 0) bytes += 4ull * (unsigned long long)xd;
@@ -298,12 +329,61 @@ __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t*
           const int mid = (lo + hi) >> 1;
           if (C[mid] < y) lo = mid + 1; else hi = mid;
         }
-        if (lo < c && C[lo] == y) atomicOr(&dsm[(size_t)i * words + (lo >> 6)], 1ull << (lo & 63));
+        if (lo < c && C[lo] == y) {
+          const int a = min(i, lo), z = max(i, lo);
+          atomicOr(&dsm[(size_t)a * words + (z >> 6)], 1ull << (z & 63));
+        }
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < c; i += kDenseThreads)
-      cnt += dense_cliques(dsm, words, dsm + (size_t)i * words, k - 3);
+    // pre[i] = adjacent pairs in rows below i: four rows a thread, a warp scan, warp sums
+    int rc[4], mine = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = 4 * threadIdx.x + q;
+      rc[q] = 0;
+      if (i < c)
+        for (int x = (i + 1) >> 6; x < words; ++x) rc[q] += __popcll(dsm[(size_t)i * words + x]);
+      mine += rc[q];
+    }
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wcount[w] = incl;
+    __syncthreads();
+    int run = incl - mine;
+    for (int q = 0; q < w; ++q) run += wcount[q];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = 4 * threadIdx.x + q;
+      if (i < c) pre[i] = run;
+      run += rc[q];
+    }
+    if (threadIdx.x == kDenseThreads - 1) pre[c] = run;  // every pair
+    __syncthreads();
+    const int npairs = pre[c];
+    for (int p = threadIdx.x; p < npairs; p += kDenseThreads) {
+      // row i: the last with pre[i] <= p (pre[c] > p); j = its (p - pre[i])-th member
+      int lo = 0, hi = c;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pre[mid] <= p) lo = mid; else hi = mid;
+      }
+      const int i = lo;
+      const unsigned long long* Ri = dsm + (size_t)i * words;
+      int r = p - pre[i];
+      int x = (i + 1) >> 6;
+      for (;; ++x) {
+        const int pc = __popcll(Ri[x]);
+        if (r < pc) break;
+        r -= pc;
+      }
+      const int j = x * 64 + select_bit(Ri[x], r);
+      cnt += pair_cliques(dsm, words, i, j, k - 4);
+    }
     __syncthreads();
   }
   for (int o = 16; o > 0; o >>= 1) {
