@@ -13,6 +13,8 @@
 // When |C0| <= 64 (every RGG edge, most R-MAT edges) the warp instead builds the 64-bit
 // successor masks of the DAG induced on C0 with one ballot per member, and each lane
 // counts the remaining (k-2)-cliques of its first member with AND / popc on registers.
+// From k = 5 on, edges with 64 < |C0| <= 1024 go to a second kernel, a CTA per edge, that
+// counts the (k-2)-cliques of C0 from bitmap rows in shared memory (kcl_dense_kernel).
 //
 // Orientation is acyclic, so every k-clique is found once, from its first two vertices
 // in orientation order — the same count kcl_gpu_solver accumulates.  Intersections:
