@@ -58,7 +58,7 @@ constexpr int kMaxK = 16;
 constexpr int kMaskMax = 64;     // candidate sets up to this size use the warp's bitmask path
 constexpr int kDenseMax = 1024;  // larger ones up to this size: a CTA per edge, bitmaps in shared memory
 constexpr int kDenseWords = kDenseMax / 64;
-constexpr int kDenseThreads = 256;
+constexpr int kDenseThreads = 1024;  // 256: R-MAT s20 k = 6 4.84 s; 512: 3.81 s; 1024: 3.70 s
 
 // d-cliques inside `mask` of the DAG whose successor sets (within C0) are adj[]:
 // cliq(1, M) = |M|, cliq(d, M) = sum_{i in M} cliq(d-1, M & adj[i]).  Iterative, one
@@ -270,7 +270,8 @@ __device__ unsigned long long pair_cliques(const unsigned long long* U, int word
 // popcounts, and each thread counts the (k-4)-cliques of row i AND row j with AND / popc
 // over 64-member words.  The pairs, not the rows, are the unit, so a dense core's few
 // heavy rows are spread over every thread.
-static_assert(kDenseMax == 4 * kDenseThreads, "the row scan gives each thread four rows");
+constexpr int kDenseRows = kDenseMax / kDenseThreads;  // rows a thread sums in the row scan
+static_assert(kDenseRows * kDenseThreads == kDenseMax, "the row scan covers kDenseMax rows");
 __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t* off, const int32_t* cols,
                                                                   const int32_t* esrc, const unsigned long long* dense,
                                                                   int k, int cmax, unsigned long long* next,
@@ -338,11 +339,11 @@ __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t*
       }
     }
     __syncthreads();
-    // pre[i] = adjacent pairs in rows below i: four rows a thread, a warp scan, warp sums
-    int rc[4], mine = 0;
+    // pre[i] = adjacent pairs in rows below i: kDenseRows rows a thread, a warp scan, warp sums
+    int rc[kDenseRows], mine = 0;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = 4 * threadIdx.x + q;
+    for (int q = 0; q < kDenseRows; ++q) {
+      const int i = kDenseRows * threadIdx.x + q;
       rc[q] = 0;
       if (i < c)
         for (int x = (i + 1) >> 6; x < words; ++x) rc[q] += __popcll(dsm[(size_t)i * words + x]);
@@ -359,8 +360,8 @@ __global__ void __launch_bounds__(kDenseThreads) kcl_dense_kernel(const int64_t*
     int run = incl - mine;
     for (int q = 0; q < w; ++q) run += wcount[q];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = 4 * threadIdx.x + q;
+    for (int q = 0; q < kDenseRows; ++q) {
+      const int i = kDenseRows * threadIdx.x + q;
       if (i < c) pre[i] = run;
       run += rc[q];
     }
