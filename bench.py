@@ -253,7 +253,7 @@ def run_reference(a):
     cfg = workload_config(a)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": steps,
-        "warmup": warm, "ms_per_step": secs / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": warm, "ms_per_step": secs / steps * 1e3, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded R-MAT)", "config": cfg,
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": "per step every %d-th vertex u with all its smaller-neighbour edges "
