@@ -139,6 +139,27 @@ def test_kclique_identities():
     assert oracle.kclique(g, 3) == oracle.tc_count(g)
 
 
+def test_kclique_oracle_matches_networkx():
+    # the oracle's DFS against an independent clique enumeration, k = 4..6
+    nx = pytest.importorskip("networkx")
+    import atc
+    rng = np.random.default_rng(11)
+    graphs = [atc.rmat_graph(9, 8, 3), atc.rmat_graph(8, 16, 4)]
+    er = rng.integers(0, 120, size=(1500, 2)).astype(np.int32)
+    graphs.append(atc.simplify(er, symmetric=True))
+    for g in graphs:
+        G = nx.Graph()
+        G.add_edges_from(map(tuple, g.tolist()))
+        G.remove_edges_from(nx.selfloop_edges(G))
+        want = {}
+        for cl in nx.enumerate_all_cliques(G):
+            if len(cl) > 6:
+                break
+            want[len(cl)] = want.get(len(cl), 0) + 1
+        for k in (4, 5, 6):
+            assert oracle.kclique(g, k) == want.get(k, 0), k
+
+
 def test_hu_csr_matches_reference_rules():
     # Hu's preTC CSR on a once-per-edge list: every vertex of degree >= 2 kept, lists
     # oriented low degree -> high degree (ties: larger id is the source), sorted.
