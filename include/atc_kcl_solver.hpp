@@ -1,8 +1,8 @@
 /* Source-level drop-in for the reference's k-clique entry point,
      void kcl_gpu_solver(std::string filename, unsigned k, AccType& total, size_t N_CHUNK = 1);
-   (k-clique/kcl.h:6-7, defined in k-clique/kcl.cu:147-215).  A program written against it
-   (k-clique/kcl_gpu.cpp) includes this header instead of kcl.h and links libatc instead of
-   Pangolin/Galois.
+   (k-clique/kcl.h:6-7, defined in k-clique/kcl.cu:147-215).  A caller of the solver (such as
+   k-clique/kcl_gpu.cpp:28-29) includes this header instead of kcl.h and links libatc instead
+   of Pangolin's solver.
 
    Same name and argument meaning: the graph file (a Galois .gr file, the reference's input, or
    an int32 pair file), k, and an accumulator to which the number of k-cliques is ADDED, as the
