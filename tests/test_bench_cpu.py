@@ -1,5 +1,6 @@
-"""The benchmark's reference arm (CPU, no GPU needed): one JSON line with the contract's keys,
-on the same metric, unit, config and direction as the GPU arm, at a small R-MAT scale."""
+"""The benchmark's CPU parts (no GPU needed): the reference arm's JSON line carries the
+contract's keys on the GPU arm's metric, unit, config and direction (small R-MAT scale), and
+the k-clique CPU baseline calibrates its sample."""
 import json
 import os
 import subprocess
@@ -26,3 +27,18 @@ def test_reference_arm_line():
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["kind"] in ("port", "reference")
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_kcl_cpu_sample_is_calibrated():
+    # the k-clique CPU baseline lowers its stride from a sparse first sample towards the target
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    import atc
+    g = atc.rmat_graph(12, 16, 1)
+    n = int(g.max()) + 1
+    t0 = time.perf_counter()
+    s = bench.kcl_cpu_sample(g, 4, n, 0.5)
+    assert time.perf_counter() - t0 < 30
+    assert set(s) == {"stride", "edges", "seconds", "edges_per_s", "cores", "kind"}
+    assert 1 <= s["stride"] < n // 16 and s["edges"] > 0 and s["kind"] == "port"
