@@ -123,3 +123,33 @@ def test_read_edges_pair_file_and_errors(tmp_path):
         atc.read_edges(trunc)
     with pytest.raises(atc.ATCError):
         atc.read_edges(tmp_path / "missing.bin")
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    # sizeof / offsetof of every struct of atc.h, from a C compiler, against the ctypes mirrors
+    import os
+    import shutil
+    import subprocess
+    from conftest import ROOT
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"atc_tuning": atc.Tuning, "atc_csr": atc.CSRStruct, "atc_stats": atc.StatsStruct}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "atc.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (ln.split() for ln in out if ln)}
+    for cname, py in mirrors.items():
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
