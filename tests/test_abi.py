@@ -125,8 +125,9 @@ def test_read_edges_pair_file_and_errors(tmp_path):
         atc.read_edges(tmp_path / "missing.bin")
 
 
-def test_struct_layouts_match_the_header(tmp_path):
-    # sizeof / offsetof of every struct of atc.h, from a C compiler, against the ctypes mirrors
+def test_struct_layouts_and_enums_match_the_header(tmp_path):
+    # sizeof / offsetof of every struct of atc.h and the value of every enumerator, from a C
+    # compiler, against the ctypes mirrors
     import os
     import shutil
     import subprocess
@@ -140,6 +141,11 @@ def test_struct_layouts_match_the_header(tmp_path):
         lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
         for f, _ in py._fields_:
             lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    enums = {"ATC_": atc.Status, "ATC_DIR_": atc.Dir, "ATC_ORDER_": atc.Order, "ATC_RELABEL_": atc.Relabel,
+             "ATC_KERNEL_": atc.Kernel}
+    for prefix, py in enums.items():
+        for e in py:
+            lines.append('printf("enum %s%s %%d\\n", (int)%s%s);' % (prefix, e.name, prefix, e.name))
     lines += ["return 0;", "}"]
     src = tmp_path / "layout.c"
     src.write_text("\n".join(lines))
@@ -149,6 +155,9 @@ def test_struct_layouts_match_the_header(tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
     got = {(a, b): int(c) for a, b, c in (ln.split() for ln in out if ln)}
+    for prefix, py in enums.items():
+        for e in py:
+            assert got[("enum", prefix + e.name)] == int(e), prefix + e.name
     for cname, py in mirrors.items():
         assert got[(cname, "sizeof")] == C.sizeof(py), cname
         for f, _ in py._fields_:
