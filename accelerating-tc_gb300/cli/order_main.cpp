@@ -51,8 +51,26 @@ static bool write_pairs(const char* path, const int32_t* p, size_t n) {
   return w == n;
 }
 
+// Arguments of each program, as its reference counterpart takes them.
+#if defined(ATC_PROGRAM_COST_FUNC_CAL)
+static const char* const kArgs = "<edges.bin> <k>";
+static const int kMinArgc = 3;
+#elif defined(ATC_PROGRAM_PEEL)
+static const char* const kArgs = "inputFileName outFileName [--compat]";
+static const int kMinArgc = 3;
+#elif defined(ATC_PROGRAM_KCORE_DIRECTION)
+static const char* const kArgs = "<in.u64> <out.u64>";
+static const int kMinArgc = 3;
+#elif defined(ATC_PROGRAM_REORDER)
+static const char* const kArgs = "<graph.u64>";
+static const int kMinArgc = 2;
+#else
+static const char* const kArgs = "<edges.bin>";
+static const int kMinArgc = 2;
+#endif
+
 int main(int argc, char** argv) {
-  if (argc < 2) { fprintf(stderr, "usage: %s <edges.bin>%s\n", argv[0], argc > 2 ? "" : " [k]"); return 2; }
+  if (argc < kMinArgc) { fprintf(stderr, "usage: %s %s\n", argv[0], kArgs); return 2; }
   std::vector<int32_t> pairs;
   if (!read_pairs(argv[1], pairs)) { fprintf(stderr, "cannot read %s\n", argv[1]); return 1; }
   uint64_t np = pairs.size() / 2;
@@ -84,7 +102,6 @@ int main(int argc, char** argv) {
   if (s != ATC_OK) return fail("atc_relabel", s);
   if (!write_pairs("naive", naive.data(), np) || !write_pairs("degreeOrder", naive.data(), 0)) return 1;
 #elif defined(ATC_PROGRAM_COST_FUNC_CAL)
-  if (argc < 3) { fprintf(stderr, "usage: %s <edges.bin> <k>\n", argv[0]); return 2; }
   float c[3];
   s = atc_costfunc(pairs.data(), np, atoi(argv[2]), c, nullptr);
   if (s != ATC_OK) return fail("atc_costfunc", s);
@@ -92,7 +109,6 @@ int main(int argc, char** argv) {
   std::cout << "degreePartCost: " << c[1] << std::endl;
   std::cout << "lpPartCost: " << c[2] << std::endl;
 #elif defined(ATC_PROGRAM_PEEL)
-  if (argc < 3) { fprintf(stderr, "Usage: ./Peel inputFileName outFileName [--compat]\n"); return 2; }
   const int compat = argc > 3 && strcmp(argv[3], "--compat") == 0;
   std::vector<uint64_t> packed(np), out(np ? np : 1);
   if (np) memcpy(packed.data(), pairs.data(), 8 * np);
@@ -104,7 +120,6 @@ int main(int argc, char** argv) {
   std::cout << "iterations " << iters << std::endl;
   if (!write_pairs(argv[2], reinterpret_cast<const int32_t*>(out.data()), np)) return 1;
 #elif defined(ATC_PROGRAM_KCORE_DIRECTION)
-  if (argc < 3) { fprintf(stderr, "usage: %s <in> <out>\n", argv[0]); return 2; }
   // the file's bytes read as little-endian uint64 edges
   std::vector<uint64_t> packed(np), out(np ? np : 1);
   if (np) memcpy(packed.data(), pairs.data(), 8 * np);
