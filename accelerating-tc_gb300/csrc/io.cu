@@ -7,6 +7,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -52,7 +54,8 @@ static bool read_gr_file(const char* path, std::vector<int32_t>& pairs) {
   if ((version != 1 && version != 2) || nodes > 0x7fffffffull) return false;
   const size_t idx_at = 32, dst_at = idx_at + 8 * nodes;
   const size_t dst_size = version == 1 ? 4 : 8;
-  if (raw.size() < dst_at + dst_size * edges) return false;
+  // the header's counts must fit the file (checked by division: a forged count cannot wrap)
+  if (raw.size() < dst_at || edges > (raw.size() - dst_at) / dst_size) return false;
   pairs.resize(2 * edges);
   uint64_t prev = 0;
   for (uint64_t u = 0; u < nodes; ++u) {
@@ -85,7 +88,16 @@ using namespace atc;
 extern "C" atc_status atc_read_edges(const char* path, int32_t* pairs, uint64_t cap, uint64_t* n_out) {
   ATC_CHECK_ARG(path != nullptr && n_out != nullptr, "NULL argument");
   std::vector<int32_t> buf;
-  bool ok = ends_with(path, ".gr") ? read_gr_file(path, buf) : read_pairs_file(path, buf);
+  bool ok;
+  try {
+    ok = ends_with(path, ".gr") ? read_gr_file(path, buf) : read_pairs_file(path, buf);
+  } catch (const std::bad_alloc&) {
+    atc::set_error("out of host memory reading %s", path);
+    return ATC_ERR_OOM;
+  } catch (const std::exception&) {
+    atc::set_error("cannot read %s", path);
+    return ATC_ERR_INVALID;
+  }
   if (!ok) {
     atc::set_error("cannot read %s as %s", path, ends_with(path, ".gr") ? "a Galois .gr file" : "int32 pairs");
     return ATC_ERR_INVALID;

@@ -123,6 +123,17 @@ def test_read_edges_pair_file_and_errors(tmp_path):
         atc.read_edges(trunc)
     with pytest.raises(atc.ATCError):
         atc.read_edges(tmp_path / "missing.bin")
+    # forged headers: an edge count whose byte size wraps, a node count beyond the file,
+    # an unknown version, and end offsets that go down
+    for hdr in ([1, 0, 2, 1 << 62], [2, 0, 1 << 30, 1], [3, 0, 2, 1]):
+        forged = tmp_path / "forged.gr"
+        forged.write_bytes(np.array(hdr + [0, 1, 1, 0], dtype=np.uint64).tobytes())
+        with pytest.raises(atc.ATCError):
+            atc.read_edges(forged)
+    down = tmp_path / "down.gr"
+    down.write_bytes(np.array([2, 0, 2, 1, 1, 0, 1], dtype=np.uint64).tobytes())
+    with pytest.raises(atc.ATCError):
+        atc.read_edges(down)
 
 
 def test_struct_layouts_and_enums_match_the_header(tmp_path):
