@@ -10,6 +10,7 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <vector>
 
 #include "internal.cuh"
@@ -744,16 +745,29 @@ static atc_status csr_load_impl(const char* path, bool host_resident, atc_csr* o
     set_error("cannot open %s", path);
     return ATC_ERR_INVALID;
   }
+  fseek(f, 0, SEEK_END);
+  const long fsize = ftell(f);
+  fseek(f, 0, SEEK_SET);
   char magic[8];
   int64_t h64[5];
   int32_t h32[4];
   bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, atc::kCsrMagic, 8) == 0 && fread(h64, 8, 5, f) == 5 &&
             fread(h32, 4, 4, f) == 4 && h64[0] >= 0 && h64[1] >= 0 && h64[0] < (int64_t)INT32_MAX;
+  // the header's n and m must fit the file (64-byte header, n+1 offsets, m targets), checked
+  // by division so that a forged count cannot wrap or reach the allocations below
+  const int64_t body = (int64_t)fsize - 64;
+  if (ok) ok = body >= 8 * (h64[0] + 1) && h64[1] <= (body - 8 * (h64[0] + 1)) / 4;
   std::vector<int64_t> off;
   std::vector<int32_t> cols;
   if (ok) {
-    off.resize(h64[0] + 1);
-    cols.resize(h64[1]);
+    try {
+      off.resize(h64[0] + 1);
+      cols.resize(h64[1]);
+    } catch (const std::exception&) {
+      fclose(f);
+      set_error("out of host memory reading %s", path);
+      return ATC_ERR_OOM;
+    }
     ok = fread(off.data(), 8, off.size(), f) == off.size() &&
          (cols.empty() || fread(cols.data(), 4, cols.size(), f) == cols.size());
   }

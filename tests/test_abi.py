@@ -72,6 +72,30 @@ def test_argument_checks_without_gpu():
     assert lib.atc_csr_host_resident(None, None) == atc.Status.ERR_INVALID
     assert lib.atc_csr_host_resident(C.byref(st), None) == atc.Status.ERR_INVALID  # not built by the library
     assert lib.atc_csr_load_host(b"/nonexistent/g.atccsr", C.byref(st), None) == atc.Status.ERR_INVALID
+
+
+def test_csr_cache_forged_headers_rejected(tmp_path):
+    # the cache reader checks n and m against the file before allocating or touching a device
+    lib = atc.lib()
+    st = atc.CSRStruct()
+
+    def cache(n, m, body_ints):
+        h = b"ATCCSR01" + np.array([n, m, n, 0, 0], dtype=np.int64).tobytes() + np.zeros(4, np.int32).tobytes()
+        return h + np.array(body_ints, dtype=np.int32).tobytes()
+
+    cases = {
+        "huge_m": cache(2, 1 << 60, [0, 0, 1, 0, 1, 0, 1]),       # m far beyond the file
+        "wrapping_m": cache(2, (1 << 62) + 1, [0, 0, 1, 0, 1, 0, 1]),
+        "short_offsets": cache(1 << 20, 1, [0, 0]),               # n beyond the file
+        "negative_n": cache(-1, 0, []),
+        "bad_order": cache(2, 2, [0, 0, 2, 0, 2, 0, 1, 0]),      # offsets 0, 2, 2 but row 0 is [1, 0]
+        "bad_magic": b"ATCCSR02" + cache(1, 0, [0, 0, 0, 0])[8:],
+    }
+    for name, data in cases.items():
+        p = tmp_path / (name + ".atccsr")
+        p.write_bytes(data)
+        for load in (lib.atc_csr_load, lib.atc_csr_load_host):
+            assert load(str(p).encode(), C.byref(st), None) == atc.Status.ERR_INVALID, name
     # unknown relabel kind
     pairs = np.array([[0, 1], [1, 2]], dtype=np.int32)
     lookup = np.zeros(3, dtype=np.int32)
