@@ -478,7 +478,7 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
 using namespace atc;
 
 extern "C" atc_status atc_aorder(const int32_t* pairs, uint64_t np, int32_t* lookup, int32_t* normal,
-                                 int32_t* reordered, atc_stream st) {
+                                 int32_t* reordered, atc_stream st) try {
   ATC_CHECK_ARG(lookup != nullptr, "lookup is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
   cudaStream_t s = as_stream(st);
@@ -510,10 +510,10 @@ extern "C" atc_status atc_aorder(const int32_t* pairs, uint64_t np, int32_t* loo
   }
   ATC_CK(cudaStreamSynchronize(s));
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel_kind kind, int32_t* lookup,
-                                  int32_t* normal, int32_t* relabeled, atc_stream st) {
+                                  int32_t* normal, int32_t* relabeled, atc_stream st) try {
   ATC_CHECK_ARG(lookup != nullptr, "lookup is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
   ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_GRO, "unknown atc_relabel_kind");
@@ -546,4 +546,4 @@ extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel
   }
   ATC_CK(cudaStreamSynchronize(s));
   return ATC_OK;
-}
+} ATC_CATCH

@@ -46,7 +46,7 @@ extern "C" const char* atc_status_string(atc_status s) {
 
 extern "C" const char* atc_last_error(void) { return atc::g_err; }
 
-extern "C" atc_status atc_init(int device) {
+extern "C" atc_status atc_init(int device) try {
   int count = 0;
   cudaError_t e = cudaGetDeviceCount(&count);
   if (e != cudaSuccess || count == 0) {
@@ -57,4 +57,4 @@ extern "C" atc_status atc_init(int device) {
   ATC_CK(cudaSetDevice(device));
   ATC_CK(cudaFree(nullptr));
   return ATC_OK;
-}
+} ATC_CATCH

@@ -116,18 +116,18 @@ atc_status ensure_union(atc_batch* b, int64_t n, int64_t m, cudaStream_t s) {
 
 using namespace atc;
 
-extern "C" atc_status atc_batch_create(atc_batch** out) {
+extern "C" atc_status atc_batch_create(atc_batch** out) try {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   *out = new atc_batch();
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_batch_reserve(atc_batch* b, int64_t n, int64_t m, atc_stream s) {
+extern "C" atc_status atc_batch_reserve(atc_batch* b, int64_t n, int64_t m, atc_stream s) try {
   ATC_CHECK_ARG(b != nullptr && n >= 0 && m >= 0, "bad argument");
   return ensure_union(b, n, m, as_stream(s));
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_batch_add(atc_batch* b, const atc_csr* csr, int32_t* index, atc_stream st) {
+extern "C" atc_status atc_batch_add(atc_batch* b, const atc_csr* csr, int32_t* index, atc_stream st) try {
   ATC_CHECK_ARG(b != nullptr && csr != nullptr, "NULL argument");
   ATC_CHECK_ARG(b->n + csr->n < (int64_t)INT32_MAX, "batch would exceed 2^31 vertices");
   cudaStream_t s = as_stream(st);
@@ -146,17 +146,17 @@ extern "C" atc_status atc_batch_add(atc_batch* b, const atc_csr* csr, int32_t* i
   b->max_outdeg = std::max(b->max_outdeg, csr->max_outdeg);
   b->dirty = true;
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_batch_info(const atc_batch* b, int32_t* graphs, int64_t* n, int64_t* m) {
+extern "C" atc_status atc_batch_info(const atc_batch* b, int32_t* graphs, int64_t* n, int64_t* m) try {
   ATC_CHECK_ARG(b != nullptr, "NULL batch");
   if (graphs) *graphs = (int32_t)(b->vbase.size() - 1);
   if (n) *n = b->n;
   if (m) *m = b->m;
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_batch_destroy(atc_batch* b) {
+extern "C" atc_status atc_batch_destroy(atc_batch* b) try {
   if (!b) return ATC_OK;
   free_pipeline(b);
   if (b->off) cudaFree(b->off);
@@ -164,7 +164,7 @@ extern "C" atc_status atc_batch_destroy(atc_batch* b) {
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
   delete b;
   return ATC_OK;
-}
+} ATC_CATCH
 
 namespace atc {
 namespace {
@@ -288,7 +288,7 @@ atc_status run_once(atc_batch* b, const ItemShape& sh, uint64_t* counts, float* 
 }  // namespace atc
 
 extern "C" atc_status atc_batch_run(atc_batch* b, const atc_tuning* t, uint64_t* counts, atc_stats* stats,
-                                    atc_stream st) {
+                                    atc_stream st) try {
   ATC_CHECK_ARG(b != nullptr, "NULL batch");
   const int ng = (int)(b->vbase.size() - 1);
   ATC_CHECK_ARG(counts != nullptr || ng == 0, "counts is NULL");
@@ -308,10 +308,10 @@ extern "C" atc_status atc_batch_run(atc_batch* b, const atc_tuning* t, uint64_t*
     stats->launches = 6;
   }
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_batch_tune(atc_batch* b, const atc_tuning* cands, int32_t ncand, int32_t* best, float* ms,
-                                     atc_stream st) {
+                                     atc_stream st) try {
   ATC_CHECK_ARG(b != nullptr && cands != nullptr && ncand > 0 && best != nullptr, "bad argument");
   cudaStream_t s = as_stream(st);
   const int ng = (int)(b->vbase.size() - 1);
@@ -337,4 +337,4 @@ extern "C" atc_status atc_batch_tune(atc_batch* b, const atc_tuning* cands, int3
   }
   b->shape = atc::shape_from(&cands[*best], atc::default_shape(32));
   return ATC_OK;
-}
+} ATC_CATCH

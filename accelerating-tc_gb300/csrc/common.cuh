@@ -5,6 +5,8 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <exception>
+#include <new>
 #include <string>
 
 #include "atc.h"
@@ -24,6 +26,19 @@ void set_error(const char* fmt, ...);
       return e_ == cudaErrorMemoryAllocation ? ATC_ERR_OOM : ATC_ERR_CUDA;            \
     }                                                                                 \
   } while (0)
+
+// Closes a function-try-block around an entry point's body: a host allocation that fails
+// (std::bad_alloc) or any other C++ exception becomes a status, never an exception
+// crossing the C ABI.
+#define ATC_CATCH                                                       \
+  catch (const std::bad_alloc&) {                                       \
+    ::atc::set_error("out of host memory");                             \
+    return ATC_ERR_OOM;                                                 \
+  }                                                                     \
+  catch (const std::exception& ex_) {                                   \
+    ::atc::set_error("%s", ex_.what());                                 \
+    return ATC_ERR_INVALID;                                             \
+  }
 
 #define ATC_TRY(expr)                         \
   do {                                        \

@@ -63,7 +63,7 @@ atc_status upload_pairs(const int32_t* pairs, uint64_t np, DevBuf<int2>* d, int*
 
 using namespace atc;
 
-extern "C" atc_status atc_costfunc(const int32_t* pairs, uint64_t np, int32_t k, float* out, atc_stream st) {
+extern "C" atc_status atc_costfunc(const int32_t* pairs, uint64_t np, int32_t k, float* out, atc_stream st) try {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
   cudaStream_t s = as_stream(st);
@@ -103,9 +103,9 @@ extern "C" atc_status atc_costfunc(const int32_t* pairs, uint64_t np, int32_t k,
   out[1] = dPart;
   out[2] = lpPart;
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_verification(const int32_t* pairs, uint64_t np, float* out, atc_stream st) {
+extern "C" atc_status atc_verification(const int32_t* pairs, uint64_t np, float* out, atc_stream st) try {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
   cudaStream_t s = as_stream(st);
@@ -134,4 +134,4 @@ extern "C" atc_status atc_verification(const int32_t* pairs, uint64_t np, float*
   out[0] = f_lp;
   out[1] = f_deg;
   return ATC_OK;
-}
+} ATC_CATCH

@@ -194,7 +194,7 @@ static bool chunglu_params(uint32_t n, double gamma, double mean_degree, uint64_
 using namespace atc;
 
 extern "C" atc_status atc_gen_chunglu_device(uint32_t n, double gamma, double mean_degree, uint64_t seed,
-                                             int32_t* out_dev, uint64_t capacity, uint64_t* n_out, atc_stream st) {
+                                             int32_t* out_dev, uint64_t capacity, uint64_t* n_out, atc_stream st) try {
   ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
   ChungLu c;
   ATC_CHECK_ARG(chunglu_params(n, gamma, mean_degree, seed, &c), "need n >= 2, gamma > 1.05, 0 < mean degree < n");
@@ -220,10 +220,10 @@ extern "C" atc_status atc_gen_chunglu_device(uint32_t n, double gamma, double me
   ATC_CK(cudaGetLastError());
   ATC_CK(cudaStreamSynchronize(s));
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_gen_rgg_host(uint32_t n, double mean_degree, uint64_t seed, int32_t* out,
-                                       uint64_t capacity, uint64_t* n_out, int nthreads) {
+                                       uint64_t capacity, uint64_t* n_out, int nthreads) try {
   ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
   RggGrid gr;
   ATC_CHECK_ARG(rgg_grid(n, mean_degree, &gr), "need n >= 2 and 0 < mean degree with radius < 0.5");
@@ -278,10 +278,10 @@ extern "C" atc_status atc_gen_rgg_host(uint32_t n, double mean_degree, uint64_t 
     out[2 * k + 1] = all[k].second;
   }
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_gen_rgg_device(uint32_t n, double mean_degree, uint64_t seed, int32_t* out_dev,
-                                         uint64_t capacity, uint64_t* n_out, atc_stream st) {
+                                         uint64_t capacity, uint64_t* n_out, atc_stream st) try {
   ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
   RggGrid gr;
   ATC_CHECK_ARG(rgg_grid(n, mean_degree, &gr), "need n >= 2 and 0 < mean degree with radius < 0.5");
@@ -316,10 +316,10 @@ extern "C" atc_status atc_gen_rgg_device(uint32_t n, double mean_degree, uint64_
     return ATC_ERR_INVALID;
   }
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_gen_rmat_host(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm,
-                                        uint32_t c_ppm, uint64_t seed, int32_t* out, int nthreads) {
+                                        uint32_t c_ppm, uint64_t seed, int32_t* out, int nthreads) try {
   ATC_CHECK_ARG(out != nullptr, "out_pairs is NULL");
   ATC_CHECK_ARG(scale >= 1 && scale <= 30, "scale must be in [1,30]");
   uint32_t t1, t2, t3;
@@ -335,10 +335,10 @@ extern "C" atc_status atc_gen_rmat_host(uint32_t scale, uint32_t edge_factor, ui
     });
   for (auto& x : th) x.join();
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_gen_rmat_device(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm,
-                                          uint32_t c_ppm, uint64_t seed, int32_t* out, atc_stream s) {
+                                          uint32_t c_ppm, uint64_t seed, int32_t* out, atc_stream s) try {
   ATC_CHECK_ARG(out != nullptr, "out_pairs_dev is NULL");
   ATC_CHECK_ARG(scale >= 1 && scale <= 30, "scale must be in [1,30]");
   uint32_t t1, t2, t3;
@@ -350,10 +350,10 @@ extern "C" atc_status atc_gen_rmat_device(uint32_t scale, uint32_t edge_factor, 
   ATC_CK(cudaGetLastError());
   ATC_CK(cudaStreamSynchronize(as_stream(s)));
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_simplify_host(const int32_t* pairs, uint64_t np, int symmetric, int32_t* out,
-                                        uint64_t* n_out) {
+                                        uint64_t* n_out) try {
   ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
   ATC_CHECK_ARG(np == 0 || (pairs != nullptr && out != nullptr), "NULL array");
   std::vector<uint64_t> k;
@@ -374,4 +374,4 @@ extern "C" atc_status atc_simplify_host(const int32_t* pairs, uint64_t np, int s
   }
   *n_out = k.size();
   return ATC_OK;
-}
+} ATC_CATCH

@@ -85,7 +85,7 @@ static bool read_gr_file(const char* path, std::vector<int32_t>& pairs) {
 using namespace atc;
 
 // Two-call pattern: with pairs == nullptr only *n_out is written.
-extern "C" atc_status atc_read_edges(const char* path, int32_t* pairs, uint64_t cap, uint64_t* n_out) {
+extern "C" atc_status atc_read_edges(const char* path, int32_t* pairs, uint64_t cap, uint64_t* n_out) try {
   ATC_CHECK_ARG(path != nullptr && n_out != nullptr, "NULL argument");
   std::vector<int32_t> buf;
   bool ok;
@@ -108,4 +108,4 @@ extern "C" atc_status atc_read_edges(const char* path, int32_t* pairs, uint64_t 
   ATC_CHECK_ARG(cap >= n, "pairs buffer smaller than the file's edge count");
   if (n) memcpy(pairs, buf.data(), 8 * n);
   return ATC_OK;
-}
+} ATC_CATCH

@@ -469,15 +469,15 @@ static atc_status kcl_window(const atc_csr* csr, uint32_t k, int64_t e0, int64_t
   return ATC_OK;
 }
 
-extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream st) {
+extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
   ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
   ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
   return kcl_window(csr, k, 0, csr->m, count, stats, as_stream(st));
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_kcl_part(const atc_csr* csr, uint32_t k, uint32_t part, uint32_t nparts, uint64_t* count,
-                                   int64_t* edge_range, atc_stats* stats, atc_stream st) {
+                                   int64_t* edge_range, atc_stats* stats, atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
   ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
   ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
@@ -491,4 +491,4 @@ extern "C" atc_status atc_kcl_part(const atc_csr* csr, uint32_t k, uint32_t part
     edge_range[1] = b[1];
   }
   return kcl_window(csr, k, b[0], b[1], count, stats, s);
-}
+} ATC_CATCH

@@ -302,7 +302,7 @@ __global__ void feat_loops_kernel(const int2* p, uint64_t np, unsigned long long
 
 using namespace atc;
 
-extern "C" atc_status atc_mlp_create(int32_t n_in, int32_t hidden, int32_t n_out, uint64_t seed, atc_mlp** out) {
+extern "C" atc_status atc_mlp_create(int32_t n_in, int32_t hidden, int32_t n_out, uint64_t seed, atc_mlp** out) try {
   ATC_CHECK_ARG(out != nullptr && n_in > 0 && hidden > 0 && n_out > 0, "bad MLP shape");
   atc_mlp* net = new atc_mlp();
   net->I = n_in;
@@ -341,18 +341,18 @@ extern "C" atc_status atc_mlp_create(int32_t n_in, int32_t hidden, int32_t n_out
   ATC_CK(cudaMemset(net->adam_v, 0, sizeof(float) * net->nparams));
   *out = net;
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_mlp_destroy(atc_mlp* net) {
+extern "C" atc_status atc_mlp_destroy(atc_mlp* net) try {
   if (!net) return ATC_OK;
   cudaFree(net->params);
   cudaFree(net->adam_m);
   cudaFree(net->adam_v);
   delete net;
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_mlp_params(atc_mlp* net, float* get, const float* set, int64_t* count) {
+extern "C" atc_status atc_mlp_params(atc_mlp* net, float* get, const float* set, int64_t* count) try {
   ATC_CHECK_ARG(net != nullptr, "NULL MLP");
   if (count) *count = net->nparams;
   if (set) {
@@ -363,19 +363,19 @@ extern "C" atc_status atc_mlp_params(atc_mlp* net, float* get, const float* set,
   }
   if (get) ATC_CK(cudaMemcpy(get, net->params, sizeof(float) * net->nparams, cudaMemcpyDeviceToHost));
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_mlp_scaling(atc_mlp* net, float* get_mean, float* get_std, const float* set_mean,
-                                      const float* set_std) {
+                                      const float* set_std) try {
   ATC_CHECK_ARG(net != nullptr, "NULL MLP");
   if (set_mean) memcpy(net->mean.data(), set_mean, sizeof(float) * net->I);
   if (set_std) memcpy(net->stdv.data(), set_std, sizeof(float) * net->I);
   if (get_mean) memcpy(get_mean, net->mean.data(), sizeof(float) * net->I);
   if (get_std) memcpy(get_std, net->stdv.data(), sizeof(float) * net->I);
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_mlp_forward(atc_mlp* net, const float* x, int32_t rows, float* y, atc_stream st) {
+extern "C" atc_status atc_mlp_forward(atc_mlp* net, const float* x, int32_t rows, float* y, atc_stream st) try {
   ATC_CHECK_ARG(net != nullptr && x != nullptr && y != nullptr && rows > 0, "bad argument");
   cudaStream_t s = as_stream(st);
   Scratch sc;
@@ -385,10 +385,10 @@ extern "C" atc_status atc_mlp_forward(atc_mlp* net, const float* x, int32_t rows
   ATC_CK(cudaMemcpyAsync(y, sc.y.p, sizeof(float) * rows * net->O, cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_mlp_gradients(atc_mlp* net, const float* x, const float* t, const float* mask, int32_t rows,
-                                        float* grads, float* loss, atc_stream st) {
+                                        float* grads, float* loss, atc_stream st) try {
   ATC_CHECK_ARG(net != nullptr && x != nullptr && t != nullptr && rows > 0, "bad argument");
   cudaStream_t s = as_stream(st);
   Scratch sc;
@@ -400,11 +400,11 @@ extern "C" atc_status atc_mlp_gradients(atc_mlp* net, const float* x, const floa
   if (loss) ATC_CK(cudaMemcpyAsync(loss, sc.loss.p, sizeof(float), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   return ATC_OK;
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_mlp_train(atc_mlp* net, const float* x, const float* t, const float* mask, int32_t rows,
                                     int32_t epochs, int32_t batch, float lr, uint64_t seed, float* final_loss,
-                                    atc_stream st) {
+                                    atc_stream st) try {
   ATC_CHECK_ARG(net != nullptr && x != nullptr && t != nullptr && rows > 0 && epochs > 0, "bad argument");
   cudaStream_t s = as_stream(st);
   const int I = net->I, O = net->O;
@@ -470,9 +470,9 @@ extern "C" atc_status atc_mlp_train(atc_mlp* net, const float* x, const float* t
   ATC_CK(cudaStreamSynchronize(s));
   if (final_loss) *final_loss = last;
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_graph_features(const int32_t* pairs_dev, uint64_t np, float* feat, atc_stream st) {
+extern "C" atc_status atc_graph_features(const int32_t* pairs_dev, uint64_t np, float* feat, atc_stream st) try {
   ATC_CHECK_ARG(feat != nullptr && (np == 0 || pairs_dev != nullptr), "bad argument");
   cudaStream_t s = as_stream(st);
   for (int i = 0; i < 6; ++i) feat[i] = 0.0f;
@@ -522,9 +522,9 @@ extern "C" atc_status atc_graph_features(const int32_t* pairs_dev, uint64_t np, 
   feat[4] = (float)std::log1p((double)h[2]);
   feat[5] = (float)std::log1p(tail > 0 ? tail : 0.0);
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_select(atc_mlp* net, const float* feat, int32_t* choice, float* predicted, atc_stream st) {
+extern "C" atc_status atc_select(atc_mlp* net, const float* feat, int32_t* choice, float* predicted, atc_stream st) try {
   ATC_CHECK_ARG(net != nullptr && feat != nullptr && choice != nullptr, "bad argument");
   std::vector<float> y(net->O);
   ATC_TRY(atc_mlp_forward(net, feat, 1, y.data(), st));
@@ -534,4 +534,4 @@ extern "C" atc_status atc_select(atc_mlp* net, const float* feat, int32_t* choic
   *choice = best;
   if (predicted) memcpy(predicted, y.data(), sizeof(float) * net->O);
   return ATC_OK;
-}
+} ATC_CATCH

@@ -469,13 +469,13 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
 using namespace atc;
 
 extern "C" atc_status atc_pretc_device(const int32_t* pairs_dev, uint64_t np, atc_dir dir, atc_order order,
-                                       const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) {
+                                       const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) try {
   ATC_CHECK_ARG(np == 0 || pairs_dev != nullptr, "pairs_dev is NULL");
   return pretc_impl(reinterpret_cast<const int2*>(pairs_dev), np, dir, order, t, out, perm_out, as_stream(s));
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_pretc(const int32_t* pairs, uint64_t np, atc_dir dir, atc_order order,
-                                const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) {
+                                const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) try {
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
   cudaStream_t st = as_stream(s);
   keep_pool();
@@ -483,18 +483,18 @@ extern "C" atc_status atc_pretc(const int32_t* pairs, uint64_t np, atc_dir dir, 
   ATC_TRY(d.alloc(np, st));
   if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
   return pretc_impl(d.p, np, dir, order, t, out, perm_out, st);
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_csr_to_host(const atc_csr* csr, int64_t* offsets, int32_t* cols, atc_stream s) {
+extern "C" atc_status atc_csr_to_host(const atc_csr* csr, int64_t* offsets, int32_t* cols, atc_stream s) try {
   ATC_CHECK_ARG(csr != nullptr && offsets != nullptr && cols != nullptr, "NULL argument");
   cudaStream_t st = as_stream(s);
   ATC_CK(cudaMemcpyAsync(offsets, csr->offsets, sizeof(int64_t) * (csr->n + 1), cudaMemcpyDeviceToHost, st));
   if (csr->m) ATC_CK(cudaMemcpyAsync(cols, csr->cols, sizeof(int32_t) * csr->m, cudaMemcpyDefault, st));
   ATC_CK(cudaStreamSynchronize(st));
   return ATC_OK;
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_csr_free(atc_csr* csr) {
+extern "C" atc_status atc_csr_free(atc_csr* csr) try {
   if (!csr) return ATC_OK;
   CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
   const bool host = pv && pv->host_cols;
@@ -512,12 +512,12 @@ extern "C" atc_status atc_csr_free(atc_csr* csr) {
   }
   *csr = atc_csr{};
   return ATC_OK;
-}
+} ATC_CATCH
 
 // A-direction-seri as a library call: orient the simple graph by peel priority and emit
 // the edges sorted by (src, dst) — the byte order of lpBasedGraph.bin (A-direction-seri.cpp:254-273).
 extern "C" atc_status atc_adirection(const int32_t* pairs, uint64_t np, int32_t* oriented_out, uint64_t* n_out,
-                                     int32_t* prio_out, atc_stream st) {
+                                     int32_t* prio_out, atc_stream st) try {
   ATC_CHECK_ARG(n_out != nullptr, "n_out is NULL");
   ATC_CHECK_ARG(np == 0 || (pairs != nullptr && oriented_out != nullptr), "NULL array");
   cudaStream_t s = as_stream(st);
@@ -556,7 +556,7 @@ extern "C" atc_status atc_adirection(const int32_t* pairs, uint64_t np, int32_t*
   ATC_CK(cudaStreamSynchronize(s));
   *n_out = (uint64_t)e.m;
   return ATC_OK;
-}
+} ATC_CATCH
 
 // ---- k-core direction (edge_directing/kcore_direction.cpp:12-146) -------------------
 namespace atc {
@@ -581,7 +581,7 @@ __global__ void kcore_orient_kernel(const int2* p, int64_t ne, const int32_t* co
 }  // namespace atc
 
 extern "C" atc_status atc_kcore_direction(const uint64_t* edges, uint64_t ne, uint64_t* oriented_out,
-                                          int32_t* core_out, uint64_t* n_vertices, atc_stream st) {
+                                          int32_t* core_out, uint64_t* n_vertices, atc_stream st) try {
   ATC_CHECK_ARG(ne == 0 || (edges != nullptr && oriented_out != nullptr), "NULL array");
   cudaStream_t s = as_stream(st);
   keep_pool();
@@ -608,7 +608,7 @@ extern "C" atc_status atc_kcore_direction(const uint64_t* edges, uint64_t ne, ui
   ATC_CK(cudaStreamSynchronize(s));
   if (n_vertices) *n_vertices = (uint64_t)e.n_in;
   return ATC_OK;
-}
+} ATC_CATCH
 
 // ---- approximate parallel A-direction (edge_directing/A-direction-parallel/peel.cu) -----
 namespace atc {
@@ -633,7 +633,7 @@ __global__ void apeel_orient_kernel(const int2* p, int64_t ne, const uint32_t* f
 
 extern "C" atc_status atc_adirection_par(const uint64_t* edges, uint64_t ne, int compat, uint64_t* oriented_out,
                                          uint32_t* flags_out, uint32_t* minor_out, uint64_t* n_vertices,
-                                         int32_t* iterations, atc_stream st) {
+                                         int32_t* iterations, atc_stream st) try {
   ATC_CHECK_ARG(ne == 0 || (edges != nullptr && oriented_out != nullptr), "NULL array");
   cudaStream_t s = as_stream(st);
   keep_pool();
@@ -666,7 +666,7 @@ extern "C" atc_status atc_adirection_par(const uint64_t* edges, uint64_t ne, int
   if (n_vertices) *n_vertices = (uint64_t)e.n_in;
   if (iterations) *iterations = iters;
   return ATC_OK;
-}
+} ATC_CATCH
 
 // ---- binary CSR cache -----------------------------------------------------------------
 // File: "ATCCSR01", then int64 n, m, n_input, wedges, wedges_min, int32 dir, order,
@@ -714,7 +714,7 @@ struct HostMapped {
 };
 }  // namespace atc
 
-extern "C" atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_stream st) {
+extern "C" atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr && path != nullptr, "NULL argument");
   std::vector<int64_t> off(csr->n + 1);
   std::vector<int32_t> cols(csr->m);
@@ -735,7 +735,7 @@ extern "C" atc_status atc_csr_save(const atc_csr* csr, const char* path, atc_str
     return ATC_ERR_INVALID;
   }
   return ATC_OK;
-}
+} ATC_CATCH
 
 static atc_status csr_load_impl(const char* path, bool host_resident, atc_csr* out, cudaStream_t s) {
   ATC_CHECK_ARG(path != nullptr && out != nullptr, "NULL argument");
@@ -838,15 +838,15 @@ static atc_status csr_load_impl(const char* path, bool host_resident, atc_csr* o
   return ATC_OK;
 }
 
-extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st) {
+extern "C" atc_status atc_csr_load(const char* path, atc_csr* out, atc_stream st) try {
   return csr_load_impl(path, false, out, as_stream(st));
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_csr_load_host(const char* path, atc_csr* out, atc_stream st) {
+extern "C" atc_status atc_csr_load_host(const char* path, atc_csr* out, atc_stream st) try {
   return csr_load_impl(path, true, out, as_stream(st));
-}
+} ATC_CATCH
 
-extern "C" atc_status atc_csr_host_resident(atc_csr* csr, atc_stream st) {
+extern "C" atc_status atc_csr_host_resident(atc_csr* csr, atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr, "csr is NULL");
   ATC_CHECK_ARG(csr->priv != nullptr, "csr was not built by atc_pretc or atc_csr_load");
   CsrPriv* pv = static_cast<CsrPriv*>(csr->priv);
@@ -866,4 +866,4 @@ extern "C" atc_status atc_csr_host_resident(atc_csr* csr, atc_stream st) {
   pv->host_cols = hcols.release();
   pv->host_esrc = hesrc.release();
   return ATC_OK;
-}
+} ATC_CATCH

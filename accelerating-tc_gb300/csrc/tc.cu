@@ -725,17 +725,17 @@ static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tun
 }
 
 extern "C" atc_status atc_tc(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint64_t* count,
-                             atc_stats* stats, atc_stream st) {
+                             atc_stats* stats, atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
   ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
   ATC_CHECK_ARG(kernel >= ATC_KERNEL_AUTO && kernel <= ATC_KERNEL_TRICORE, "unknown atc_kernel");
   *count = 0;
   return tc_window(csr, kernel, tuning, 0, csr->m, count, stats, as_stream(st));
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_tc_part(const atc_csr* csr, atc_kernel kernel, const atc_tuning* tuning, uint32_t part,
                                   uint32_t nparts, uint64_t* count, int64_t* edge_range, atc_stats* stats,
-                                  atc_stream st) {
+                                  atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
   ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
   ATC_CHECK_ARG(kernel >= ATC_KERNEL_AUTO && kernel <= ATC_KERNEL_TRICORE, "unknown atc_kernel");
@@ -749,10 +749,10 @@ extern "C" atc_status atc_tc_part(const atc_csr* csr, atc_kernel kernel, const a
     edge_range[1] = b[1];
   }
   return tc_window(csr, kernel, tuning, b[0], b[1], count, stats, s);
-}
+} ATC_CATCH
 
 extern "C" atc_status atc_tc_noalloc(const int64_t* offsets, const int32_t* cols, int64_t n, int64_t m,
-                                     uint64_t* count, atc_stream st) {
+                                     uint64_t* count, atc_stream st) try {
   ATC_CHECK_ARG(count != nullptr, "count is NULL");
   ATC_CHECK_ARG(n >= 0 && m >= 0, "negative size");
   if (n > kNoAllocMaxN || m > kNoAllocMaxM) {
@@ -764,4 +764,4 @@ extern "C" atc_status atc_tc_noalloc(const int64_t* offsets, const int32_t* cols
   if (m == 0 || n == 0) return ATC_OK;
   ATC_CHECK_ARG(offsets != nullptr && cols != nullptr, "NULL CSR array");
   return tc_noalloc_impl(offsets, cols, n, m, count, as_stream(st));
-}
+} ATC_CATCH
