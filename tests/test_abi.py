@@ -197,3 +197,35 @@ def test_struct_layouts_and_enums_match_the_header(tmp_path):
         assert got[(cname, "sizeof")] == C.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_error_text_is_per_thread():
+    # two threads fail different argument checks at the same time; each reads its own message
+    import threading
+    lib = atc.lib()
+    cnt = C.c_uint64()
+    barrier = threading.Barrier(2)
+    seen = {}
+
+    def fail_kcl():
+        barrier.wait()
+        for _ in range(200):
+            assert lib.atc_kcl(None, 4, C.byref(cnt), None, None) == atc.Status.ERR_INVALID
+            seen.setdefault("kcl", set()).add(lib.atc_last_error())
+
+    def fail_relabel():
+        pairs = np.array([[0, 1]], dtype=np.int32)
+        lookup = np.zeros(2, dtype=np.int32)
+        barrier.wait()
+        for _ in range(200):
+            assert lib.atc_relabel(pairs.ctypes.data, 1, 9, lookup.ctypes.data, None, None, None) == \
+                atc.Status.ERR_INVALID
+            seen.setdefault("relabel", set()).add(lib.atc_last_error())
+
+    ts = [threading.Thread(target=fail_kcl), threading.Thread(target=fail_relabel)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert len(seen["kcl"]) == 1 and len(seen["relabel"]) == 1
+    assert seen["kcl"] != seen["relabel"]
