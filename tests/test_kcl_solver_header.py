@@ -15,10 +15,12 @@ from conftest import ROOT, write_gr
 
 PROGRAM = r"""
 #include <cstdio>
+#include <cstdlib>
 #include <iostream>
 #include "atc_kcl_solver.hpp"
 
 int main(int argc, char** argv) {
+  if (argc < 3) return 2;
   typedef unsigned long long AccType;  // as in the reference's kcl_gpu.cpp
   AccType total = 7;
   try {
@@ -42,7 +44,8 @@ def _build(tmp_path):
     src.write_text(PROGRAM)
     libdir = os.path.dirname(atc.LIB_PATH)
     exe = tmp_path / "kcl_prog"
-    r = subprocess.run([cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe),
                         "-L", libdir, "-latc", "-Wl,-rpath," + libdir], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe
