@@ -80,7 +80,8 @@ class Tuning(C.Structure):
         ("bisson_block_chunk", C.c_int32),
         ("bisson_slots", C.c_int32),
         ("group_by_source", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("kcl_dense", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -113,6 +114,14 @@ class StatsStruct(C.Structure):
     ]
 
 
+class PhaseTimeStruct(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 40),
+        ("depth", C.c_int32),
+        ("ms", C.c_float),
+    ]
+
+
 @dataclass
 class Stats:
     kernel_ms: float
@@ -133,6 +142,9 @@ _SIGS = {
     "atc_status_string": (C.c_char_p, [C.c_int]),
     "atc_last_error": (C.c_char_p, []),
     "atc_init": (C.c_int, [C.c_int]),
+    "atc_set_alloc_budget": (C.c_int, [C.c_int64]),
+    "atc_phase_timing": (C.c_int, [C.c_int32]),
+    "atc_phase_times": (C.c_int, [C.POINTER(PhaseTimeStruct), C.c_int32, C.POINTER(C.c_int32)]),
     "atc_gen_rmat_host": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, C.c_int]),
     "atc_gen_rmat_device": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P]),
     "atc_gen_rgg_host": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, _P, C.c_uint64, C.POINTER(C.c_uint64), C.c_int]),
@@ -160,6 +172,8 @@ _SIGS = {
                                C.POINTER(C.c_int64), C.POINTER(StatsStruct), _P]),
     "atc_tc_part": (C.c_int, [C.POINTER(CSRStruct), C.c_int, C.POINTER(Tuning), C.c_uint32, C.c_uint32,
                               C.POINTER(C.c_uint64), C.POINTER(C.c_int64), C.POINTER(StatsStruct), _P]),
+    "atc_kcl_part_tuned": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(Tuning), C.c_uint32, C.c_uint32,
+                                     C.POINTER(C.c_uint64), C.POINTER(C.c_int64), C.POINTER(StatsStruct), _P]),
     "atc_kcl": (C.c_int, [C.POINTER(CSRStruct), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(StatsStruct), _P]),
     "atc_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "atc_batch_reserve": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _P]),
@@ -222,7 +236,27 @@ def version():
 
 
 def init(device=0):
+    """Initialises `device` and makes it current (-1: the current device, left as it is)."""
     _check(lib().atc_init(device))
+
+
+def set_alloc_budget(nbytes):
+    """Caps the library's device allocations at `nbytes` in total from now on (None or a
+    negative value: no cap).  An allocation beyond the cap fails with ERR_OOM."""
+    _check(lib().atc_set_alloc_budget(-1 if nbytes is None else int(nbytes)))
+
+
+def phase_timing(enable=True):
+    """Starts (or stops) recording the library's named phases on this thread."""
+    _check(lib().atc_phase_timing(1 if enable else 0))
+
+
+def phase_times(cap=256):
+    """[(name, depth, ms)] of the phases recorded since the last read (cleared by the read)."""
+    buf = (PhaseTimeStruct * cap)()
+    n = C.c_int32(0)
+    _check(lib().atc_phase_times(buf, cap, C.byref(n)))
+    return [(buf[i].name.decode(), buf[i].depth, buf[i].ms) for i in range(min(n.value, cap))]
 
 
 GRAPH500 = (570000, 190000, 190000)
@@ -395,12 +429,17 @@ def tc_part(csr: CSR, part, nparts, kernel=Kernel.AUTO, tuning=None, stream=None
     return cnt.value, (rng[0], rng[1]), _stats(st)
 
 
-def kcl_part(csr: CSR, k, part, nparts, stream=None):
-    """atc_kcl_part: (k-cliques of part `part` of `nparts` edge ranges, (first, last) edge, stats)."""
+def kcl_part(csr: CSR, k, part, nparts, dense=True, stream=None):
+    """atc_kcl_part: (k-cliques of part `part` of `nparts` edge ranges, (first, last) edge, stats).
+    dense=False puts every edge on the warp search (atc_kcl_part_tuned, kcl_dense = -1)."""
     cnt = C.c_uint64(0)
     rng = (C.c_int64 * 2)()
     st = StatsStruct()
-    _check(lib().atc_kcl_part(C.byref(csr.struct), k, part, nparts, C.byref(cnt), rng, C.byref(st), stream))
+    if dense:
+        _check(lib().atc_kcl_part(C.byref(csr.struct), k, part, nparts, C.byref(cnt), rng, C.byref(st), stream))
+    else:
+        _check(lib().atc_kcl_part_tuned(C.byref(csr.struct), k, _tuning({"kcl_dense": -1}), part, nparts,
+                                        C.byref(cnt), rng, C.byref(st), stream))
     return cnt.value, (rng[0], rng[1]), _stats(st)
 
 

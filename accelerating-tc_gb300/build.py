@@ -119,10 +119,11 @@ def build_cli(force=False):
 
 
 def build_oracle():
+    """The oracle library, and the reference's CPU programs where the reference tree
+    exists (oracle/Makefile's REF, or ATC_REFERENCE_TREE when set)."""
     _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"])
-    ref = os.environ.get("ATC_REFERENCE_TREE", "/root/reference")
-    if os.path.isdir(ref):
-        _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + ref])
+    ref = os.environ.get("ATC_REFERENCE_TREE")
+    _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref-if-present"] + (["REF=" + ref] if ref else []))
 
 
 def build_all(force=False):

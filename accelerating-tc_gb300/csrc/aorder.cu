@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <optional>
 #include <thread>
 #include <vector>
 
@@ -377,6 +378,8 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
   }
   DevBuf<int32_t> deg, rt;
   DevBuf<int> mx;
+  std::optional<Phase> ph;
+  ph.emplace("aorder.device", s);
   ATC_TRY(rt.alloc(n_v, s));
   ATC_TRY(mx.alloc(1, s));
   ATC_CK(cudaMemsetAsync(rt.p, 0, sizeof(int32_t) * n_v, s));
@@ -438,6 +441,8 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
   ATC_TRY(sort_keys_u64(a, b, n_v, 0, B + rb, s));
 
   std::vector<uint32_t> log, rank;
+  ph.reset();
+  ph.emplace(overlap ? "aorder.heap||peel" : "aorder.heap", s);
   if (overlap) {
     bool heap_ok = true;
     std::thread heap([&] {
@@ -457,6 +462,8 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
   } else {
     bucket_heap(hist, maxrt, S, mdp, log, rank);
   }
+  ph.reset();
+  ph.emplace("aorder.scatter", s);
   const int64_t total = nb * kBucket;
   DevBuf<uint32_t> dlog, drank;
   DevBuf<int32_t> dpos;

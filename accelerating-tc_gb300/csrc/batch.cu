@@ -76,6 +76,12 @@ void free_pipeline(atc_batch* b) {
 
 template <class T>
 atc_status dev_alloc(T** p, size_t count) {
+  if (!alloc_budget_take(sizeof(T) * (count ? count : 1))) {
+    *p = nullptr;
+    set_error("device allocation of %zu bytes for the batch refused: the allocation budget (atc_set_alloc_budget) "
+              "is spent", sizeof(T) * count);
+    return ATC_ERR_OOM;
+  }
   cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
   if (e != cudaSuccess) {
     *p = nullptr;
@@ -299,6 +305,7 @@ extern "C" atc_status atc_batch_run(atc_batch* b, const atc_tuning* t, uint64_t*
   }
   atc::ItemShape sh = atc::shape_from(t, b->shape);
   float ms = 0;
+  atc::Phase ph("batch", as_stream(st));
   ATC_TRY(atc::run_once(b, sh, counts, &ms, as_stream(st)));
   if (stats) {
     memset(stats, 0, sizeof(*stats));

@@ -28,8 +28,8 @@ void set_error(const char* fmt, ...);
   } while (0)
 
 // Closes a function-try-block around an entry point's body: a host allocation that fails
-// (std::bad_alloc) or any other C++ exception becomes a status, never an exception
-// crossing the C ABI.
+// (std::bad_alloc), any other C++ exception, and any exception of a type outside the
+// std::exception hierarchy become a status, never an exception crossing the C ABI.
 #define ATC_CATCH                                                       \
   catch (const std::bad_alloc&) {                                       \
     ::atc::set_error("out of host memory");                             \
@@ -37,6 +37,10 @@ void set_error(const char* fmt, ...);
   }                                                                     \
   catch (const std::exception& ex_) {                                   \
     ::atc::set_error("%s", ex_.what());                                 \
+    return ATC_ERR_INVALID;                                             \
+  }                                                                     \
+  catch (...) {                                                         \
+    ::atc::set_error("unknown C++ exception");                          \
     return ATC_ERR_INVALID;                                             \
   }
 
@@ -59,6 +63,27 @@ inline cudaStream_t as_stream(atc_stream s) { return reinterpret_cast<cudaStream
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Device allocation budget (atc_set_alloc_budget): takes `bytes` from the budget and
+// returns true, or returns false (and takes nothing) when the budget would go below zero.
+// Unlimited unless a budget was set.
+bool alloc_budget_take(size_t bytes);
+
+// A named phase of a call: an NVTX range (visible to Nsight tools and ncu's NVTX filters)
+// and, when phase timing is on for the calling thread (atc_phase_timing), a pair of CUDA
+// events on the phase's stream, read back by atc_phase_times.  Phases nest; a phase is
+// recorded with its nesting depth.
+class Phase {
+ public:
+  Phase(const char* name, cudaStream_t s);
+  ~Phase();
+  Phase(const Phase&) = delete;
+  Phase& operator=(const Phase&) = delete;
+
+ private:
+  int slot_ = -1;
+  cudaStream_t s_ = nullptr;
+};
+
 // Stream-ordered device buffer: allocated with cudaMallocAsync on the call's stream
 // and released on the same stream when it goes out of scope.
 template <class T>
@@ -80,6 +105,12 @@ struct DevBuf {
     s = stream;
     n = count;
     if (count == 0) return ATC_OK;
+    if (!alloc_budget_take(sizeof(T) * count)) {
+      n = 0;
+      set_error("device allocation of %zu bytes refused: the allocation budget (atc_set_alloc_budget) is spent",
+                sizeof(T) * count);
+      return ATC_ERR_OOM;
+    }
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * count, stream);
     if (e != cudaSuccess) {
       p = nullptr;

@@ -407,7 +407,7 @@ using namespace atc;
 
 // k-cliques whose first two vertices (in orientation order) form an edge of [e0, e1).
 static atc_status kcl_window(const atc_csr* csr, uint32_t k, int64_t e0, int64_t e1, uint64_t* count, atc_stats* stats,
-                             cudaStream_t s) {
+                             cudaStream_t s, bool allow_dense = true) {
   *count = 0;
   unsigned long long h[2] = {0, 0};
   EventTimer tm;
@@ -428,7 +428,7 @@ static atc_status kcl_window(const atc_csr* csr, uint32_t k, int64_t e0, int64_t
     // edges with mid-sized C0 go to the dense kernel from k = 5 on (at k = 4 the count is
     // one intersection per member of C0, which the warp path does as fast: R-MAT scale 20
     // took 562 ms dense, 422 ms without)
-    const bool use_dense = k >= 5 && cap > kMaskMax;
+    const bool use_dense = allow_dense && k >= 5 && cap > kMaskMax;
     DevBuf<unsigned long long> dense;
     if (use_dense) ATC_TRY(dense.alloc((size_t)csr->m + 2, s));
     tm.start(s);
@@ -473,11 +473,18 @@ extern "C" atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, a
   ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
   ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
   ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
+  Phase ph("kcl", as_stream(st));
   return kcl_window(csr, k, 0, csr->m, count, stats, as_stream(st));
 } ATC_CATCH
 
 extern "C" atc_status atc_kcl_part(const atc_csr* csr, uint32_t k, uint32_t part, uint32_t nparts, uint64_t* count,
                                    int64_t* edge_range, atc_stats* stats, atc_stream st) try {
+  return atc_kcl_part_tuned(csr, k, nullptr, part, nparts, count, edge_range, stats, st);
+} ATC_CATCH
+
+extern "C" atc_status atc_kcl_part_tuned(const atc_csr* csr, uint32_t k, const atc_tuning* tuning, uint32_t part,
+                                         uint32_t nparts, uint64_t* count, int64_t* edge_range, atc_stats* stats,
+                                         atc_stream st) try {
   ATC_CHECK_ARG(csr != nullptr && count != nullptr, "NULL argument");
   ATC_CHECK_ARG(k >= 3 && k <= (uint32_t)kMaxK, "k must be in [3, 16]");
   ATC_CHECK_ARG(csr->priv != nullptr || csr->m == 0, "csr was not built by atc_pretc");
@@ -490,5 +497,7 @@ extern "C" atc_status atc_kcl_part(const atc_csr* csr, uint32_t k, uint32_t part
     edge_range[0] = b[0];
     edge_range[1] = b[1];
   }
-  return kcl_window(csr, k, b[0], b[1], count, stats, s);
+  ATC_CHECK_ARG(!tuning || tuning->kcl_dense == 0 || tuning->kcl_dense == -1, "kcl_dense must be 0 or -1");
+  Phase ph("kcl", s);
+  return kcl_window(csr, k, b[0], b[1], count, stats, s, !(tuning && tuning->kcl_dense == -1));
 } ATC_CATCH

@@ -91,6 +91,7 @@ __global__ void peel_wave_kernel(const int32_t* frontier, int nf, const int64_t*
 }  // namespace
 
 atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* prio, int* waves_out, cudaStream_t s) {
+  Phase ph("peel", s);
   int64_t n = e.n_in, m = e.m;
   *waves_out = 0;
   if (n == 0) return ATC_OK;

@@ -313,14 +313,20 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
   SimpleEdges e;
+  std::optional<Phase> ph;
+  ph.emplace("pretc.dedup", s);
   ATC_TRY(build_simple_edges(pairs, np, &e, s));
+  ph.reset();
   int64_t n_in = e.n_in;
   DevBuf<int32_t> deg, prio, perm, cmap;
   DevBuf<uint32_t> minor;
   bool peeled = false;  // A-direction priorities computed already
+  ph.emplace("pretc.degrees", s);
   ATC_TRY(deg.alloc(n_in, s));
   ATC_TRY(simple_degrees(e, deg.p, s));
+  ph.reset();
   if (order != ATC_ORDER_NONE) {
+    ph.emplace(order == ATC_ORDER_AORDER && dir == ATC_DIR_ADIRECTION ? "pretc.order+peel" : "pretc.order", s);
     // The relabelling programs see the simple graph with each edge once, as when they
     // read the output of A-direction-seri; their id range ends at the largest id that
     // has an edge.
@@ -362,7 +368,9 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
       ATC_TRY(relabel_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v,
                              order == ATC_ORDER_DEGREE_DESC ? ATC_RELABEL_DEGREE_DESC : ATC_RELABEL_AORDER_V2, perm.p,
                              nullptr, s));
+    ph.reset();
   }
+  ph.emplace("pretc.direction", s);
   if (dir == ATC_DIR_ADIRECTION && !peeled) {
     ATC_TRY(prio.alloc(n_in, s));
     int waves = 0;
@@ -375,8 +383,10 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
     ATC_TRY(minor.alloc(n_in, s));
     ATC_TRY(approx_peel(e, deg.p, reinterpret_cast<uint32_t*>(prio.p), minor.p, nullptr, s));
   }
+  ph.reset();
   int64_t n = n_in;
   if (prune) {
+    ph.emplace("pretc.prune", s);
     DevBuf<int32_t> keep;
     DevBuf<int64_t> pre;
     ATC_TRY(keep.alloc(n_in + 1, s));
@@ -392,7 +402,9 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
     ATC_CK(cudaMemcpyAsync(&kept, pre.p + n_in, sizeof(kept), cudaMemcpyDeviceToHost, s));
     ATC_CK(cudaStreamSynchronize(s));
     n = kept;
+    ph.reset();
   }
+  ph.emplace("pretc.orient+sort", s);
   int bout = id_bits(n);
   DevBuf<uint64_t> k1, k2;
   DevBuf<unsigned long long> dropped;
@@ -411,6 +423,8 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
   ATC_CK(cudaMemcpyAsync(&hdrop, dropped.p, sizeof(hdrop), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   int64_t m = e.m - (int64_t)hdrop;
+  ph.reset();
+  ph.emplace("pretc.csr", s);
 
   // Own buffers of the CSR.  cols gets 16 ints of padding so that 16-byte-rounded bulk
   // copies of any list stay inside the allocation.
@@ -444,6 +458,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
     std::copy(id.begin(), id.end(), perm_out);
   }
   ATC_CK(cudaStreamSynchronize(s));
+  ph.reset();
 
   CsrPriv* pv = new CsrPriv();
   pv->esrc = esrc.detach();
@@ -471,6 +486,7 @@ using namespace atc;
 extern "C" atc_status atc_pretc_device(const int32_t* pairs_dev, uint64_t np, atc_dir dir, atc_order order,
                                        const atc_tuning* t, atc_csr* out, int32_t* perm_out, atc_stream s) try {
   ATC_CHECK_ARG(np == 0 || pairs_dev != nullptr, "pairs_dev is NULL");
+  Phase ph("pretc", as_stream(s));
   return pretc_impl(reinterpret_cast<const int2*>(pairs_dev), np, dir, order, t, out, perm_out, as_stream(s));
 } ATC_CATCH
 
@@ -479,9 +495,13 @@ extern "C" atc_status atc_pretc(const int32_t* pairs, uint64_t np, atc_dir dir, 
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
   cudaStream_t st = as_stream(s);
   keep_pool();
+  Phase ph("pretc", st);
   DevBuf<int2> d;
-  ATC_TRY(d.alloc(np, st));
-  if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
+  {
+    Phase ph_copy("pretc.h2d", st);
+    ATC_TRY(d.alloc(np, st));
+    if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
+  }
   return pretc_impl(d.p, np, dir, order, t, out, perm_out, st);
 } ATC_CATCH
 

@@ -257,6 +257,7 @@ __global__ void fox_deal_kernel(const uint64_t* keys, const int64_t* list, int64
 // ---- family drivers ----------------------------------------------------------------
 static atc_status run_tricore(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                               int* launches) {
+  Phase ph("tc.count", s);
   int grid = t && t->tricore_blocks > 0 ? t->tricore_blocks
                                         : sm_count() * blocks_per_sm((const void*)tricore_kernel, kTriWarps * 32, 0);
   tricore_kernel<<<grid, kTriWarps * 32, 0, s>>>(g, ctr);
@@ -269,6 +270,8 @@ static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long l
                           int* launches) {
   DevBuf<int> mx;
   DevBuf<unsigned long long> hist, cursor;
+  std::optional<Phase> ph;
+  ph.emplace("tc.bins", s);
   ATC_TRY(mx.alloc(1, s));
   ATC_TRY(hist.alloc(6, s));
   ATC_TRY(cursor.alloc(6, s));
@@ -328,6 +331,8 @@ static atc_status run_fox(const CsrView& g, const atc_tuning* t, unsigned long l
     }
     L = list2.p;
   }
+  ph.reset();
+  ph.emplace("tc.count", s);
   int sms = sm_count();
   for (int b = 0; b < 6; ++b) {
     int64_t nb = (int64_t)h[b];
@@ -421,6 +426,8 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
   // the sorted copy only for N+(u) of at most 8 (every N+(v) is searched in it; the hash
   // takes one probe): 4 % faster than 32 at R-MAT scale 24
   if (!t || t->bisson_cutover <= 0) sh.cutover = 8;
+  std::optional<Phase> ph;
+  ph.emplace("tc.items", s);
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
   ATC_TRY(counters.alloc(8, s));
   ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
@@ -435,6 +442,8 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   *launches += 1;
+  ph.reset();
+  ph.emplace("tc.count", s);
   return launch_slots(slots, g, g.cols, witems.p, bitems.p, hc, counters.p, ctr, s, launches);
 }
 
@@ -443,6 +452,8 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   ItemShape sh;
   int slots;
   ATC_TRY(item_shape(t, &sh, &slots));
+  std::optional<Phase> ph;
+  ph.emplace("tc.group", s);
   DevBuf<int32_t> cnt, cur, plist;
   DevBuf<int64_t> gstart;
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
@@ -474,19 +485,23 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   *launches += 4;
+  ph.reset();
+  ph.emplace("tc.count", s);
   return launch_slots(slots, g, plist.p, witems.p, bitems.p, hc, counters.p, ctr, s, launches);
 }
 
 // ---- counting without device allocation ------------------------------------------
-// Some callers cannot call cudaMalloc: code recording into a CUDA graph whose capture
-// mode forbids allocation, hosts whose device memory is owned by another allocator or
-// runtime, or real-time loops that must not block in the driver.  atc_tc_noalloc runs
-// the Bisson-style count above with every scratch buffer (edge sources, group counts,
-// grouped partner list, work items, counters) carved out of one file-scope device array
-// of kNoAllocBytes, fixed in size, which every GPU that loads this library keeps until
-// the process exits.  Graphs above kNoAllocMaxN vertices or kNoAllocMaxM edges are
-// refused.  All calls share the one array: calls that overlap on the GPU (concurrent
-// streams or host threads on one device) race and must be serialised by the caller.
+// Some callers cannot call cudaMalloc: a host whose device memory is all owned by
+// another allocator or runtime (a framework's caching pool, a memory manager that
+// reserves the device up front), or a real-time loop that must not block in the
+// driver's allocator.  atc_tc_noalloc runs the Bisson-style count above with every
+// scratch buffer (edge sources, group counts, grouped partner list, work items,
+// counters) carved out of one file-scope device array of kNoAllocBytes, fixed in size,
+// which every GPU that loads this library keeps until the process exits.  Graphs above
+// kNoAllocMaxN vertices or kNoAllocMaxM edges are refused.  The call synchronises its
+// stream: it reads the CSR check, the item counts and the count back to the host.  All
+// calls share the one array: calls that overlap on the GPU (concurrent streams or host
+// threads on one device) race and must be serialised by the caller.
 constexpr int64_t kNoAllocMaxN = 1 << 17;  // 131072 vertices
 constexpr int64_t kNoAllocMaxM = 1 << 20;  // 1048576 oriented edges
 constexpr int64_t kNoAllocItems = kNoAllocMaxN + kNoAllocMaxM / kWarpChunk + 1;
@@ -507,7 +522,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 
-// Device address of g_noalloc_scratch for each device, looked up once per device.
+// Device address of g_noalloc_scratch for each device, looked up once per device (with
+// that device current) and kept for the life of the process.  cudaDeviceReset destroys
+// the context that holds the array, so after a reset of a device this entry point must
+// not be called on it again in the same process.
 atc_status noalloc_scratch(unsigned char** out) {
   static std::mutex mu;
   static unsigned char* addr[64] = {};
@@ -621,26 +639,8 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
   int hc[4];
   ATC_CK(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
-  if (hc[1]) {
-    uint32_t words = 64;
-    while (words < 4u * (uint32_t)hc[3]) words <<= 1;
-    if (words > (uint32_t)kTabWords) words = kTabWords;
-    size_t smem = sizeof(int32_t) * words;
-    ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<FullItems, kDefaultSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-    int bps = blocks_per_sm((const void*)bisson_block_kernel<FullItems, kDefaultSlots>, kBgWarps * 32, smem);
-    int grid = std::min(hc[1], sm_count() * bps);
-    bisson_block_kernel<FullItems, kDefaultSlots><<<grid, kBgWarps * 32, smem, s>>>(g, plist, FullItems{bitems}, hc[1], nullptr, counters + 5, words,
-                                                          GraphTags{nullptr, 0, nullptr}, total_ctr);
-    ATC_CK(cudaGetLastError());
-  }
-  if (hc[0]) {
-    int bps = blocks_per_sm((const void*)bisson_warp_kernel<FullItems, kDefaultSlots>, kBgWarps * 32, 0);
-    int grid = (int)std::min<int64_t>((hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
-    bisson_warp_kernel<FullItems, kDefaultSlots><<<grid, kBgWarps * 32, 0, s>>>(g, plist, FullItems{witems}, hc[0], nullptr, counters + 4,
-                                                      GraphTags{nullptr, 0, nullptr}, total_ctr);
-    ATC_CK(cudaGetLastError());
-  }
+  int launches = 0;
+  ATC_TRY(launch_bisson<kDefaultSlots>(g, plist, witems, bitems, hc, counters, total_ctr, s, &launches));
   unsigned long long h = 0;
   ATC_CK(cudaMemcpyAsync(&h, total_ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
@@ -697,6 +697,7 @@ static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tun
     g.e0 = e0;
     g.e1 = e1;
     unsigned long long* ctr = pv->counter;
+    Phase ph("tc", s);
     tm.start(s);
     ATC_CK(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s));
     switch (kernel) {
@@ -707,7 +708,10 @@ static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tun
     }
     tm.stop(s);
     unsigned long long h = 0;
-    ATC_CK(cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    {
+      Phase ph_rb("tc.readback", s);
+      ATC_CK(cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s));
+    }
     ATC_CK(cudaStreamSynchronize(s));
     *count = h;
   }

@@ -121,7 +121,10 @@ typedef struct atc_tuning {
   int32_t group_by_source;   /* batches: 1 = every edge at its source, the items index the
                                 CSR rows (Hu-style wedge tests, no grouping passes); 0 = at
                                 the endpoint with the longer list (Bisson-style) */
-  int32_t reserved[4];
+  int32_t kcl_dense;         /* k-cliques (atc_kcl_part_tuned): 0 = candidate sets of 65..1024
+                                members on the dense kernel from k = 5 on; -1 = every edge on
+                                the warp search */
+  int32_t reserved[3];
 } atc_tuning;
 
 /* Oriented CSR on the device (the reference's edgeOffset/edgeRow/adjLength globals,
@@ -156,7 +159,26 @@ const char* atc_version(void);
 const char* atc_status_string(atc_status s);
 /* Text of the last error on the calling thread (CUDA message or argument check). */
 const char* atc_last_error(void);
-/* Makes `device` current on the calling thread and initialises its context. */
+/* Device allocation budget, for capacity tests and memory-capped hosts: after
+   atc_set_alloc_budget(b) with b >= 0, the library's stream-ordered device allocations take
+   their size from a budget of b bytes (never returned), and an allocation that the budget
+   cannot cover fails with ATC_ERR_OOM before any device call.  b < 0 removes the budget
+   (the default).  No counterpart in the reference, which aborts on a failed cudaMalloc. */
+atc_status atc_set_alloc_budget(int64_t bytes);
+/* Phase timing, for profiling: with atc_phase_timing(1) the library records its named phases
+   (preTC stages, counting passes) on the calling thread as CUDA events on each call's
+   stream; atc_phase_times copies up to `cap` recorded phases, in the order they began, sets
+   *n to the number recorded, waits for their end events, and clears the record.
+   atc_phase_timing(0) stops recording.  Every phase is also an NVTX range. */
+typedef struct atc_phase_time {
+  char name[40];
+  int32_t depth; /* nesting depth: 0 = a phase of its own, 1 = inside a depth-0 phase, ... */
+  float ms;      /* device time between the phase's start and end events */
+} atc_phase_time;
+atc_status atc_phase_timing(int32_t enable);
+atc_status atc_phase_times(atc_phase_time* out, int32_t cap, int32_t* n);
+/* Makes `device` current on the calling thread and initialises its context.  device = -1
+   initialises the calling thread's current device and leaves the current device as it is. */
 atc_status atc_init(int device);
 
 /* ---- synthetic inputs (deterministic, integer-only; no GPU needed for _host) --- */
@@ -289,17 +311,24 @@ atc_status atc_tc_part(const atc_csr* csr, atc_kernel kernel, const atc_tuning* 
                        uint32_t nparts, uint64_t* count, int64_t* edge_range, atc_stats* stats, atc_stream s);
 /* Triangle count of an oriented CSR given as plain device arrays, computed without
    allocating any device memory.  No counterpart in the reference: it is for callers
-   that cannot call cudaMalloc (capture of a CUDA graph in a mode that forbids
-   allocation, device memory owned by another allocator, real-time loops).  Runs the
-   ATC_KERNEL_BISSON count with all scratch in one fixed device array of the library
-   (about 17 MiB, held by every device that loads the library until exit).  Limits:
-   n <= 131072 vertices and m <= 1048576 edges, else ATC_ERR_INVALID; offsets (n+1,
-   int64) and cols (m) must form a CSR whose rows are strictly increasing ids in
-   [0, n) (checked on the device first; ATC_ERR_INVALID otherwise).  The first call on
-   a device looks up the array's device address, so make it before any stream capture.
-   All calls share the array: calls that overlap on the GPU race. */
+   that cannot call cudaMalloc, such as a host whose device memory is all owned by
+   another allocator or runtime, or a real-time loop that must not block in the
+   driver's allocator.  Runs the ATC_KERNEL_BISSON count with all scratch in one fixed
+   device array of the library (about 17 MiB, held by every device that loads the
+   library until exit).  Limits: n <= 131072 vertices and m <= 1048576 edges, else
+   ATC_ERR_INVALID; offsets (n+1, int64) and cols (m) must form a CSR whose rows are
+   strictly increasing ids in [0, n) (checked on the device first; ATC_ERR_INVALID
+   otherwise).  The call synchronises `s` (it reads results back to the host).  The
+   first call on a device looks up the array's device address, so make it before any
+   stream capture; after cudaDeviceReset of a device, do not call it on that device
+   again in the same process.  All calls share the array: calls that overlap on the
+   GPU race. */
 atc_status atc_tc_noalloc(const int64_t* offsets_dev, const int32_t* cols_dev, int64_t n, int64_t m,
                           uint64_t* count, atc_stream s);
+/* atc_kcl_part with tuning (nullable; tuning->kcl_dense selects the kernels). */
+atc_status atc_kcl_part_tuned(const atc_csr* csr, uint32_t k, const atc_tuning* tuning, uint32_t part,
+                              uint32_t nparts, uint64_t* count, int64_t* edge_range, atc_stats* stats,
+                              atc_stream s);
 /* k-clique count (k >= 3) of the oriented CSR, exact in uint64.  Replaces
    kcl_gpu_solver(std::string, unsigned k, AccType& total, size_t) (k-clique/kcl.h:6-7). */
 atc_status atc_kcl(const atc_csr* csr, uint32_t k, uint64_t* count, atc_stats* stats, atc_stream s);

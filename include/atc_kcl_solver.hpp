@@ -9,7 +9,8 @@
    reference adds each chunk's count to `total`.  N_CHUNK, the reference's split of the
    embedding list into chunks, is accepted and has no effect: no level of the search is
    materialised here.  The graph is oriented by A-direction on the device; the count does not
-   depend on the orientation.
+   depend on the orientation.  The count runs on the calling thread's current CUDA device, which
+   the call does not change (the reference solver never selects a device either).
 
    Errors: the reference aborts the process from inside the solver (CUDA_SAFE_CALL).  Here the
    solver throws std::runtime_error carrying libatc's message, and `total` is left unchanged. */
@@ -42,7 +43,7 @@ inline void kcl_gpu_solver(std::string filename, unsigned k, AccType& total, siz
   std::vector<int32_t> pairs(2 * (size_t)np);
   s = atc_read_edges(filename.c_str(), pairs.data(), np, &np);
   if (s != ATC_OK) atc_compat::kcl_fail(s, "reading the graph");
-  s = atc_init(0);
+  s = atc_init(-1);  // the caller's current device, as the reference solver uses it
   if (s != ATC_OK) atc_compat::kcl_fail(s, "device");
   atc_csr csr;
   s = atc_pretc(pairs.data(), np, ATC_DIR_ADIRECTION, ATC_ORDER_NONE, nullptr, &csr, nullptr, nullptr);

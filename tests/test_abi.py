@@ -170,7 +170,8 @@ def test_struct_layouts_and_enums_match_the_header(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    mirrors = {"atc_tuning": atc.Tuning, "atc_csr": atc.CSRStruct, "atc_stats": atc.StatsStruct}
+    mirrors = {"atc_tuning": atc.Tuning, "atc_csr": atc.CSRStruct, "atc_stats": atc.StatsStruct,
+               "atc_phase_time": atc.PhaseTimeStruct}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "atc.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
@@ -230,3 +231,42 @@ def test_error_text_is_per_thread():
         t.join()
     assert len(seen["kcl"]) == 1 and len(seen["relabel"]) == 1
     assert seen["kcl"] != seen["relabel"]
+
+
+def test_alloc_budget_refuses_device_allocations_before_any_device_call():
+    # a spent budget turns the first device allocation of a call into ATC_ERR_OOM; the call
+    # returns before it touches the device, so this runs without a GPU
+    pairs = np.array([[0, 1], [1, 2], [2, 0]], dtype=np.int32)
+    csr = atc.CSRStruct()
+    lib = atc.lib()
+    try:
+        atc.set_alloc_budget(0)
+        rc = lib.atc_pretc(pairs.ctypes.data, 3, int(atc.Dir.DEGREE), 0, None, C.byref(csr), None, None)
+        assert rc == atc.Status.ERR_OOM
+        assert b"allocation budget" in lib.atc_last_error()
+        with pytest.raises(atc.ATCError) as ei:
+            atc.pretc(pairs, atc.Dir.DEGREE)
+        assert ei.value.status == atc.Status.ERR_OOM
+        b = C.c_void_p()
+        assert lib.atc_batch_create(C.byref(b)) == 0
+        try:
+            assert lib.atc_batch_reserve(b, 1 << 20, 1 << 22, None) == atc.Status.ERR_OOM
+            assert b"allocation budget" in lib.atc_last_error()
+        finally:
+            lib.atc_batch_destroy(b)
+    finally:
+        atc.set_alloc_budget(None)
+
+
+def test_phase_timing_without_gpu():
+    # recording on, nothing recorded by calls that fail their argument checks, then off
+    atc.phase_timing(True)
+    try:
+        cnt = C.c_uint64()
+        assert atc.lib().atc_kcl(None, 4, C.byref(cnt), None, None) == atc.Status.ERR_INVALID
+        assert atc.phase_times() == []
+    finally:
+        atc.phase_timing(False)
+    n = C.c_int32(5)
+    assert atc.lib().atc_phase_times(None, 0, C.byref(n)) == 0 and n.value == 0
+    assert atc.lib().atc_phase_times(None, 0, None) == atc.Status.ERR_INVALID

@@ -1,12 +1,13 @@
 """atc_tc_noalloc: the triangle count for callers that cannot allocate device memory.
 
-Such callers (a CUDA graph being captured in a mode that forbids allocation, a host whose
-device memory belongs to another allocator, a real-time loop) hand the library their own
-device CSR arrays.  The entry point runs the Bisson-style count with all of its scratch
-in one fixed array inside the library.  Here it must return exactly the count of the
-allocating entry point, atc_tc, for the same CSR, on two calls in a row (the second call
-finds the first call's leftovers in the shared array), and refuse graphs above its limits
-and malformed CSRs.  This file runs last so that a failure here cannot stop other tests.
+Such callers (a host whose device memory belongs to another allocator or runtime, a
+real-time loop that must not block in the allocator) hand the library their own device
+CSR arrays.  The entry point runs the Bisson-style count with all of its scratch in one
+fixed array inside the library.  Here it must return exactly the count of the allocating
+entry point, atc_tc, for the same CSR, and the oracle's count of the same graph, on two
+calls in a row (the second call finds the first call's leftovers in the shared array),
+and refuse graphs above its limits and malformed CSRs.  This file runs last so that a
+failure here cannot stop other tests.
 """
 import ctypes as C
 
@@ -14,6 +15,7 @@ import numpy as np
 import pytest
 
 import atc
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +36,7 @@ def test_noalloc_matches_allocating_entry_point(scale, seed, d):
     g = atc.rmat_graph(scale, 16, seed)
     csr = atc.pretc(g, d)
     want, _ = atc.tc(csr, atc.Kernel.BISSON)
+    assert want == oracle.tc_count(g)
     assert _noalloc(csr) == want
     assert _noalloc(csr) == want  # second call reuses the shared scratch
 
