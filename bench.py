@@ -71,6 +71,10 @@ def parse():
                     help="batched path picks each graph's orientation (degree or A-direction) by its work estimate")
     ap.add_argument("--kcl-graphs", default="rgg:20:4-7,rmat:20:4-6,rmat:14:6-7",
                     help="comma list of kind:log2size:kmin-kmax (kind rmat or rgg)")
+    ap.add_argument("--leg-batch-graphs", type=int, default=256,
+                    help="tc mode: graphs of the reduced batch leg (every (4096 / N)-th graph of the 4096-graph "
+                         "batch; 0 = no batch leg)")
+    ap.add_argument("--no-select-leg", action="store_true", help="tc mode: skip the selector leg")
     return ap.parse_args()
 
 
@@ -220,10 +224,9 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import atc
     import oracle
     t0 = time.perf_counter()
-    raw = atc.gen_rmat(a.scale, a.edge_factor, a.seed)
+    raw = oracle.gen_rmat(a.scale, a.edge_factor, a.seed)  # the same bytes as libatc's generator
     loff, lcols = oracle.lower_csr(raw)
     m = int(loff[-1])
     setup = time.perf_counter() - t0
@@ -250,6 +253,12 @@ def run_reference(a):
         secs += time.perf_counter() - t1
         edges += e
     v = edges / secs if secs > 0 else None
+    # the same count on one host thread, on a sparser sample of the same kind (vertex 0, the top
+    # hub, is in phase 0 of every stride and is left out of both by starting at phase 1)
+    stride1 = stride * max(1, nthreads)
+    t1 = time.perf_counter()
+    _, e1 = oracle.tc_count_lower_sample(loff, lcols, stride1, 1, 1)
+    s1 = time.perf_counter() - t1
     cfg = workload_config(a)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": steps,
@@ -258,7 +267,10 @@ def run_reference(a):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": "per step every %d-th vertex u with all its smaller-neighbour edges "
                                    "(OrgTriangleCount scalar merge, other_order/set_operation.cpp:129-144); "
-                                   "graph build %.1f s untimed" % (stride, setup)},
+                                   "graph build %.1f s untimed" % (stride, setup),
+                         "one_thread": {"value": e1 / s1 if s1 > 0 else None, "unit": UNIT, "cores": 1,
+                                        "sample": "every %d-th vertex u from vertex 1 (%d edges), %.1f s"
+                                                  % (stride1, e1, s1)}},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "graph": {"n": int(n), "m": m},
     }
@@ -345,9 +357,12 @@ def run_ours(a):
     peak, peak_kind = measured_peak()
     achieved = alg / (kern_ms * 1e-3) / 1e9
 
-    # ---- e2e: public C ABI from pinned host buffers
+    # ---- e2e: public C ABI from pinned host buffers; the library's phase events give the
+    # stage breakdown of each step
     e2e_ms = []
+    stage_ms = {}
     for i in range(a.e2e_steps + 1 if a.e2e_steps > 0 else 0):
+        atc.phase_timing(i > 0)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -361,7 +376,12 @@ def run_ours(a):
         assert cnt == head_count
         if i > 0:  # first pass warms the allocator pools
             e2e_ms.append(max(wall, e0.elapsed_time(e1)))
+            for name, depth, ms in atc.phase_times():
+                stage_ms.setdefault((depth, name), []).append(ms)
+    atc.phase_timing(False)
     e2e_step = statistics.mean(e2e_ms) if e2e_ms else None
+    stages = {("  " * d) + nm: statistics.mean(v) for (d, nm), v in stage_ms.items() if len(v) == len(e2e_ms)}
+    top = sum(v for k, v in stages.items() if not k.startswith(" "))
     if dist and e2e_step is not None:
         e2e_step = sharded_throughput(m, e2e_step, 0, dist, "cuda")[1]
     e2e_value = m / (e2e_step * 1e-3) if e2e_step else None
@@ -382,11 +402,24 @@ def run_ours(a):
                      "achieved_min": alg_min / (kern_ms * 1e-3) / 1e9,
                      "frac_min": alg_min / (kern_ms * 1e-3) / 1e9 / peak},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nraw * 8, "d2h_bytes_per_step": 8,
-                "ms_per_step": e2e_step, "steps": len(e2e_ms)},
+                "ms_per_step": e2e_step, "steps": len(e2e_ms),
+                "stages_ms": stages,
+                "stages_note": "device time between each library phase's start and end events on the step's stream "
+                               "(indented = nested); unattributed = step time outside the top-level phases "
+                               "(host work before the first and after the last event)",
+                "unattributed_ms": (e2e_step - top) if e2e_step else None},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "pretc_s_first_call": pretc_s,
     }
+    csr.free()
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and a.leg_batch_graphs > 0:
+        step = max(1, 4096 // a.leg_batch_graphs)
+        idx = list(range(0, 4096, step))[: a.leg_batch_graphs]
+        line["batch_leg"] = batch_leg(a, idx, ["bisson", "hu"], sp, stream)
+    if rank == 0 and world == 1 and not a.no_select_leg:
+        line["select_leg"] = select_leg()
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         import oracle
         off, cols = oracle.lower_csr(host_raw.numpy())
@@ -483,26 +516,31 @@ def batch_params(count, seed):
     return out
 
 
-def run_batch(a):
-    """Batched TC of seeded Chung-Lu graphs: one CUDA-graph replay for all graphs vs a per-graph loop."""
+BATCH_CANDIDATES = [{}, {"bisson_warp_max": 128}, {"bisson_warp_max": 64, "bisson_cutover": 16},
+                    {"bisson_warp_chunk": 256, "bisson_block_chunk": 1024},
+                    {"bisson_warp_chunk": 2048, "bisson_block_chunk": 8192},
+                    {"bisson_cutover": 64}, {"group_by_source": 1}, {"group_by_source": 1, "bisson_cutover": 8}]
+
+
+def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
+    """Graphs `indices` of the seeded Chung-Lu batch (batch_params(4096, seed)) counted in one
+    CUDA-graph replay (autotuned items) and, for comparison, one atc_tc call per graph with each
+    of `plain_kernels` (host-synchronised, L2 flushed before each timed call)."""
     import ctypes as C
     import torch
     import atc
-    torch.cuda.set_device(0)
-    atc.init(0)
-    stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    params = batch_params(a.batch_graphs, a.seed)
+    allp = batch_params(max(4096, max(indices) + 1), a.seed)
+    params = [(i, allp[i]) for i in indices]
     # sizes first, so the batch's union is allocated once
     tot_n = tot_m = 0
-    for i, (n, gamma, d) in enumerate(params):
+    for i, (n, gamma, d) in params:
         cnt = C.c_uint64(0)
         assert atc.lib().atc_gen_chunglu_device(n, gamma, d, a.seed * 100003 + i, None, 0, C.byref(cnt), sp) == 0
         tot_n += n
         tot_m += int(cnt.value)
     batch = atc.Batch()
     batch.reserve(tot_n, tot_m, stream=sp)
-    kfixed = [atc.Kernel[x.strip().upper()] for x in a.batch_plain_kernels.split(",")]
+    kfixed = [atc.Kernel[x.strip().upper()] for x in plain_kernels]
     plain_ms = [[] for _ in kfixed]
     plain_counts = []
     dirs = []
@@ -512,7 +550,7 @@ def run_batch(a):
     # and the batch, cannot do)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     t_setup = time.perf_counter()
-    for i, (n, gamma, d) in enumerate(params):
+    for i, (n, gamma, d) in params:
         pairs = atc.gen_chunglu_device(n, gamma, d, a.seed * 100003 + i, stream=sp)
         csr = atc.pretc_device(pairs.data_ptr(), pairs.shape[0], atc.Dir.ADIRECTION, stream=sp)
         for j, kf in enumerate(kfixed):
@@ -529,7 +567,7 @@ def run_batch(a):
         wmin_adir += csr.wedges_min
         chosen = csr
         dsel = "A-direction"
-        if a.batch_select:
+        if getattr(a, "batch_select", False):
             alt = atc.pretc_device(pairs.data_ptr(), pairs.shape[0], atc.Dir.DEGREE, stream=sp)
             if alt.wedges_min < csr.wedges_min:
                 chosen, dsel = alt, "degree"
@@ -539,14 +577,13 @@ def run_batch(a):
         csr.free()
         if chosen is not csr:
             chosen.free()
-        elif a.batch_select:
+        elif getattr(a, "batch_select", False):
             alt.free()
         del pairs
+    del flush
     setup_s = time.perf_counter() - t_setup
     ng, n_all, m_all = batch.info()
-    cands = [{}, {"bisson_warp_max": 128}, {"bisson_warp_max": 64, "bisson_cutover": 16},
-             {"bisson_warp_chunk": 256, "bisson_block_chunk": 1024}, {"bisson_warp_chunk": 2048, "bisson_block_chunk": 8192},
-             {"bisson_cutover": 64}, {"group_by_source": 1}, {"group_by_source": 1, "bisson_cutover": 8}]
+    cands = candidates or BATCH_CANDIDATES
     best, tune_ms = batch.tune(cands, stream=sp)
     counts, _ = batch.run(stream=sp)
     assert counts.tolist() == plain_counts, "batched and per-graph counts differ"
@@ -555,10 +592,13 @@ def run_batch(a):
         _, st = batch.run(stream=sp)
         times.append(st.kernel_ms)
     batch_ms = statistics.mean(times)
-    plain_total = sum(plain_ms[0])
-    line = {
-        "mode": "batch", "metric": "graphs/s, batched (one CUDA-graph replay, autotuned items) vs per-graph loop",
+    batch.free()
+    return {
+        "metric": "graphs/s, batched (one CUDA-graph replay, autotuned items) vs per-graph loop",
         "unit": "graphs/s", "dtype": "int32", "data": "synthetic Chung-Lu graphs generated on the device",
+        "subset": "graphs %s of the %d-graph batch" % (
+            "all" if len(indices) == 4096 else "every %d-th" % (indices[1] - indices[0]) if len(indices) > 1 else
+            str(indices), 4096),
         "graphs": ng, "vertices": n_all, "edges": m_all, "triangles": int(sum(plain_counts)),
         "plain": {kf.name.lower(): {"ms_total": sum(ms), "graphs_per_s": ng / (sum(ms) * 1e-3),
                                     "edges_per_s": m_all / (sum(ms) * 1e-3)} for kf, ms in zip(kfixed, plain_ms)},
@@ -566,13 +606,40 @@ def run_batch(a):
                       "(256 MB written) before each timed call",
         "batched": {"ms_per_replay": batch_ms, "graphs_per_s": ng / (batch_ms * 1e-3),
                     "edges_per_s": m_all / (batch_ms * 1e-3), "tuned": cands[best],
-                    "tune_ms": [float(x) for x in tune_ms], "selection": "work estimate" if a.batch_select else "none",
+                    "tune_ms": [float(x) for x in tune_ms],
+                    "selection": "work estimate" if getattr(a, "batch_select", False) else "none",
                     "degree_chosen": dirs.count("degree"), "wedges_min_adirection": wmin_adir,
                     "wedges_min_selected": wmin_sel},
         "speedup_vs": {kf.name.lower(): sum(ms) / batch_ms for kf, ms in zip(kfixed, plain_ms)},
         "setup_s": setup_s,
     }
+
+
+def run_batch(a):
+    """Batched TC of seeded Chung-Lu graphs: one CUDA-graph replay for all graphs vs a per-graph loop."""
+    import torch
+    import atc
+    torch.cuda.set_device(0)
+    atc.init(0)
+    sp = torch.cuda.current_stream().cuda_stream
+    idx = list(range(a.batch_graphs)) if a.batch_graphs >= 4096 else \
+        list(range(0, 4096, max(1, 4096 // a.batch_graphs)))[: a.batch_graphs]
+    line = {"mode": "batch", **batch_leg(a, idx, [x.strip() for x in a.batch_plain_kernels.split(",")], sp)}
     print(json.dumps(line), flush=True)
+
+
+def select_leg():
+    """The learned selector trained on the committed timings fixture (640 seeded graphs, every
+    (direction, ordering, kernel) triple timed on a GB300): policies on its held-out quarter."""
+    path = os.path.join(ROOT, "tests", "golden", "select_timings.npz")
+    d = np.load(path)
+    feats, times, costs = d["features"], d["times_ms"], d["costs"]
+    ntr = int(0.75 * feats.shape[0])
+    t0 = time.perf_counter()
+    res = train_and_evaluate(feats, times, costs, ntr, seed=1)
+    res["train_s"] = time.perf_counter() - t0
+    res["data"] = "tests/golden/select_timings.npz: %d training, %d held-out graphs" % (ntr, feats.shape[0] - ntr)
+    return res
 
 
 SEL_DIRS = ("ID", "DEGREE", "ADIRECTION")

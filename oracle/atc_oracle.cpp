@@ -1103,4 +1103,41 @@ int32_t orc_gro(const uint64_t* edges, uint64_t ne, int32_t* new_id, int32_t* ma
   return vn;
 }
 
+
+// Seeded R-MAT samples of the benchmark workloads, written independently of libatc so that
+// the CPU arm of the benchmark builds its input without loading the product library.  The
+// generator is the benchmark's own (no reference counterpart: the reference reads dataset
+// files): splitmix64 (Steele, Lea, Flood 2014) over a counter, two 32-bit draws per 64-bit
+// output, one draw per recursion level, quadrant thresholds a, a+b, a+b+c in parts per
+// million scaled to 2^32, row bit then column bit chosen most-significant first.  A CPU test
+// checks that the bytes equal atc_gen_rmat_host's.
+static uint64_t orc_splitmix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+int orc_gen_rmat(uint32_t scale, uint32_t edge_factor, uint32_t a_ppm, uint32_t b_ppm, uint32_t c_ppm, uint64_t seed,
+                 int32_t* out, int nthreads) {
+  const uint64_t sa = a_ppm, sb = sa + b_ppm, sc = sb + c_ppm;
+  if (sc > 1000000ull || scale < 1 || scale > 30) return 1;
+  const uint32_t t1 = (uint32_t)((sa << 32) / 1000000ull), t2 = (uint32_t)((sb << 32) / 1000000ull);
+  const uint32_t t3 = sc == 1000000ull ? 0xFFFFFFFFu : (uint32_t)((sc << 32) / 1000000ull);
+  const uint64_t count = (uint64_t)edge_factor << scale;
+  const uint64_t golden = 0x9E3779B97F4A7C15ull, s0 = orc_splitmix(seed);
+  parallel_for((int64_t)count, nthreads, 1 << 16, [&](int64_t i, int) {
+    uint32_t row = 0, col = 0;
+    uint64_t r = 0;
+    for (uint32_t l = 0; l < scale; ++l) {
+      if ((l & 1) == 0) r = orc_splitmix(s0 + ((uint64_t)i * 16 + (l >> 1) + 1) * golden);
+      const uint32_t x = (l & 1) ? (uint32_t)(r >> 32) : (uint32_t)r;
+      row = (row << 1) | (uint32_t)(x >= t2);
+      col = (col << 1) | (uint32_t)((x >= t1 && x < t2) || x >= t3);
+    }
+    out[2 * i] = (int32_t)row;
+    out[2 * i + 1] = (int32_t)col;
+  });
+  return 0;
+}
+
 }  // extern "C"

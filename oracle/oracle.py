@@ -55,6 +55,9 @@ def lib():
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
         L.orc_hu_csr.restype = C.c_int64
         L.orc_hu_csr.argtypes = [_P, C.c_uint64, _P, _P, C.POINTER(C.c_int64)]
+        L.orc_gen_rmat.restype = C.c_int
+        L.orc_gen_rmat.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P,
+                                   C.c_int]
         L.orc_wedges.restype = C.c_uint64
         L.orc_wedges.argtypes = [_P, _P, C.c_int64]
         _lib = L
@@ -72,6 +75,15 @@ def _ptr(a):
 
 def nthreads_default():
     return os.cpu_count() or 1
+
+
+def gen_rmat(scale, edge_factor=16, seed=1, abc=(570000, 190000, 190000), nthreads=None):
+    """The benchmark's seeded R-MAT samples (edge_factor * 2^scale pairs), generated without
+    libatc (equal to atc.gen_rmat, checked by a CPU test)."""
+    out = np.empty(((edge_factor << scale), 2), dtype=np.int32)
+    rc = lib().orc_gen_rmat(scale, edge_factor, abc[0], abc[1], abc[2], seed, _ptr(out), nthreads or nthreads_default())
+    assert rc == 0, "bad R-MAT parameters"
+    return out
 
 
 def simple_stats(pairs):

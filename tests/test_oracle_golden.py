@@ -242,3 +242,10 @@ def test_oracle_adirection_par_compat_term():
     # compat: minor[0] - flag[2] = 1 - 3 < 0 keeps 0 -> 2, and minor[2] - flag[0] < 0 keeps
     # 2 -> 0 as well: the program's rule is not antisymmetric
     assert out_c.tolist() == _pack([[1, 0], [1, 2], [3, 2], [3, 0], [0, 2], [2, 0]]).tolist()
+
+
+def test_oracle_rmat_generator_equals_libatc():
+    # the CPU arm of the benchmark generates its input with the oracle's copy of the generator
+    import atc
+    for scale, ef, seed in ((6, 4, 3), (10, 16, 1), (14, 8, 9)):
+        assert np.array_equal(oracle.gen_rmat(scale, ef, seed, nthreads=3), atc.gen_rmat(scale, ef, seed))
