@@ -503,6 +503,120 @@ int64_t orc_adirection(const int32_t* pairs, uint64_t np, int32_t* out, int32_t*
   return k;
 }
 
+// Bisson's A-direction relabelling (Bisson/A-direction.cpp:43-163, 196-304): the same
+// symmetric, duplicate-free reading as A-direction-seri (:221-239), a serial peel over the
+// doubled adjacency list (allEdges, :63-80) whose priorities number the outer selection and
+// each wave (:91-126), then new id = nodeNum-1 - rank of (priority, degreeRecord, id)
+// (:29-35,283-292).  degreeRecord is written at the selected vertex in the outer scan (:97)
+// but at the frontier POSITION in the waves (:118, `degreeRecord[i]`); that quirk makes
+// the secondary key depend on the serial visiting order, reproduced here statement by
+// statement.  Fills `lookup` (nodeNum ints) and, when `out` is not null, the bytes of
+// lpBasedGraph.bin: every (i, neighbour) of the symmetric lists relabelled (:293-300).
+// Returns nodeNum (0 for an empty graph, with no output), or -1 where the serial program
+// would loop forever (the float threshold stops growing).
+int64_t orc_adirection_bisson(const int32_t* pairs, uint64_t np, int32_t* lookup, int32_t* out) {
+  int nodeNum = 0;                                                  // :213-219
+  for (uint64_t i = 0; i < np; ++i) {
+    if (pairs[2 * i] > nodeNum) nodeNum = pairs[2 * i];
+    if (pairs[2 * i + 1] > nodeNum) nodeNum = pairs[2 * i + 1];
+  }
+  nodeNum++;
+  std::vector<std::vector<int>> nb(nodeNum);                        // :224-239
+  for (uint64_t i = 0; i < np; ++i) {
+    int s = pairs[2 * i], e = pairs[2 * i + 1];
+    if (s == e) continue;
+    nb[s].push_back(e);
+    nb[e].push_back(s);
+  }
+  int totalEdge = 0;                                                // :242-246
+  for (int i = 0; i < nodeNum; ++i) {
+    std::sort(nb[i].begin(), nb[i].end());
+    nb[i].erase(std::unique(nb[i].begin(), nb[i].end()), nb[i].end());
+    totalEdge += (int)nb[i].size();
+  }
+  // peel (:43-163) on originEdges = every (i, neighbour) in list order (:263-268)
+  const unsigned edgeNum = (unsigned)totalEdge;
+  float threshold = ((float)edgeNum) / nodeNum + 1;                 // :45
+  std::vector<int> priority(nodeNum, -1), degree(nodeNum, 0);
+  for (int i = 0; i < nodeNum; ++i)                                 // :53-56
+    for (int x : nb[i]) { degree[i]++; degree[x]++; }
+  std::vector<int> rt(degree);                                      // :57-58
+  std::vector<long long> off(nodeNum + 1, 0);                       // :59-63
+  for (int i = 0; i < nodeNum - 1; ++i) off[i + 1] = off[i] + degree[i];
+  std::vector<int> all((size_t)edgeNum * 2);                        // :69-80
+  {
+    std::vector<long long> cur(off.begin(), off.end() - 1);
+    for (int i = 0; i < nodeNum; ++i)
+      for (int x : nb[i]) {
+        all[cur[i]++] = x;
+        all[cur[x]++] = i;
+      }
+  }
+  std::vector<int> degreeRecord(nodeNum, 0);
+  std::vector<int> F, Fn;
+  int priorityNum = 0;
+  const int threshold_old = threshold;                              // :83
+  int peeled = 0;
+  for (;;) {                                                        // :85
+    F.clear();
+    Fn.clear();
+    for (int i = 0; i < nodeNum; ++i)                               // :89-98
+      if (rt[i] <= threshold && priority[i] == -1) {
+        F.push_back(i);
+        peeled++;
+        priority[i] = priorityNum;
+        degreeRecord[i] = rt[i];
+      }
+    priorityNum++;
+    while (!F.empty()) {                                            // :101-131
+      for (size_t i = 0; i < F.size(); ++i) {
+        const int cur = F[i];
+        const int* co = all.data() + off[cur];
+        for (int j = 0; j < degree[cur]; ++j) {
+          const int node = co[j];
+          if (priority[node] != -1) {
+            if (priority[node] == priority[cur] && (rt[node] > rt[cur] || (rt[node] == rt[cur] && node > cur)))
+              rt[node]--;
+          } else {
+            rt[node]--;
+            if (rt[node] <= threshold) {
+              Fn.push_back(node);
+              degreeRecord[i] = rt[node];                           // :118, indexed by position
+              peeled++;
+              priority[node] = priorityNum;
+            }
+          }
+        }
+      }
+      std::swap(F, Fn);
+      Fn.clear();
+      priorityNum++;
+    }
+    if (peeled >= nodeNum) break;                                   // :137-139
+    const float grown = threshold + threshold_old;
+    if (!(grown > threshold)) return -1;
+    threshold = grown;
+  }
+  std::vector<int> order(nodeNum);                                  // :283-292
+  for (int i = 0; i < nodeNum; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int a, int b) {
+    if (priority[a] != priority[b]) return priority[a] < priority[b];
+    if (degreeRecord[a] != degreeRecord[b]) return degreeRecord[a] < degreeRecord[b];
+    return a < b;
+  });
+  for (int i = 0; i < nodeNum; ++i) lookup[order[i]] = nodeNum - 1 - i;
+  if (out) {                                                        // :293-300
+    int64_t k = 0;
+    for (int i = 0; i < nodeNum; ++i)
+      for (int x : nb[i]) {
+        out[2 * k] = lookup[i];
+        out[2 * k + 1] = lookup[x];
+        ++k;
+      }
+  }
+  return np ? nodeNum : 0;
+}
+
 // A-order (vertex_ordering/A-order/A-order.cpp:62-247).  Fills `lookup`
 // (maxNodeId+1 ints: badLookUpTable, the new id of every old id), `normal` and
 // `reordered` (2*np ints each: the bytes of the two output files).  Returns ORC_OK,

@@ -55,6 +55,8 @@ def lib():
         L.orc_verification.argtypes = [_P, C.c_uint64, _P]
         L.orc_hu_csr.restype = C.c_int64
         L.orc_hu_csr.argtypes = [_P, C.c_uint64, _P, _P, C.POINTER(C.c_int64)]
+        L.orc_adirection_bisson.restype = C.c_int64
+        L.orc_adirection_bisson.argtypes = [_P, C.c_uint64, _P, _P]
         L.orc_gen_rmat.restype = C.c_int
         L.orc_gen_rmat.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P,
                                    C.c_int]
@@ -138,6 +140,20 @@ def adirection(pairs, want_prio=False):
 
 
 UNSUPPORTED = 5
+
+
+def adirection_bisson(pairs):
+    """Bisson/A-direction.cpp: (lookup, lpBasedGraph.bin pairs), or None where the serial
+    program would not terminate."""
+    p = _pairs(pairs)
+    n = int(p.max()) + 1 if p.size else 1
+    lookup = np.empty(n, dtype=np.int32)
+    out = np.empty((2 * p.shape[0] + 1, 2), dtype=np.int32)
+    r = lib().orc_adirection_bisson(_ptr(p), p.shape[0], _ptr(lookup), _ptr(out))
+    if r < 0:
+        return None
+    sym = simple_stats(p)[1] * 2 if p.size else 0
+    return lookup, out[:sym].copy()
 
 
 def aorder(pairs):

@@ -7,6 +7,7 @@ SHA-256 is recorded so a generator change shows up as a fixture mismatch).  For 
 case the script records what the reference programs output:
 
   adirection   A-direction-seri E.bin        -> lpBasedGraph.bin
+  bisson_adir  Bisson/A-direction E.bin      -> lpBasedGraph.bin (both directions, relabelled)
   aorder       A-order lpBasedGraph.bin      -> lookup-free outputs normal / reordered
   aorder_raw   A-order E.bin                 -> normal / reordered on the raw input
   aorder_v2    A-order-v2 lpBasedGraph.bin   -> naive (the 40-column mix, relabelled)
@@ -122,6 +123,10 @@ def case(name, pairs):
         assert r.returncode == 0, r.stdout
         lp = read_pairs(os.path.join(d, "lpBasedGraph.bin"))
         out["adirection"] = record(lp)
+        with tempfile.TemporaryDirectory() as d2:
+            r = run([os.path.join(REF, "Bisson-A-direction"), e], d2)
+            assert r.returncode == 0, r.stdout
+            out["bisson_adir"] = record(read_pairs(os.path.join(d2, "lpBasedGraph.bin")))
 
         for key, src in (("aorder", os.path.join(d, "lpBasedGraph.bin")), ("aorder_raw", e)):
             src_pairs = read_pairs(src)

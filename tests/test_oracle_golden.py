@@ -43,6 +43,15 @@ def test_adirection(golden, name):
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_adirection_bisson(golden, name):
+    # Bisson/A-direction.cpp's lpBasedGraph.bin, position-indexed degreeRecord included
+    c = golden["cases"][name]
+    lookup, out = oracle.adirection_bisson(golden_input(c))
+    check_pairs(out, c["bisson_adir"])
+    assert np.array_equal(np.sort(lookup), np.arange(lookup.size))
+
+
+@pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("which", ["aorder", "aorder_raw"])
 def test_aorder(golden, name, which):
     c = golden["cases"][name]
