@@ -49,6 +49,7 @@ class Order(enum.IntEnum):
     DEGREE_DESC = 2
     AORDER_V2 = 3
     GRO = 4
+    ADIRECTION_BISSON = 5
 
 
 class Relabel(enum.IntEnum):
@@ -56,6 +57,7 @@ class Relabel(enum.IntEnum):
     AORDER_V2 = 1
     OUTDEG_DESC = 2
     GRO = 3
+    ADIRECTION_BISSON = 4
 
 
 class Kernel(enum.IntEnum):
@@ -81,7 +83,8 @@ class Tuning(C.Structure):
         ("bisson_slots", C.c_int32),
         ("group_by_source", C.c_int32),
         ("kcl_dense", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("edge_kernels", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

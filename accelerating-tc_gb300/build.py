@@ -39,6 +39,7 @@ CLI_PROGRAMS = {
     "tric_gpu": "tc_main.cpp",
     "a_direction_seri": "order_main.cpp",
     "a_order": "order_main.cpp",
+    "bisson_a_direction": "order_main.cpp",
     "a_order_v2": "order_main.cpp",
     "kcl": "kcl_main.cpp",
     "cost_func_cal": "order_main.cpp",

@@ -2,6 +2,9 @@
 //
 //   a_direction_seri <edges.bin>     edge_directing/A-direction-seri.cpp:170-288
 //        writes lpBasedGraph (text "src dst") and lpBasedGraph.bin in the working directory
+//   bisson_a_direction <edges.bin>   Bisson/A-direction.cpp:196-336 (READFROMFILE, EDGEBINARY)
+//        writes lpBasedGraph.bin (every edge in both directions, relabelled by the peel
+//        order) and the empty lpBasedGraph the program also creates
 //   a_order <edges.bin>              vertex_ordering/A-order/A-order.cpp:62-247
 //        writes normal and reordered in the working directory
 //   a_order_v2 <edges.bin>           vertex_ordering/A-order/A-order-v2.cpp:14-193
@@ -87,6 +90,23 @@ int main(int argc, char** argv) {
   fclose(t);
   if (!write_pairs("lpBasedGraph.bin", out.data(), n_out)) return 1;
   std::cout << "we have dealed with " << n_out << " edges up to now" << std::endl;
+#elif defined(ATC_PROGRAM_BISSON_A_DIRECTION)
+  int32_t mx = 0;
+  for (int32_t x : pairs) mx = x > mx ? x : mx;
+  std::vector<int32_t> lookup((size_t)mx + 1);
+  s = atc_relabel(pairs.data(), np, ATC_RELABEL_ADIRECTION_BISSON, lookup.data(), nullptr, nullptr, nullptr);
+  if (s != ATC_OK) return fail("atc_relabel", s);
+  // the program writes each vertex's sorted, duplicate-free neighbours (:293-300)
+  std::vector<int32_t> sym(4 * (np ? np : 1));
+  uint64_t ns = 0;
+  s = atc_simplify_host(pairs.data(), np, 1, sym.data(), &ns);
+  if (s != ATC_OK) return fail("atc_simplify_host", s);
+  for (uint64_t i = 0; i < 2 * ns; ++i) sym[i] = lookup[sym[i]];
+  FILE* t = fopen("lpBasedGraph", "w");  // created empty, as the program leaves it
+  if (!t) return 1;
+  fclose(t);
+  if (!write_pairs("lpBasedGraph.bin", sym.data(), ns)) return 1;
+  std::cout << "we have dealed with 0 edges up to now" << std::endl;  // the program's count stays 0
 #elif defined(ATC_PROGRAM_A_ORDER)
   int32_t mx = 0;
   for (int32_t x : pairs) mx = x > mx ? x : mx;

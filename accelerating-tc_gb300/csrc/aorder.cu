@@ -523,7 +523,7 @@ extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel
                                   int32_t* normal, int32_t* relabeled, atc_stream st) try {
   ATC_CHECK_ARG(lookup != nullptr, "lookup is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
-  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_GRO, "unknown atc_relabel_kind");
+  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_ADIRECTION_BISSON, "unknown atc_relabel_kind");
   cudaStream_t s = as_stream(st);
   int maxid = 0;  // the programs start maxNodeId at 0, so an empty list has one vertex
   for (uint64_t i = 0; i < 2 * np; ++i) {
@@ -539,6 +539,19 @@ extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel
   if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, s));
   if (kind == ATC_RELABEL_GRO) {
     ATC_TRY(gro_lookup(d.p, np, n_v, lk.p, s));
+    if (np) ATC_CK(cudaMemcpyAsync(o.p, d.p, sizeof(int2) * np, cudaMemcpyDeviceToDevice, s));
+  } else if (kind == ATC_RELABEL_ADIRECTION_BISSON) {
+    SimpleEdges e;
+    ATC_TRY(build_simple_edges(d.p, np, &e, s));
+    DevBuf<int32_t> deg;
+    ATC_TRY(deg.alloc(n_v, s));
+    if (np == 0) {
+      ATC_CK(cudaMemsetAsync(deg.p, 0, sizeof(int32_t) * n_v, s));
+      e.n_in = n_v;  // the programs number vertex 0 even for an empty file
+    } else {
+      ATC_TRY(simple_degrees(e, deg.p, s));
+    }
+    ATC_TRY(bisson_adirection_lookup(e, deg.p, lk.p, s));
     if (np) ATC_CK(cudaMemcpyAsync(o.p, d.p, sizeof(int2) * np, cudaMemcpyDeviceToDevice, s));
   } else {
     ATC_TRY(relabel_lookup(d.p, nullptr, 1, np, n_v, kind, lk.p, o.p, s));

@@ -12,6 +12,10 @@ namespace atc {
 // Sorts n keys on bits [begin_bit, end_bit).  `keys` and `alt` are two buffers of n
 // elements; on return `keys` points at the sorted data (the two may be swapped).
 atc_status sort_keys_u64(uint64_t*& keys, uint64_t*& alt, size_t n, int begin_bit, int end_bit, cudaStream_t s);
+// Stable sort of n (key, value) pairs on key bits [begin_bit, end_bit); on return `keys` /
+// `vals` point at the sorted data (each may be swapped with its alternate buffer).
+atc_status sort_pairs_u64_i32(uint64_t*& keys, uint64_t*& kalt, int32_t*& vals, int32_t*& valt, size_t n, int begin_bit,
+                             int end_bit, cudaStream_t s);
 // Unique over sorted keys; *n_out (host) receives the count.
 atc_status unique_u64(const uint64_t* in, uint64_t* out, size_t n, size_t* n_out, cudaStream_t s);
 // out[i] = sum_{j<i} in[j], for n elements.
@@ -45,6 +49,11 @@ atc_status simple_degrees(const SimpleEdges& e, int32_t* deg, cudaStream_t s);
 // graph given by canonical keys: prio (n_in ints, device).  stats: number of waves.
 atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* prio, int* waves_out,
                            cudaStream_t s);
+
+// Bisson's A-direction relabelling (Bisson/A-direction.cpp:43-163,283-292) of the simple
+// graph given by canonical keys: lookup (n_in ints, device) = the new id of every vertex.
+// ATC_ERR_UNSUPPORTED where the serial program would not terminate.
+atc_status bisson_adirection_lookup(const SimpleEdges& e, const int32_t* deg, int32_t* lookup, cudaStream_t s);
 
 // Core numbers (n_in ints, device) of the simple graph given by canonical keys.
 atc_status core_numbers(const SimpleEdges& e, const int32_t* deg, int32_t* core, cudaStream_t s);

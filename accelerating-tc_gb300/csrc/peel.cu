@@ -166,6 +166,292 @@ atc_status peel_priorities(const SimpleEdges& e, const int32_t* deg, int32_t* pr
   return ATC_OK;
 }
 
+// ---- Bisson's A-direction relabelling (Bisson/A-direction.cpp:43-163, 283-292) ----------
+// The program peels serially over a doubled adjacency list and numbers the outer selection
+// and every wave with one priority each (:91-126); the new ids sort the vertices by
+// (priority, degreeRecord, id) and reverse the rank (:283-292).  degreeRecord is written at
+// the selected vertex in the outer scan but at the frontier POSITION in the waves (:118),
+// so it depends on the order in which the serial loop admits vertices.  That order is
+// rebuilt here wave by wave, in parallel:
+//   - the list of x (allEdges, :69-80) holds N(x) ∩ [0, x), then N(x), then N(x) ∩ (x, n),
+//     each ascending, so a neighbour y sits at two known entries of it (first, second);
+//   - an unpeeled y loses 1 per entry processed and is admitted at its k-th loss,
+//     k = rt(y) - floor(threshold) (rt > threshold while unpeeled, so the loss that crosses
+//     leaves rt exactly at the floor): that is entry (k odd ? first : second) of its
+//     ceil(k/2)-th frontier neighbour in frontier order;
+//   - the next frontier lists the admitted vertices by (position of that neighbour, entry);
+//   - every admission writes degreeRecord[position] = floor(threshold); writes happen in
+//     program order across waves, so the last one wins as in the serial program.
+// Pairs (y, position of an adjacent frontier vertex) are radix-sorted per wave to find
+// each y's ceil(k/2)-th frontier neighbour.
+namespace {
+
+__global__ void both_dir_keys_kernel(const uint64_t* keys, int64_t m, int B, uint64_t* out) {
+  const uint64_t mask = (1ull << B) - 1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += stride) {
+    const uint64_t k = keys[i], a = k >> B, b = k & mask;
+    out[2 * i] = (a << B) | b;
+    out[2 * i + 1] = (b << B) | a;
+  }
+}
+
+// adj[j] = the low half of the sorted both-direction keys; nlow[x] = |N(x) ∩ [0, x)|.
+__global__ void sorted_adj_kernel(const uint64_t* sk, int64_t m2, int B, int32_t* adj) {
+  const uint64_t mask = (1ull << B) - 1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m2; i += stride)
+    adj[i] = (int32_t)(sk[i] & mask);
+}
+
+__global__ void nlow_kernel(const int64_t* off, const int32_t* adj, int64_t n, int32_t* nlow) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += stride) {
+    int64_t lo = off[x], hi = off[x + 1];
+    const int64_t b = lo;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (adj[mid] < (int32_t)x) lo = mid + 1; else hi = mid;
+    }
+    nlow[x] = (int32_t)(lo - b);
+  }
+}
+
+__global__ void bis_init_kernel(const int32_t* deg, int64_t n, int32_t* rt, int32_t* prio, int32_t* drec) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    rt[v] = 2 * deg[v];
+    prio[v] = -1;
+    drec[v] = 0;
+  }
+}
+
+// Outer selection (:89-98), in id order: flag, then (after a scan) place.
+__global__ void bis_flag_kernel(const int32_t* rt, const int32_t* prio, int64_t n, float thr, int32_t* flag) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride)
+    flag[v] = prio[v] == -1 && (float)rt[v] <= thr;
+}
+
+__global__ void bis_place_kernel(const int32_t* flag, const int64_t* pos, const int32_t* rt, int64_t n, int32_t P,
+                                 int32_t* prio, int32_t* drec, int32_t* F) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride)
+    if (flag[v]) {
+      F[pos[v]] = (int32_t)v;
+      prio[v] = P;
+      drec[v] = rt[v];
+    }
+}
+
+__global__ void bis_fdeg_kernel(const int32_t* F, int64_t nf, const int32_t* deg, int32_t* fd) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nf; p += stride) fd[p] = deg[F[p]];
+}
+
+// (y << 32 | position, rank of y in N(x)) for every unpeeled neighbour y of frontier
+// position p; peeled neighbours get the all-ones key, which sorts last.
+__global__ void bis_emit_kernel(const int32_t* F, int64_t nf, const int64_t* fstart, const int64_t* off,
+                                const int32_t* adj, const int32_t* prio, uint64_t* keys, int32_t* vals) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; p < nf; p += warps) {
+    const int32_t x = F[p];
+    const int64_t b = off[x], d = off[x + 1] - b, at = fstart[p];
+    for (int64_t j = lane; j < d; j += 32) {
+      const int32_t y = adj[b + j];
+      keys[at + j] = prio[y] == -1 ? (((uint64_t)(uint32_t)y << 32) | (uint64_t)p) : ~0ull;
+      vals[at + j] = (int32_t)j;
+    }
+  }
+}
+
+// One thread per segment start of the sorted pairs: admit y at its k-th loss, or take
+// away 2 per adjacent frontier vertex.  cand gets (position << 32 | entry, y).
+__global__ void bis_admit_kernel(const uint64_t* keys, const int32_t* vals, int64_t total, const int32_t* F,
+                                 const int32_t* deg, const int32_t* nlow, int32_t T, int32_t P, int32_t* rt,
+                                 int32_t* prio, int32_t* drec, uint64_t* ckeys, int32_t* cvals, int* ccount) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
+    const uint64_t key = keys[i];
+    if (key == ~0ull) continue;
+    const uint32_t y = (uint32_t)(key >> 32);
+    if (i > 0 && (uint32_t)(keys[i - 1] >> 32) == y) continue;  // not a segment start
+    int64_t lo = i + 1, hi = total;  // first pair of another vertex (the sentinels too)
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (keys[mid] != ~0ull && (uint32_t)(keys[mid] >> 32) == y) lo = mid + 1; else hi = mid;
+    }
+    const int64_t c = lo - i;
+    const int32_t k = rt[y] - T;  // >= 1
+    if (2 * c >= (int64_t)k) {
+      const int64_t cross = i + (k + 1) / 2 - 1;
+      const uint32_t p = (uint32_t)(keys[cross] & 0xffffffffull);
+      const int32_t r = vals[cross];
+      const int32_t x = F[p];
+      const int32_t nl = nlow[x];
+      const int32_t entry = (k & 1) ? ((int32_t)y < x ? r : nl + r) : ((int32_t)y < x ? nl + r : deg[x] + r);
+      prio[y] = P;
+      rt[y] = T;
+      drec[p] = T;  // :118 writes at the frontier position
+      const int at = atomicAdd(ccount, 1);
+      ckeys[at] = ((uint64_t)p << 32) | (uint32_t)entry;
+      cvals[at] = (int32_t)y;
+    } else {
+      rt[y] -= (int32_t)(2 * c);
+    }
+  }
+}
+
+__global__ void bis_rank_keys_kernel(const int32_t* prio, const int32_t* drec, int64_t n, uint64_t* keys, int32_t* ids) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    keys[v] = ((uint64_t)(uint32_t)prio[v] << 32) | (uint32_t)drec[v];
+    ids[v] = (int32_t)v;
+  }
+}
+
+__global__ void bis_lookup_kernel(const int32_t* ids, int64_t n, int32_t* lookup) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    lookup[ids[i]] = (int32_t)(n - 1 - i);
+}
+
+}  // namespace
+
+atc_status bisson_adirection_lookup(const SimpleEdges& e, const int32_t* deg, int32_t* lookup, cudaStream_t s) {
+  Phase ph("bisson_adirection", s);
+  const int64_t n = e.n_in, m = e.m, m2 = 2 * m;
+  if (n == 0) return ATC_OK;
+  DevBuf<int64_t> off, fstart, pos;
+  DevBuf<int32_t> adj, nlow, rt, prio, drec, fa, fb, flag, fd, va, vb, cva, cvb;
+  DevBuf<uint64_t> ka, kb, cka, ckb;
+  DevBuf<int> cnt;
+  // sorted symmetric adjacency
+  ATC_TRY(off.alloc(n + 1, s));
+  ATC_TRY(exclusive_scan_i32_to_i64(deg, off.p, n, s));
+  ATC_CK(cudaMemcpyAsync(off.p + n, &m2, sizeof(m2), cudaMemcpyHostToDevice, s));
+  // ka/kb/va/vb: the both-direction keys, each wave's (y, position) pairs (at most 2m) and
+  // the final (priority, degreeRecord) keys of all n vertices
+  const int64_t cap = std::max(m2, n) + 1;
+  ATC_TRY(adj.alloc(m2 + 1, s));
+  ATC_TRY(ka.alloc(cap, s));
+  ATC_TRY(kb.alloc(cap, s));
+  if (m) {
+    both_dir_keys_kernel<<<grid_for(m, 256), 256, 0, s>>>(e.keys.p, m, e.bits, ka.p);
+    ATC_CK(cudaGetLastError());
+    uint64_t* k0 = ka.p;
+    uint64_t* k1 = kb.p;
+    ATC_TRY(sort_keys_u64(k0, k1, m2, 0, 2 * e.bits, s));
+    sorted_adj_kernel<<<grid_for(m2, 256), 256, 0, s>>>(k0, m2, e.bits, adj.p);
+    ATC_CK(cudaGetLastError());
+  }
+  ATC_TRY(nlow.alloc(n, s));
+  nlow_kernel<<<grid_for(n, 256), 256, 0, s>>>(off.p, adj.p, n, nlow.p);
+  ATC_TRY(rt.alloc(n, s));
+  ATC_TRY(prio.alloc(n, s));
+  ATC_TRY(drec.alloc(n, s));
+  bis_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(deg, n, rt.p, prio.p, drec.p);
+  ATC_CK(cudaGetLastError());
+  ATC_TRY(fa.alloc(n + 1, s));
+  ATC_TRY(fb.alloc(n + 1, s));
+  ATC_TRY(flag.alloc(n + 1, s));
+  ATC_TRY(pos.alloc(n + 1, s));
+  ATC_TRY(fd.alloc(n + 1, s));
+  ATC_TRY(fstart.alloc(n + 1, s));
+  ATC_TRY(va.alloc(cap, s));
+  ATC_TRY(vb.alloc(cap, s));
+  ATC_TRY(cka.alloc(n + 1, s));
+  ATC_TRY(ckb.alloc(n + 1, s));
+  ATC_TRY(cva.alloc(n + 1, s));
+  ATC_TRY(cvb.alloc(n + 1, s));
+  ATC_TRY(cnt.alloc(1, s));
+
+  // threshold arithmetic of :45, :83, :138 on the host (edgeNum = 2m, nodeNum = max id + 1)
+  const unsigned edgeNum = (unsigned)m2;
+  const int nodeNum = (int)n;
+  float threshold = ((float)edgeNum) / nodeNum + 1;
+  const int threshold_old = threshold;
+  int32_t P = 0;
+  int64_t peeled = 0;
+  int32_t* F = fa.p;
+  int32_t* N = fb.p;
+  for (;;) {
+    // outer selection in id order
+    ATC_CK(cudaMemsetAsync(flag.p + n, 0, sizeof(int32_t), s));
+    bis_flag_kernel<<<grid_for(n, 256), 256, 0, s>>>(rt.p, prio.p, n, threshold, flag.p);
+    ATC_CK(cudaGetLastError());
+    ATC_TRY(exclusive_scan_i32_to_i64(flag.p, pos.p, n + 1, s));
+    bis_place_kernel<<<grid_for(n, 256), 256, 0, s>>>(flag.p, pos.p, rt.p, n, P, prio.p, drec.p, F);
+    ATC_CK(cudaGetLastError());
+    int64_t nf = 0;
+    ATC_CK(cudaMemcpyAsync(&nf, pos.p + n, sizeof(nf), cudaMemcpyDeviceToHost, s));
+    ATC_CK(cudaStreamSynchronize(s));
+    peeled += nf;
+    ++P;
+    const int32_t T = (int32_t)floorf(threshold);
+    while (nf > 0) {
+      // pairs (y, position) of the unpeeled neighbours of the frontier
+      bis_fdeg_kernel<<<grid_for(nf, 256), 256, 0, s>>>(F, nf, deg, fd.p);
+      ATC_CK(cudaMemsetAsync(fd.p + nf, 0, sizeof(int32_t), s));
+      ATC_CK(cudaGetLastError());
+      ATC_TRY(exclusive_scan_i32_to_i64(fd.p, fstart.p, nf + 1, s));
+      int64_t total = 0;
+      ATC_CK(cudaMemcpyAsync(&total, fstart.p + nf, sizeof(total), cudaMemcpyDeviceToHost, s));
+      ATC_CK(cudaStreamSynchronize(s));
+      ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int), s));
+      if (total > 0) {
+        bis_emit_kernel<<<grid_for(nf * 32, 256), 256, 0, s>>>(F, nf, fstart.p, off.p, adj.p, prio.p, ka.p, va.p);
+        ATC_CK(cudaGetLastError());
+        uint64_t* k0 = ka.p;
+        uint64_t* k1 = kb.p;
+        int32_t* v0 = va.p;
+        int32_t* v1 = vb.p;
+        ATC_TRY(sort_pairs_u64_i32(k0, k1, v0, v1, total, 0, 64, s));
+        bis_admit_kernel<<<grid_for(total, 256), 256, 0, s>>>(k0, v0, total, F, deg, nlow.p, T, P, rt.p, prio.p,
+                                                              drec.p, cka.p, cva.p, cnt.p);
+        ATC_CK(cudaGetLastError());
+      }
+      int hc = 0;
+      ATC_CK(cudaMemcpyAsync(&hc, cnt.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      ATC_CK(cudaStreamSynchronize(s));
+      // the next frontier in admission order
+      uint64_t* c0 = cka.p;
+      uint64_t* c1 = ckb.p;
+      int32_t* w0 = cva.p;
+      int32_t* w1 = cvb.p;
+      ATC_TRY(sort_pairs_u64_i32(c0, c1, w0, w1, (size_t)hc, 0, 64, s));
+      if (hc) ATC_CK(cudaMemcpyAsync(N, w0, sizeof(int32_t) * hc, cudaMemcpyDeviceToDevice, s));
+      std::swap(F, N);
+      nf = hc;
+      peeled += nf;
+      ++P;
+    }
+    if (peeled >= n) break;
+    const float grown = threshold + threshold_old;
+    if (!(grown > threshold)) {
+      set_error("Bisson A-direction threshold stopped growing at %g with %lld vertices unpeeled", (double)threshold,
+                (long long)(n - peeled));
+      return ATC_ERR_UNSUPPORTED;
+    }
+    threshold = grown;
+  }
+  // new id = nodeNum - 1 - rank of (priority, degreeRecord, id)
+  {
+    uint64_t* k0 = ka.p;
+    uint64_t* k1 = kb.p;
+    int32_t* v0 = va.p;
+    int32_t* v1 = vb.p;
+    bis_rank_keys_kernel<<<grid_for(n, 256), 256, 0, s>>>(prio.p, drec.p, n, k0, v0);
+    ATC_CK(cudaGetLastError());
+    ATC_TRY(sort_pairs_u64_i32(k0, k1, v0, v1, n, 0, 64, s));
+    bis_lookup_kernel<<<grid_for(n, 256), 256, 0, s>>>(v0, n, lookup);
+    ATC_CK(cudaGetLastError());
+  }
+  ATC_CK(cudaStreamSynchronize(s));
+  return ATC_OK;
+}
+
 // ---- k-core numbers (for the k-core direction, edge_directing/kcore_direction.cpp:91-146) ----
 // Level-synchronous peeling: at level k every vertex whose remaining degree is <= k
 // leaves with core number k, each leaving vertex lowers its remaining neighbours by 1,

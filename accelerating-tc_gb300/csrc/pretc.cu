@@ -309,7 +309,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
                              atc_csr* out, int32_t* perm_out, cudaStream_t s) {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION_PAR, "unknown atc_dir");
-  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_GRO, "unknown atc_order");
+  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_ADIRECTION_BISSON, "unknown atc_order");
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
   SimpleEdges e;
@@ -355,6 +355,9 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
       peeled = true;
     } else if (order == ATC_ORDER_AORDER) {
       ATC_TRY(aorder_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, perm.p, nullptr, s, deg.p));
+    } else if (order == ATC_ORDER_ADIRECTION_BISSON) {
+      // the program numbers every id up to the largest one in its input (:213-219)
+      ATC_TRY(bisson_adirection_lookup(e, deg.p, perm.p, s));
     } else if (order == ATC_ORDER_GRO) {
       // GRO of the undirected graph: both directions of every simple edge
       DevBuf<int2> sym;

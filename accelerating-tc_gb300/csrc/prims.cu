@@ -26,6 +26,27 @@ atc_status sort_keys_u64(uint64_t*& keys, uint64_t*& alt, size_t n, int begin_bi
   return ATC_OK;
 }
 
+atc_status sort_pairs_u64_i32(uint64_t*& keys, uint64_t*& kalt, int32_t*& vals, int32_t*& valt, size_t n, int begin_bit,
+                             int end_bit, cudaStream_t s) {
+  if (n <= 1) return ATC_OK;
+  cub::DoubleBuffer<uint64_t> dk(keys, kalt);
+  cub::DoubleBuffer<int32_t> dv(vals, valt);
+  size_t tmp = 0;
+  ATC_CK(cub::DeviceRadixSort::SortPairs(nullptr, tmp, dk, dv, (int64_t)n, begin_bit, end_bit, s));
+  DevBuf<char> t;
+  ATC_TRY(t.alloc(tmp, s));
+  ATC_CK(cub::DeviceRadixSort::SortPairs(t.p, tmp, dk, dv, (int64_t)n, begin_bit, end_bit, s));
+  if (dk.Current() != keys) {
+    kalt = keys;
+    keys = dk.Current();
+  }
+  if (dv.Current() != vals) {
+    valt = vals;
+    vals = dv.Current();
+  }
+  return ATC_OK;
+}
+
 atc_status unique_u64(const uint64_t* in, uint64_t* out, size_t n, size_t* n_out, cudaStream_t s) {
   if (n == 0) { *n_out = 0; return ATC_OK; }
   DevBuf<int64_t> cnt;

@@ -71,7 +71,11 @@ typedef enum atc_order {
   ATC_ORDER_AORDER_V2 = 3,
   /* other_order's GRO order of the simple graph, both directions of every edge
      (vertex_ordering/other_order/porder.cpp:141-226, ATC_RELABEL_GRO) */
-  ATC_ORDER_GRO = 4
+  ATC_ORDER_GRO = 4,
+  /* Bisson's A-direction relabelling of the simple graph (Bisson/A-direction.cpp,
+     ATC_RELABEL_ADIRECTION_BISSON); with ATC_DIR_ID it is the program's A-direction
+     pipeline for Bisson and Fox */
+  ATC_ORDER_ADIRECTION_BISSON = 5
 } atc_order;
 
 /* Rank relabellings of vertex_ordering/A-order (atc_relabel). */
@@ -91,7 +95,13 @@ typedef enum atc_relabel_kind {
      _GRO_newID.txt of its reorder program); `normal` = the pairs as given.  The program
      reads uninitialised memory once a vertex's gain reaches the vertex count; this
      build reads those gains as unset. */
-  ATC_RELABEL_GRO = 3
+  ATC_RELABEL_GRO = 3,
+  /* Bisson's A-direction relabelling (Bisson/A-direction.cpp:43-163,283-304): the serial
+     peel's priorities, then new id = n-1 - rank of (priority, degreeRecord, id), with the
+     program's position-indexed degreeRecord (:118) reproduced.  Counting the relabelled
+     graph with ATC_DIR_ID realises the A-direction orientation as an id order, which is
+     how the program feeds Bisson's kernel.  `normal` = the pairs as given. */
+  ATC_RELABEL_ADIRECTION_BISSON = 4
 } atc_relabel_kind;
 
 typedef enum atc_kernel {
@@ -124,7 +134,11 @@ typedef struct atc_tuning {
   int32_t kcl_dense;         /* k-cliques (atc_kcl_part_tuned): 0 = candidate sets of 65..1024
                                 members on the dense kernel from k = 5 on; -1 = every edge on
                                 the warp search */
-  int32_t reserved[3];
+  int32_t edge_kernels;      /* TriCore- and Fox-style: 1 = per-edge kernels searching the longer
+                                list in global memory, as the reference kernels do (a warp per
+                                edge with 32 pivots; 1..32 threads per edge in work bins);
+                                0 = the longer lists staged in shared memory per group item */
+  int32_t reserved[2];
 } atc_tuning;
 
 /* Oriented CSR on the device (the reference's edgeOffset/edgeRow/adjLength globals,

@@ -6,6 +6,9 @@ orientation, the A-order permutation and its output files, the CSR.  The cost fi
 must print identically to the reference tools.
 """
 import hashlib
+import json
+import os
+import sys
 from math import comb
 
 import numpy as np
@@ -13,7 +16,7 @@ import pytest
 
 import atc
 import oracle
-from conftest import golden_input, load_golden, write_gr
+from conftest import ROOT, golden_input, load_golden, write_gr
 
 pytestmark = pytest.mark.gpu
 
@@ -45,6 +48,32 @@ def test_adirection_matches_reference(golden, name):
     assert sha(got) == c["adirection"]["sha256"]
     _, oprio = oracle.adirection(golden_input(c), want_prio=True)
     assert np.array_equal(prio, oprio)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_adirection_bisson_matches_reference(golden, name):
+    """Bisson/A-direction.cpp: the relabelling (lookup) and its lpBasedGraph.bin output."""
+    c = golden["cases"][name]
+    g = golden_input(c)
+    lookup, normal, rel = atc.relabel(g, atc.Relabel.ADIRECTION_BISSON)
+    olookup, oout = oracle.adirection_bisson(g)
+    assert np.array_equal(lookup, olookup)
+    assert np.array_equal(normal, g) and np.array_equal(rel, lookup[g])
+    out = lookup[atc.simplify(g, symmetric=True)] if g.size else np.zeros((0, 2), dtype=np.int32)
+    assert out.shape[0] == c["bisson_adir"]["count"] and sha(out) == c["bisson_adir"]["sha256"]
+
+
+def test_adirection_bisson_order_in_pretc():
+    # with the id orientation (src = larger new id) the relabelling realises A-direction:
+    # every edge leaves the vertex the peel took first
+    for g in (atc.rmat_graph(13, 16, 5), atc.gen_rgg(30000, 10.0, 2), atc.gen_rmat(12, 8, 3)):
+        want = oracle.tc_count(g)
+        csr = atc.pretc(g, atc.Dir.ID, atc.Order.ADIRECTION_BISSON, want_perm=True)
+        olookup, _ = oracle.adirection_bisson(g)
+        assert np.array_equal(csr.perm[: olookup.size], olookup)
+        for k in KERNELS:
+            assert atc.tc(csr, k)[0] == want, k.name
+        csr.free()
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -149,6 +178,8 @@ def test_counts_all_kernels_and_directions(golden, name):
             got, st = atc.tc(csr, k)
             assert got == want, (d.name, k.name)
             assert st.kernel_used == int(k)
+        for k in (atc.Kernel.FOX, atc.Kernel.TRICORE):  # the per-edge global-search kernels
+            assert atc.tc(csr, k, tuning={"edge_kernels": 1})[0] == want, (d.name, k.name)
         csr.free()
 
 
@@ -168,8 +199,9 @@ def test_tuning_knobs_do_not_change_counts():
     g = atc.rmat_graph(12, 16, 3)
     want = oracle.tc_count(g)
     csr = atc.pretc(g, atc.Dir.ID)  # id orientation: long lists, hubs
-    for t in ({"bisson_cutover": 8}, {"bisson_cutover": 64}, {"fox_rearrange": 1}, {"fox_work_per_thread": 4},
-              {"hu_blocks": 7}, {"tricore_blocks": 3}, {"hu_blocks": 2000}, {"bisson_slots": 1},
+    for t in ({"bisson_cutover": 8}, {"bisson_cutover": 64}, {"fox_rearrange": 1, "edge_kernels": 1},
+              {"fox_work_per_thread": 4, "edge_kernels": 1}, {"edge_kernels": 1},
+              {"hu_blocks": 7}, {"tricore_blocks": 3, "edge_kernels": 1}, {"hu_blocks": 2000}, {"bisson_slots": 1},
               {"bisson_slots": 2}, {"bisson_slots": 4}, {"bisson_slots": 2, "bisson_warp_max": 64, "bisson_cutover": 4}):
         for k in KERNELS:
             assert atc.tc(csr, k, tuning=t)[0] == want, (t, k.name)
@@ -372,6 +404,13 @@ def test_cli_dropins(tmp_path):
     assert r.returncode == 0, r.stderr
     lp = np.fromfile(tmp_path / "lpBasedGraph.bin", dtype=np.int32).reshape(-1, 2)
     assert np.array_equal(lp, oracle.adirection(g))
+    bdir = tmp_path / "bisson"
+    bdir.mkdir()
+    r = subprocess.run([os.path.join(bindir, "bisson_a_direction"), str(e)], cwd=bdir, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(np.fromfile(bdir / "lpBasedGraph.bin", dtype=np.int32).reshape(-1, 2),
+                          oracle.adirection_bisson(g)[1])
+    assert (bdir / "lpBasedGraph").stat().st_size == 0
     r = subprocess.run([os.path.join(bindir, "a_order"), str(tmp_path / "lpBasedGraph.bin")], cwd=tmp_path,
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -543,19 +582,8 @@ def test_kcore_direction_program_matches_oracle():
     assert atc.kcore_direction(np.zeros(0, dtype=np.uint64)).size == 0
 
 
-def _packed(g):
-    return (g[:, 0].astype(np.uint64) << np.uint64(32)) | g[:, 1].astype(np.uint32).astype(np.uint64)
-
-
-def _apeel_graphs():
-    rng = np.random.default_rng(21)
-    yield "rmat12-sym", atc.rmat_graph(12, 16, 2)
-    yield "rmat13-once", atc.simplify(atc.gen_rmat(13, 8, 9), symmetric=False)
-    yield "rmat11-raw", atc.gen_rmat(11, 16, 4)                       # repeats and loops kept
-    yield "uniform", rng.integers(0, 2000, size=(20000, 2)).astype(np.int32)
-    yield "rgg", atc.gen_rgg(20000, 12.0, 3)
-    yield "sparse", rng.integers(0, 5000, size=(2000, 2)).astype(np.int32)  # m / n < 1
-    yield "clique", np.array([(i, j) for i in range(40) for j in range(40) if i != j], dtype=np.int32)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+from apeel_cases import apeel_graphs as _apeel_graphs, packed as _packed  # noqa: E402
 
 
 @pytest.mark.parametrize("compat", [False, True])
@@ -569,6 +597,22 @@ def test_adirection_par_matches_oracle(compat):
         assert np.array_equal(got[2], want[2]), name
         assert got[3] == want[3], name
         assert np.array_equal(got[0], want[0]), name
+
+
+PEEL_GOLDEN = os.path.join(ROOT, "tests", "golden", "peel_par.json")
+
+
+@pytest.mark.skipif(not os.path.exists(PEEL_GOLDEN), reason="no recorded output of the Peel program")
+def test_adirection_par_matches_the_peel_program():
+    """The Peel drop-in (compat comparison, peel.cu:49) against the output file the reference
+    program itself wrote on the same inputs (recorded on a GB300 by make_peel_golden.py)."""
+    with open(PEEL_GOLDEN) as f:
+        rec = json.load(f)["cases"]
+    for name, g in _apeel_graphs():
+        e = _packed(g)
+        assert hashlib.sha256(e.tobytes()).hexdigest() == rec[name]["input"]["sha256"], name
+        got = atc.adirection_par(e, compat=True)[0]
+        assert hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest() == rec[name]["peel_out"]["sha256"], name
 
 
 def test_adirection_par_direction_in_pretc():
