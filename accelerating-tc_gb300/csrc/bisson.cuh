@@ -518,21 +518,32 @@ struct HashQueueProber {
 // time, four coalesced loads in flight per lane.  Shorter lists are laid end to end by
 // a warp prefix sum of their lengths and dealt 32 elements per round; each lane finds
 // the list holding its element by a 5-step binary search over the lanes' start offsets,
-// done with shuffles so that every lane runs the same steps.  Every probe call is made
-// by all 32 lanes together.
+// done with shuffles so that every lane runs the same steps.  The next batch's partners and
+// list bounds (three dependent loads) are loaded while the current batch streams.  Every
+// probe call is made by all 32 lanes together.
 template <class NextBatch, class Prober>
 __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
                                                     int lane, NextBatch next_batch, Prober& pr) {
   unsigned cnt = 0;
-  for (int64_t base = next_batch(); base < i1; base = next_batch()) {
-    int64_t i = base + lane;
-    int len = 0;
-    int64_t pb = 0;
+  auto meta = [&](int64_t base, int64_t* pb, int* len) {
+    const int64_t i = base + lane;
+    *pb = 0;
+    *len = 0;
     if (i < i1) {
-      int32_t p = __ldg(plist + i);
-      pb = __ldg(g.off + p);
-      len = (int)(__ldg(g.off + p + 1) - pb);
+      const int32_t p = __ldg(plist + i);
+      *pb = __ldg(g.off + p);
+      *len = (int)(__ldg(g.off + p + 1) - *pb);
     }
+  };
+  int64_t base = next_batch(), pb;
+  int len;
+  meta(base, &pb, &len);
+  while (base < i1) {
+    // the next batch's partners and list bounds load while this batch streams
+    const int64_t nbase = next_batch();
+    int64_t npb;
+    int nlen;
+    meta(nbase, &npb, &nlen);
     unsigned longm = __ballot_sync(0xffffffffu, len >= 32);
     while (longm) {
       const int k = __ffs(longm) - 1;
@@ -576,6 +587,9 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
       const bool v = t < total;
       cnt += pr.probe(v ? __ldg(g.cols + kp + (t - kx)) : 0, v);
     }
+    base = nbase;
+    pb = npb;
+    len = nlen;
   }
   cnt += pr.finish();
   return cnt;

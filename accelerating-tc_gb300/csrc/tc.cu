@@ -252,6 +252,134 @@ __global__ void fox_deal_kernel(const uint64_t* keys, const int64_t* list, int64
   }
 }
 
+// ============================== sorted-copy searches ===============================
+// TriCore-style and Fox-style counts on the Bisson-style grouping: every edge goes to its
+// endpoint h with the longer list and the partner's shorter list is streamed (sum of
+// min(d+u, d+v) searches).  N+(h), the longer list of every edge of an item, is staged once
+// per item as a sorted copy in shared memory, and every streamed element is searched in
+// it.  The reference kernels search the longer list in global memory, one dependent load
+// per step, per edge; here only lists too long for shared memory are searched there.
+//   KIND 0, TriCore-style (tricount_gpu.cu:215-290): 32 samples of the longer list (the
+//     reference's per-warp pivot cache) sit contiguous in shared memory, so the first five
+//     levels of every search touch 32 distinct banks; the sample bracket holding the
+//     element is then binary-searched.
+//   KIND 1, Fox-style (Fox/tc.cu:64-125): a lane's successive elements of a list ascend, so
+//     each search gallops forward from where the lane's previous one ended (restarting
+//     when the element is smaller than the previous one), then binary-searches the last
+//     step.
+template <int KIND>
+struct SortedProber {
+  const int32_t* T;    // sorted N+(h) (shared memory, or global for lists beyond it)
+  const int32_t* piv;  // 32 samples piv[i] = T[i * d / 32] (shared memory)
+  int d;
+  int prev;      // Fox: lower bound of the lane's previous element
+  int32_t last;  // Fox: the lane's previous element
+  __device__ __forceinline__ unsigned probe(int32_t x, bool valid) {
+    if (!valid) return 0u;
+    if constexpr (KIND == 0) {
+      int lo = 0, hi = 32;  // k = number of samples <= x
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (piv[mid] <= x) lo = mid + 1; else hi = mid;
+      }
+      if (lo == 0) return 0u;  // x < T[0]
+      if (piv[lo - 1] == x) return 1u;
+      int b = (int)(((int64_t)(lo - 1) * d) >> 5) + 1;  // strictly inside the bracket
+      int e = lo == 32 ? d : (int)(((int64_t)lo * d) >> 5);
+      while (b < e) {
+        const int mid = (b + e) >> 1;
+        if (T[mid] < x) b = mid + 1; else e = mid;
+      }
+      return b < d && T[b] == x;
+    } else {
+      if (x < last) prev = 0;
+      last = x;
+      int a = prev, b = prev, step = 1;  // every T[i], i < a, is < x
+      while (b < d && T[b] < x) {
+        a = b + 1;
+        b = a + step;
+        step <<= 1;
+      }
+      if (b > d) b = d;
+      while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (T[mid] < x) a = mid + 1; else b = mid;
+      }
+      prev = a;
+      return a < d && T[a] == x;
+    }
+  }
+  __device__ __forceinline__ unsigned finish() { return 0u; }
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kBgWarps * 32) sorted_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
+                                                                    const GroupItem* __restrict__ items, int nitems,
+                                                                    int* next, unsigned long long* out) {
+  __shared__ int32_t T[kBgWarps][kWarpMax];
+  __shared__ int32_t piv[kBgWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long total = 0;
+  for (;;) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(next, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const GroupItem gi = items[it];
+    const int64_t hb = g.off[gi.h];
+    const int dh = (int)(g.off[gi.h + 1] - hb);  // 1 .. kWarpMax
+    for (int j = lane; j < dh; j += 32) T[w][j] = __ldg(g.cols + hb + j);
+    __syncwarp();
+    piv[w][lane] = T[w][(lane * dh) >> 5];
+    __syncwarp();
+    int64_t cur = gi.b;
+    auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
+    SortedProber<KIND> pr{T[w], piv[w], dh, 0, INT32_MIN};
+    total += stream_partners(g, plist, gi.e, lane, nb, pr);
+    __syncwarp();  // the next item overwrites the copy
+  }
+  warp_add_count(total, out);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kBgWarps * 32) sorted_block_kernel(CsrView g, const int32_t* __restrict__ plist,
+                                                                     const GroupItem* __restrict__ items, int nitems,
+                                                                     int* next, uint32_t tab_words,
+                                                                     unsigned long long* out) {
+  extern __shared__ __align__(16) int32_t T[];  // tab_words
+  __shared__ int32_t piv[32];
+  __shared__ int cur_item;
+  __shared__ unsigned long long bnext;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long total = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      cur_item = atomicAdd(next, 1);
+      bnext = 0;
+    }
+    __syncthreads();
+    const int it = cur_item;
+    if (it >= nitems) break;
+    const GroupItem gi = items[it];
+    const int64_t hb = g.off[gi.h];
+    const int64_t dh = g.off[gi.h + 1] - hb;
+    const bool staged = dh <= (int64_t)tab_words;
+    if (staged)
+      for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) T[j] = __ldg(g.cols + hb + j);
+    if (threadIdx.x < 32) piv[threadIdx.x] = __ldg(g.cols + hb + (((int64_t)threadIdx.x * dh) >> 5));
+    __syncthreads();
+    auto nb = [&]() {
+      unsigned long long r = 0;
+      if (lane == 0) r = atomicAdd(&bnext, 32ull);
+      return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
+    };
+    SortedProber<KIND> pr{staged ? T : g.cols + hb, piv, (int)dh, 0, INT32_MIN};
+    total += stream_partners(g, plist, gi.e, lane, nb, pr);
+    __syncthreads();  // the next item overwrites the copy
+  }
+  warp_add_count(total, out);
+}
+
 }  // namespace
 
 // ---- family drivers ----------------------------------------------------------------
@@ -447,6 +575,47 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
   return launch_slots(slots, g, g.cols, witems.p, bitems.p, hc, counters.p, ctr, s, launches);
 }
 
+// The Bisson-style grouping of the edges of [e0, e1): every edge {u, v} at its endpoint h
+// with the longer list, the partners of each h contiguous in plist, cut into warp and block
+// items.  hc = {warp items, block items, -, longest hashed block list}.
+struct Grouping {
+  DevBuf<int32_t> cnt, cur, plist;
+  DevBuf<int64_t> gstart;
+  DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
+  DevBuf<GroupItem> witems, bitems;
+  int hc[4] = {0, 0, 0, 0};
+};
+
+static atc_status group_edges(const CsrView& g, const ItemShape& sh, Grouping* gr, cudaStream_t s, int* launches) {
+  ATC_TRY(gr->cnt.alloc(g.n + 1, s));
+  ATC_TRY(gr->cur.alloc(g.n, s));
+  ATC_TRY(gr->gstart.alloc(g.n + 1, s));
+  ATC_TRY(gr->counters.alloc(8, s));
+  ATC_CK(cudaMemsetAsync(gr->cnt.p, 0, sizeof(int32_t) * (g.n + 1), s));
+  ATC_CK(cudaMemsetAsync(gr->cur.p, 0, sizeof(int32_t) * g.n, s));
+  ATC_CK(cudaMemsetAsync(gr->counters.p, 0, sizeof(int) * 8, s));
+  group_count_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gr->cnt.p);
+  ATC_CK(cudaGetLastError());
+  ATC_TRY(exclusive_scan_i32_to_i64(gr->cnt.p, gr->gstart.p, g.n + 1, s));
+  int64_t total = 0;
+  ATC_CK(cudaMemcpyAsync(&total, gr->gstart.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  ATC_TRY(gr->plist.alloc(total + 32, s));
+  group_scatter_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gr->gstart.p, gr->cur.p, gr->plist.p);
+  ATC_CK(cudaGetLastError());
+  // items: at most one per group plus one per chunk boundary
+  int64_t max_items = g.n + total / std::min(sh.warp_chunk, sh.block_chunk) + 1;
+  ATC_TRY(gr->witems.alloc(max_items, s));
+  ATC_TRY(gr->bitems.alloc(max_items, s));
+  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gr->gstart.p, gr->witems.p, gr->bitems.p,
+                                                         gr->counters.p, sh, 0, INT64_MAX);
+  ATC_CK(cudaGetLastError());
+  ATC_CK(cudaMemcpyAsync(gr->hc, gr->counters.p, sizeof(gr->hc), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  *launches += 4;
+  return ATC_OK;
+}
+
 static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned long long* ctr, cudaStream_t s,
                              int* launches) {
   ItemShape sh;
@@ -454,40 +623,47 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
   ATC_TRY(item_shape(t, &sh, &slots));
   std::optional<Phase> ph;
   ph.emplace("tc.group", s);
-  DevBuf<int32_t> cnt, cur, plist;
-  DevBuf<int64_t> gstart;
-  DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
-  ATC_TRY(cnt.alloc(g.n + 1, s));
-  ATC_TRY(cur.alloc(g.n, s));
-  ATC_TRY(gstart.alloc(g.n + 1, s));
-  ATC_TRY(counters.alloc(8, s));
-  ATC_CK(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (g.n + 1), s));
-  ATC_CK(cudaMemsetAsync(cur.p, 0, sizeof(int32_t) * g.n, s));
-  ATC_CK(cudaMemsetAsync(counters.p, 0, sizeof(int) * 8, s));
-  group_count_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, cnt.p);
-  ATC_CK(cudaGetLastError());
-  ATC_TRY(exclusive_scan_i32_to_i64(cnt.p, gstart.p, g.n + 1, s));
-  int64_t total = 0;
-  ATC_CK(cudaMemcpyAsync(&total, gstart.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  ATC_CK(cudaStreamSynchronize(s));
-  ATC_TRY(plist.alloc(total + 32, s));
-  group_scatter_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gstart.p, cur.p, plist.p);
-  ATC_CK(cudaGetLastError());
-  // items: at most one per group plus one per chunk boundary
-  int64_t max_items = g.n + total / std::min(sh.warp_chunk, sh.block_chunk) + 1;
-  DevBuf<GroupItem> witems, bitems;
-  ATC_TRY(witems.alloc(max_items, s));
-  ATC_TRY(bitems.alloc(max_items, s));
-  group_items_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gstart.p, witems.p, bitems.p, counters.p, sh, 0,
-                                                         INT64_MAX);
-  ATC_CK(cudaGetLastError());
-  int hc[4];
-  ATC_CK(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
-  ATC_CK(cudaStreamSynchronize(s));
-  *launches += 4;
+  Grouping gr;
+  ATC_TRY(group_edges(g, sh, &gr, s, launches));
   ph.reset();
   ph.emplace("tc.count", s);
-  return launch_slots(slots, g, plist.p, witems.p, bitems.p, hc, counters.p, ctr, s, launches);
+  return launch_slots(slots, g, gr.plist.p, gr.witems.p, gr.bitems.p, gr.hc, gr.counters.p, ctr, s, launches);
+}
+
+// TriCore-style (KIND 0) and Fox-style (KIND 1) searches of the staged longer lists.
+// max_outdeg sizes the block kernels' shared copy (lists above kTabWords stay in global).
+template <int KIND>
+static atc_status run_sorted(const CsrView& g, int max_outdeg, unsigned long long* ctr, cudaStream_t s,
+                             int* launches) {
+  ItemShape sh = default_shape(kWarpMax);
+  std::optional<Phase> ph;
+  ph.emplace("tc.group", s);
+  Grouping gr;
+  ATC_TRY(group_edges(g, sh, &gr, s, launches));
+  ph.reset();
+  ph.emplace("tc.count", s);
+  if (gr.hc[1]) {
+    uint32_t words = (uint32_t)std::min(std::max(max_outdeg, kWarpMax + 1), kTabWords);
+    words = (words + 31) & ~31u;
+    const size_t smem = sizeof(int32_t) * words;
+    ATC_CK(cudaFuncSetAttribute((const void*)sorted_block_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    const int bps = blocks_per_sm((const void*)sorted_block_kernel<KIND>, kBgWarps * 32, smem);
+    const int grid = std::min(gr.hc[1], sm_count() * bps);
+    sorted_block_kernel<KIND><<<grid, kBgWarps * 32, smem, s>>>(g, gr.plist.p, gr.bitems.p, gr.hc[1],
+                                                                 gr.counters.p + 5, words, ctr);
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  if (gr.hc[0]) {
+    const int bps = blocks_per_sm((const void*)sorted_warp_kernel<KIND>, kBgWarps * 32, 0);
+    const int grid = (int)std::min<int64_t>((gr.hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
+    sorted_warp_kernel<KIND><<<grid, kBgWarps * 32, 0, s>>>(g, gr.plist.p, gr.witems.p, gr.hc[0],
+                                                            gr.counters.p + 4, ctr);
+    ATC_CK(cudaGetLastError());
+    *launches += 1;
+  }
+  return ATC_OK;
 }
 
 // ---- counting without device allocation ------------------------------------------
@@ -703,8 +879,14 @@ static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tun
     switch (kernel) {
       case ATC_KERNEL_HU: ATC_TRY(run_hu(g, tuning, ctr, s, &launches)); break;
       case ATC_KERNEL_BISSON: ATC_TRY(run_bisson(g, tuning, ctr, s, &launches)); break;
-      case ATC_KERNEL_FOX: ATC_TRY(run_fox(g, tuning, ctr, s, &launches)); break;
-      default: ATC_TRY(run_tricore(g, tuning, ctr, s, &launches)); break;
+      case ATC_KERNEL_FOX:
+        if (tuning && tuning->edge_kernels) ATC_TRY(run_fox(g, tuning, ctr, s, &launches));
+        else ATC_TRY(run_sorted<1>(g, csr->max_outdeg, ctr, s, &launches));
+        break;
+      default:
+        if (tuning && tuning->edge_kernels) ATC_TRY(run_tricore(g, tuning, ctr, s, &launches));
+        else ATC_TRY(run_sorted<0>(g, csr->max_outdeg, ctr, s, &launches));
+        break;
     }
     tm.stop(s);
     unsigned long long h = 0;

@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernels", default="hu,bisson,fox,tricore", help="families timed besides the headline")
+    ap.add_argument("--kernels", default="hu,bisson,fox,tricore,fox_edge,tricore_edge",
+                    help="families timed besides the headline (suffix _edge: the per-edge global-search kernels)")
     ap.add_argument("--mode", default="tc", choices=["tc", "kcl", "batch", "select"],
                     help="tc: the headline (R-MAT scale 24, every kernel family); kcl: k-clique counts; "
                          "batch: many Chung-Lu graphs, batched vs per-graph loop; select: the learned selector")
@@ -312,14 +313,18 @@ def run_ours(a):
     # ---- every kernel family once (count check + per-kernel time)
     kernels = {}
     counts = {}
-    wanted = [atc.Kernel[x.strip().upper()] for x in a.kernels.split(",") if x.strip()]
-    for k in wanted:
-        atc.tc(csr, k, stream=sp)
-        c, st = atc.tc(csr, k, stream=sp)
-        counts[k.name] = c
-        kernels[k.name.lower()] = {"ms": st.kernel_ms, "edges_per_s": m / (st.kernel_ms * 1e-3) if st.kernel_ms else None,
-                                   "hbm_frac_alg": st.alg_bytes / (st.kernel_ms * 1e-3) / 1e9 / measured_peak()[0]
-                                   if st.kernel_ms else None}
+    wanted = [x.strip().lower() for x in a.kernels.split(",") if x.strip()]
+    for name in wanted:
+        k = atc.Kernel[name.split("_")[0].upper()]
+        tun = {"edge_kernels": 1} if name.endswith("_edge") else None
+        atc.tc(csr, k, tuning=tun, stream=sp)
+        c, st = atc.tc(csr, k, tuning=tun, stream=sp)
+        counts[name] = c
+        kernels[name] = {"ms": st.kernel_ms, "edges_per_s": m / (st.kernel_ms * 1e-3) if st.kernel_ms else None,
+                         "hbm_frac_alg": st.alg_bytes / (st.kernel_ms * 1e-3) / 1e9 / measured_peak()[0]
+                         if st.kernel_ms else None,
+                         "hbm_frac_min": st.alg_bytes_min / (st.kernel_ms * 1e-3) / 1e9 / measured_peak()[0]
+                         if st.kernel_ms else None}
     assert len(set(counts.values())) <= 1, counts
     best = min(kernels, key=lambda k: kernels[k]["ms"]) if kernels else None
 

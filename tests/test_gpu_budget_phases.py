@@ -23,6 +23,18 @@ def _init(gpu_ready):
     atc.phase_timing(False)
 
 
+SMALL = None
+
+
+def _small():
+    """A small graph on which A-order is defined, and its count."""
+    global SMALL
+    if SMALL is None:
+        g = atc.rmat_graph(9, 8, 5)
+        SMALL = (g, oracle.tc_count(g))
+    return SMALL
+
+
 def _pipeline(g, kernel):
     csr = atc.pretc(g, atc.Dir.ADIRECTION, atc.Order.AORDER)
     try:
@@ -49,7 +61,8 @@ def test_budget_oom_anywhere_then_exact(kernel):
         finally:
             atc.set_alloc_budget(None)
         # the failed call left the library usable: a small count right after it is exact
-        assert _pipeline(np.array([[0, 1], [1, 2], [2, 0], [0, 3], [3, 1]], dtype=np.int32), kernel) == 2
+        sg, sc = _small()
+        assert _pipeline(sg, kernel) == sc
         budget = budget * 3 // 2
         assert budget < 1 << 34
     assert failed >= 5  # the budget ran out at several different allocations
