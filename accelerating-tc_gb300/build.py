@@ -119,11 +119,19 @@ def build_cli(force=False):
               "-L", PKG, "-latc", "-Wl,-rpath,$ORIGIN/.."])
 
 
+STAGED_REF = os.path.join(ROOT, "baseline", "_ref", "src")
+
+
 def build_oracle():
-    """The oracle library, and the reference's CPU programs where the reference tree
-    exists (oracle/Makefile's REF, or ATC_REFERENCE_TREE when set)."""
+    """The oracle library, and the reference's CPU programs: from the reference tree where it
+    exists (oracle/Makefile's REF, or ATC_REFERENCE_TREE when set), else from the sources
+    staged into baseline/_ref/src by `make -C oracle stage`."""
     _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"])
     ref = os.environ.get("ATC_REFERENCE_TREE")
+    if not ref and os.path.isdir(STAGED_REF):
+        default = _run(["make", "-s", "--no-print-directory", "-C", os.path.join(ROOT, "oracle"), "print-ref"]).strip()
+        if not os.path.isdir(default):
+            ref = STAGED_REF
     _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref-if-present"] + (["REF=" + ref] if ref else []))
 
 

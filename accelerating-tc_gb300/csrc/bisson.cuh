@@ -453,6 +453,7 @@ struct HashQueueProber {
   uint32_t* qs;  // 64 (next slot | steps << 16)
   int n;         // queued entries, the same on every lane
   int lane;
+  int32_t lo, hi;  // smallest and largest key: elements outside skip the table
   __device__ __forceinline__ void push(bool pend, int32_t x, uint32_t next) {
     const unsigned pm = __ballot_sync(0xffffffffu, pend);
     if (pm) {
@@ -494,7 +495,7 @@ struct HashQueueProber {
     unsigned hit = 0;
     bool pend = false;
     uint32_t s = 0;
-    if (valid) {
+    if (valid && x >= lo && x <= hi) {
       s = hash_home<S>(x, mask);
       bool stop;
       hit = bucket_has<S>(tab, s, x, &stop);
@@ -518,32 +519,21 @@ struct HashQueueProber {
 // time, four coalesced loads in flight per lane.  Shorter lists are laid end to end by
 // a warp prefix sum of their lengths and dealt 32 elements per round; each lane finds
 // the list holding its element by a 5-step binary search over the lanes' start offsets,
-// done with shuffles so that every lane runs the same steps.  The next batch's partners and
-// list bounds (three dependent loads) are loaded while the current batch streams.  Every
-// probe call is made by all 32 lanes together.
+// done with shuffles so that every lane runs the same steps.  Every probe call is made
+// by all 32 lanes together.
 template <class NextBatch, class Prober>
 __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int32_t* __restrict__ plist, int64_t i1,
                                                     int lane, NextBatch next_batch, Prober& pr) {
   unsigned cnt = 0;
-  auto meta = [&](int64_t base, int64_t* pb, int* len) {
-    const int64_t i = base + lane;
-    *pb = 0;
-    *len = 0;
+  for (int64_t base = next_batch(); base < i1; base = next_batch()) {
+    int64_t i = base + lane;
+    int len = 0;
+    int64_t pb = 0;
     if (i < i1) {
-      const int32_t p = __ldg(plist + i);
-      *pb = __ldg(g.off + p);
-      *len = (int)(__ldg(g.off + p + 1) - *pb);
+      int32_t p = __ldg(plist + i);
+      pb = __ldg(g.off + p);
+      len = (int)(__ldg(g.off + p + 1) - pb);
     }
-  };
-  int64_t base = next_batch(), pb;
-  int len;
-  meta(base, &pb, &len);
-  while (base < i1) {
-    // the next batch's partners and list bounds load while this batch streams
-    const int64_t nbase = next_batch();
-    int64_t npb;
-    int nlen;
-    meta(nbase, &npb, &nlen);
     unsigned longm = __ballot_sync(0xffffffffu, len >= 32);
     while (longm) {
       const int k = __ffs(longm) - 1;
@@ -587,9 +577,6 @@ __device__ __forceinline__ unsigned stream_partners(const CsrView& g, const int3
       const bool v = t < total;
       cnt += pr.probe(v ? __ldg(g.cols + kp + (t - kx)) : 0, v);
     }
-    base = nbase;
-    pb = npb;
-    len = nlen;
   }
   cnt += pr.finish();
   return cnt;
@@ -650,7 +637,7 @@ __global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_warp_
       const uint32_t mask = cap - 1;
       for (int j = lane; j < dh; j += 32) hash_insert<S>(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();
-      HashQueueProber<S> pr{T, mask, qx[w], qs[w], 0, lane};
+      HashQueueProber<S> pr{T, mask, qx[w], qs[w], 0, lane, __ldg(g.cols + hb), __ldg(g.cols + hb + dh - 1)};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncwarp();
       for (int j = lane; j < dh; j += 32) hash_erase<S>(T, mask, __ldg(g.cols + hb + j));
@@ -704,7 +691,7 @@ __global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_block
       const uint32_t mask = cap - 1;
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert<S>(tab, mask, Nh[j]);
       __syncthreads();
-      HashQueueProber<S> pr{tab, mask, qx[w], qs[w], 0, lane};
+      HashQueueProber<S> pr{tab, mask, qx[w], qs[w], 0, lane, Nh[0], Nh[dh - 1]};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncthreads();
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase<S>(tab, mask, Nh[j]);

@@ -93,12 +93,16 @@ struct OrientArgs {
   int bout;             // B of the output keys
 };
 
-// Orientation rules (each decides src for the edge {x, y} given on new ids xn, yn):
+// Orientation rules (each decides src for the edge {x, y}; input ids x, y, new ids xn, yn):
 //   ID            src = larger id                       Bisson/preTC.cu:135-144, Fox/preTC.cu:94-98
 //   DEGREE        lower degree; tie -> larger id        Hu/preTC.cu:125-133, A-order.cpp:91-96
 //   DEGREE_LOWID  lower degree; tie -> smaller id       tricount_gpu.cu:76-78
 //   ADIRECTION    lower priority; tie -> smaller id     A-direction-seri.cpp:259-261
 //   KCORE         lower core number; tie -> smaller id  kcore_direction.cpp:137-143
+// The first three are the counting programs' own rules, applied to the ids they read (the
+// relabelled ones, xn/yn).  The direction programs (ADIRECTION, KCORE, ADIRECTION_PAR) orient
+// their input before any relabelling, so their ties use the input ids x/y: the relabelled
+// graph is then exactly the program's output file relabelled by the ordering.
 __global__ void orient_kernel(const uint64_t* ek, int64_t m, OrientArgs a, uint64_t* out,
                               unsigned long long* dropped) {
   uint64_t mask = (1ull << a.bin) - 1;
@@ -121,18 +125,18 @@ __global__ void orient_kernel(const uint64_t* ek, int64_t m, OrientArgs a, uint6
       case ATC_DIR_DEGREE_LOWID: x_src = dx < dy || (dx == dy && xn < yn); break;
       case ATC_DIR_KCORE: {
         int32_t cx = a.prio[x], cy = a.prio[y];
-        x_src = cx < cy || (cx == cy && xn < yn);
+        x_src = cx < cy || (cx == cy && x < y);
         break;
       }
       case ATC_DIR_ADIRECTION_PAR: {  // flags compare as int32 (0xFFFFFFFF = -1)
         int32_t fx = a.prio[x], fy = a.prio[y];
         int32_t mx = (int32_t)a.minor[x], my = (int32_t)a.minor[y];
-        x_src = fx < fy || (fx == fy && (mx < my || (mx == my && xn < yn)));
+        x_src = fx < fy || (fx == fy && (mx < my || (mx == my && x < y)));
         break;
       }
       default: {
         int32_t px = a.prio[x], py = a.prio[y];
-        x_src = py > px || (py == px && xn < yn);
+        x_src = py > px || (py == px && x < y);
       }
     }
     int32_t s = x_src ? xn : yn, d = x_src ? yn : xn;
@@ -501,8 +505,11 @@ extern "C" atc_status atc_pretc(const int32_t* pairs, uint64_t np, atc_dir dir, 
   Phase ph("pretc", st);
   DevBuf<int2> d;
   {
-    Phase ph_copy("pretc.h2d", st);
+    Phase ph_alloc("pretc.alloc", st);
     ATC_TRY(d.alloc(np, st));
+  }
+  {
+    Phase ph_copy("pretc.h2d", st);
     if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
   }
   return pretc_impl(d.p, np, dir, order, t, out, perm_out, st);

@@ -272,39 +272,56 @@ struct SortedProber {
   const int32_t* T;    // sorted N+(h) (shared memory, or global for lists beyond it)
   const int32_t* piv;  // 32 samples piv[i] = T[i * d / 32] (shared memory)
   int d;
+  int32_t hi;    // T[d - 1]
   int prev;      // Fox: lower bound of the lane's previous element
   int32_t last;  // Fox: the lane's previous element
+  int gap;       // Fox: how far the lane's previous forward search moved
   __device__ __forceinline__ unsigned probe(int32_t x, bool valid) {
     if (!valid) return 0u;
+    if (x > hi) return 0u;  // above the longer list: no search
     if constexpr (KIND == 0) {
-      int lo = 0, hi = 32;  // k = number of samples <= x
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (piv[mid] <= x) lo = mid + 1; else hi = mid;
-      }
-      if (lo == 0) return 0u;  // x < T[0]
-      if (piv[lo - 1] == x) return 1u;
-      int b = (int)(((int64_t)(lo - 1) * d) >> 5) + 1;  // strictly inside the bracket
-      int e = lo == 32 ? d : (int)(((int64_t)lo * d) >> 5);
+      int k = 0;  // number of samples <= x: five fixed steps, then the last sample
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (piv[k + step - 1] <= x) k += step;
+      if (piv[k] <= x) ++k;
+      if (k == 0) return 0u;  // x < T[0]
+      if (piv[k - 1] == x) return 1u;
+      int b = (int)(((int64_t)(k - 1) * d) >> 5) + 1;  // strictly inside the bracket
+      int e = k == 32 ? d : (int)(((int64_t)k * d) >> 5);
       while (b < e) {
         const int mid = (b + e) >> 1;
         if (T[mid] < x) b = mid + 1; else e = mid;
       }
       return b < d && T[b] == x;
     } else {
-      if (x < last) prev = 0;
+      if (x < last) {
+        // a new list (or an earlier element): its lower bound lies in [0, prev]
+        int a = 0, b = prev;
+        while (a < b) {
+          const int mid = (a + b) >> 1;
+          if (T[mid] < x) a = mid + 1; else b = mid;
+        }
+        prev = a;
+        last = x;
+        return a < d && T[a] == x;
+      }
       last = x;
-      int a = prev, b = prev, step = 1;  // every T[i], i < a, is < x
+      // every T[i], i < a, is < x; the first step is half the lane's previous move, so a
+      // lane walking one list at a steady stride settles in about log2(stride) steps
+      int a = prev, step = gap > 1 ? gap >> 1 : 1;
+      int b = a + step - 1;
       while (b < d && T[b] < x) {
         a = b + 1;
-        b = a + step;
         step <<= 1;
+        b = a + step - 1;
       }
       if (b > d) b = d;
-      while (a < b) {
+      while (a < b) {  // T[b] >= x, or b == d
         const int mid = (a + b) >> 1;
         if (T[mid] < x) a = mid + 1; else b = mid;
       }
+      gap = a - prev;
       prev = a;
       return a < d && T[a] == x;
     }
@@ -334,7 +351,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_warp_kernel(CsrView g, c
     __syncwarp();
     int64_t cur = gi.b;
     auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
-    SortedProber<KIND> pr{T[w], piv[w], dh, 0, INT32_MIN};
+    SortedProber<KIND> pr{T[w], piv[w], dh, T[w][dh - 1], 0, INT32_MIN, 16};
     total += stream_partners(g, plist, gi.e, lane, nb, pr);
     __syncwarp();  // the next item overwrites the copy
   }
@@ -373,7 +390,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_block_kernel(CsrView g, 
       if (lane == 0) r = atomicAdd(&bnext, 32ull);
       return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
     };
-    SortedProber<KIND> pr{staged ? T : g.cols + hb, piv, (int)dh, 0, INT32_MIN};
+    SortedProber<KIND> pr{staged ? T : g.cols + hb, piv, (int)dh, __ldg(g.cols + hb + dh - 1), 0, INT32_MIN, 16};
     total += stream_partners(g, plist, gi.e, lane, nb, pr);
     __syncthreads();  // the next item overwrites the copy
   }

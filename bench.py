@@ -76,6 +76,8 @@ def parse():
                     help="tc mode: graphs of the reduced batch leg (every (4096 / N)-th graph of the 4096-graph "
                          "batch; 0 = no batch leg)")
     ap.add_argument("--no-select-leg", action="store_true", help="tc mode: skip the selector leg")
+    ap.add_argument("--prep-scale", type=int, default=20,
+                    help="R-MAT scale of the reference preprocessing programs' timed run (0 = skip)")
     return ap.parse_args()
 
 
@@ -218,6 +220,48 @@ def cpu_baseline(g_lower_off, g_lower_cols, m_total, target_s):
             "sample": "every %d-th vertex u (%d of %d) with all its smaller-neighbour edges (%d of %d edges); %.1f s"
             % (stride, (n + stride - 1) // stride, n, e, m_total, dt),
             "machine": os.uname().machine}
+
+
+def reference_preprocessing(scale, edge_factor, seed, sp):
+    """The reference's own preprocessing programs, A-direction-seri, A-order and costFuncCal
+    (compiled from their sources into oracle/_ref; single-threaded, as written), run one after
+    another on seeded R-MAT raw pairs of the given scale, each timed by the host wall clock,
+    next to libatc's preTC (A-direction + A-order) of the same pairs from host memory."""
+    import tempfile
+    import atc
+    import oracle
+    ref = os.path.join(ROOT, "oracle", "_ref")
+    progs = ("A-direction-seri", "A-order", "costFuncCal")
+    if not all(os.path.exists(os.path.join(ref, p)) for p in progs):
+        return {"unavailable": "reference programs not built (no reference sources here)"}
+    raw = oracle.gen_rmat(scale, edge_factor, seed)
+    out = {"graph": "R-MAT scale %d edge factor %d seed %d, %d raw pairs" % (scale, edge_factor, seed, raw.shape[0]),
+           "threads": 1, "machine": os.uname().machine, "nproc": os.cpu_count()}
+    with tempfile.TemporaryDirectory() as d:
+        e = os.path.join(d, "E.bin")
+        raw.tofile(e)
+        lp = os.path.join(d, "lpBasedGraph.bin")
+        for name, args in (("A-direction-seri", [e]), ("A-order", [lp]), ("costFuncCal", [lp, "1"])):
+            t0 = time.perf_counter()
+            r = subprocess.run([os.path.join(ref, name)] + args, cwd=d, stdout=subprocess.DEVNULL,
+                               stderr=subprocess.DEVNULL, timeout=1200)
+            out[name + "_s"] = time.perf_counter() - t0
+            if r.returncode != 0:
+                out[name + "_s"] = None
+        m = os.path.getsize(lp) // 8 if os.path.exists(lp) else 0
+    host = np.ascontiguousarray(raw)
+    atc.pretc(host, atc.Dir.ADIRECTION, atc.Order.AORDER, stream=sp).free()  # warm
+    t0 = time.perf_counter()
+    c = atc.pretc(host, atc.Dir.ADIRECTION, atc.Order.AORDER, stream=sp)
+    gpu_s = time.perf_counter() - t0
+    out["edges"] = m
+    out["libatc_pretc_s"] = gpu_s
+    ref_s = sum(out[p + "_s"] or 0 for p in progs)
+    out["reference_s"] = ref_s
+    out["reference_edges_per_s"] = m / ref_s if ref_s else None
+    out["libatc_edges_per_s"] = c.m / gpu_s if gpu_s else None
+    c.free()
+    return out
 
 
 # ---------------------------------------------------------------------------------------
@@ -429,6 +473,8 @@ def run_ours(a):
         import oracle
         off, cols = oracle.lower_csr(host_raw.numpy())
         line["cpu_baseline"] = cpu_baseline(off, cols, m, a.cpu_seconds)
+        if a.prep_scale > 0:
+            line["cpu_baseline"]["preprocessing"] = reference_preprocessing(a.prep_scale, a.edge_factor, a.seed, sp)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

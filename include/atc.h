@@ -228,8 +228,11 @@ atc_status atc_simplify_host(const int32_t* pairs, uint64_t n_pairs, int symmetr
    (Hu/preTC.cu:64, Bisson/preTC.cu:77, Fox/preTC.cu:64) and TriCore's cal_degree /
    redirect_edges / split (tricore/include/tricount.h:9-15).  Self-loops and repeated
    pairs are dropped; degrees are those of the resulting simple graph.  With
-   ATC_ORDER_AORDER the vertices are first relabelled by A-order computed on the
-   simple graph, then oriented by `dir` on the new ids; `perm_out` (nullable, n_input
+   ATC_ORDER_AORDER the vertices are relabelled by A-order computed on the simple
+   graph; the counting programs' rules (ATC_DIR_ID, DEGREE, DEGREE_LOWID) then orient on
+   the new ids, while the direction programs' orientations (ADIRECTION, KCORE,
+   ADIRECTION_PAR) are decided on the input ids and relabelled, as when A-order reads
+   their output file; `perm_out` (nullable, n_input
    ints) receives the new id of every input id.  Returns ATC_ERR_UNSUPPORTED when
    A-order is asked for on a graph where the reference A-order indexes outside its
    arrays (see atc_aorder). */

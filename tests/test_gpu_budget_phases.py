@@ -82,7 +82,7 @@ def test_phase_times_nest_and_add_up():
         atc.phase_timing(False)
     assert c == oracle.tc_count(g)
     names = [(d, n) for n, d, _ in ph]
-    for want in [(0, "pretc"), (1, "pretc.h2d"), (1, "pretc.dedup"), (1, "pretc.degrees"), (1, "pretc.order+peel"),
+    for want in [(0, "pretc"), (1, "pretc.alloc"), (1, "pretc.h2d"), (1, "pretc.dedup"), (1, "pretc.degrees"), (1, "pretc.order+peel"),
                  (1, "pretc.orient+sort"), (1, "pretc.csr"), (0, "tc"), (1, "tc.group"), (1, "tc.count"),
                  (1, "tc.readback")]:
         assert want in names, (want, names)

@@ -247,6 +247,20 @@ def test_adirection_csr_is_reference_orientation():
     assert np.array_equal(lp, oracle.adirection(g))
 
 
+@pytest.mark.parametrize("order", [atc.Order.AORDER, atc.Order.DEGREE_DESC, atc.Order.GRO])
+def test_direction_programs_orient_before_relabelling(order):
+    # the pipeline's CSR is the direction program's output relabelled by the ordering
+    g = atc.rmat_graph(12, 16, 7)
+    csr = atc.pretc(g, atc.Dir.ADIRECTION, order, want_perm=True)
+    off, cols = csr.to_host()
+    src = np.repeat(np.arange(off.size - 1), np.diff(off)).astype(np.int32)
+    got = np.stack([src, cols], 1)
+    lp = oracle.adirection(g)
+    rel = csr.perm[lp]
+    want = rel[np.lexsort((rel[:, 1], rel[:, 0]))]
+    assert np.array_equal(got, want)
+
+
 def test_aorder_perm_in_pipeline_matches_reference_program():
     # pipeline A-order = the A-order program run on A-direction-seri's output
     g = atc.rmat_graph(12, 16, 7)
