@@ -453,7 +453,6 @@ struct HashQueueProber {
   uint32_t* qs;  // 64 (next slot | steps << 16)
   int n;         // queued entries, the same on every lane
   int lane;
-  int32_t lo, hi;  // smallest and largest key: elements outside skip the table
   __device__ __forceinline__ void push(bool pend, int32_t x, uint32_t next) {
     const unsigned pm = __ballot_sync(0xffffffffu, pend);
     if (pm) {
@@ -495,7 +494,7 @@ struct HashQueueProber {
     unsigned hit = 0;
     bool pend = false;
     uint32_t s = 0;
-    if (valid && x >= lo && x <= hi) {
+    if (valid) {
       s = hash_home<S>(x, mask);
       bool stop;
       hit = bucket_has<S>(tab, s, x, &stop);
@@ -637,7 +636,7 @@ __global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_warp_
       const uint32_t mask = cap - 1;
       for (int j = lane; j < dh; j += 32) hash_insert<S>(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();
-      HashQueueProber<S> pr{T, mask, qx[w], qs[w], 0, lane, __ldg(g.cols + hb), __ldg(g.cols + hb + dh - 1)};
+      HashQueueProber<S> pr{T, mask, qx[w], qs[w], 0, lane};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncwarp();
       for (int j = lane; j < dh; j += 32) hash_erase<S>(T, mask, __ldg(g.cols + hb + j));
@@ -691,7 +690,7 @@ __global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_block
       const uint32_t mask = cap - 1;
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_insert<S>(tab, mask, Nh[j]);
       __syncthreads();
-      HashQueueProber<S> pr{tab, mask, qx[w], qs[w], 0, lane, Nh[0], Nh[dh - 1]};
+      HashQueueProber<S> pr{tab, mask, qx[w], qs[w], 0, lane};
       cnt = stream_partners(g, plist, gi.e, lane, nb, pr);
       __syncthreads();
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) hash_erase<S>(tab, mask, Nh[j]);
