@@ -593,6 +593,7 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
     batch.reserve(tot_n, tot_m, stream=sp)
     kfixed = [atc.Kernel[x.strip().upper()] for x in plain_kernels]
     plain_ms = [[] for _ in kfixed]
+    plain_dev = [[] for _ in kfixed]  # device time of the counting kernels of each call
     plain_counts = []
     dirs = []
     wmin_adir = wmin_sel = 0
@@ -609,8 +610,9 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
             flush.fill_(j)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            c, _ = atc.tc(csr, kf, stream=sp)
+            c, st = atc.tc(csr, kf, stream=sp)
             plain_ms[j].append((time.perf_counter() - t0) * 1e3)
+            plain_dev[j].append(st.kernel_ms)
             if j == 0:
                 plain_counts.append(c)
             else:
@@ -652,7 +654,9 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
             str(indices), 4096),
         "graphs": ng, "vertices": n_all, "edges": m_all, "triangles": int(sum(plain_counts)),
         "plain": {kf.name.lower(): {"ms_total": sum(ms), "graphs_per_s": ng / (sum(ms) * 1e-3),
-                                    "edges_per_s": m_all / (sum(ms) * 1e-3)} for kf, ms in zip(kfixed, plain_ms)},
+                                    "edges_per_s": m_all / (sum(ms) * 1e-3), "device_ms_total": sum(dv)}
+                  for kf, ms, dv in zip(kfixed, plain_ms, plain_dev)},
+        "plain_device_best_of_kernels_ms": float(sum(min(x) for x in zip(*plain_dev))) if plain_dev else None,
         "plain_note": "atc_tc per graph on its resident A-direction CSR, host-synchronised per call, L2 flushed "
                       "(256 MB written) before each timed call",
         "batched": {"ms_per_replay": batch_ms, "graphs_per_s": ng / (batch_ms * 1e-3),
