@@ -23,8 +23,10 @@ struct atc_batch {
   int64_t* off = nullptr;      // vcap + 1
   int32_t* cols = nullptr;     // ecap + 16
   std::vector<int64_t> vbase{0};
+  std::vector<int64_t> gm, gw, gwmin;  // per graph: edges, W, sum of min(d+u, d+v)
   int32_t max_outdeg = 0;
   bool dirty = true;
+  int rows_graphs = 0;  // graphs of the last built pipeline counted by rows
   atc::ItemShape shape = atc::default_shape(32);
   // counting pipeline, sized for the union when built
   int32_t* cnt = nullptr;
@@ -33,6 +35,9 @@ struct atc_batch {
   int32_t* plist = nullptr;
   int2* items = nullptr;
   int* counters = nullptr;
+  int2* items_r = nullptr;   // mode 2: the rows items of the graphs counted by rows
+  int* counters_r = nullptr;
+  uint8_t* vrows = nullptr;  // mode 2: 1 for the vertices of graphs counted by rows
   int64_t* vbase_d = nullptr;
   unsigned long long* gcounts = nullptr;
   void* scan_tmp = nullptr;
@@ -61,13 +66,17 @@ void free_pipeline(atc_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   b->exec = nullptr;
   b->graph = nullptr;
-  void* bufs[] = {b->cnt, b->cur, b->gstart, b->plist, b->items, b->counters, b->vbase_d, b->gcounts, b->scan_tmp};
+  void* bufs[] = {b->cnt, b->cur, b->gstart, b->plist, b->items, b->counters, b->vbase_d, b->gcounts, b->scan_tmp,
+                  b->items_r, b->counters_r, b->vrows};
   for (void* p : bufs)
     if (p) cudaFree(p);
   b->cnt = b->cur = b->plist = nullptr;
   b->gstart = b->vbase_d = nullptr;
   b->items = nullptr;
   b->counters = nullptr;
+  b->items_r = nullptr;
+  b->counters_r = nullptr;
+  b->vrows = nullptr;
   b->gcounts = nullptr;
   b->scan_tmp = nullptr;
   b->built_n = b->built_m = -1;
@@ -149,6 +158,9 @@ extern "C" atc_status atc_batch_add(atc_batch* b, const atc_csr* csr, int32_t* i
   b->n += csr->n;
   b->m += csr->m;
   b->vbase.push_back(b->n);
+  b->gm.push_back(csr->m);
+  b->gw.push_back(csr->wedges);
+  b->gwmin.push_back(csr->wedges_min);
   b->max_outdeg = std::max(b->max_outdeg, csr->max_outdeg);
   b->dirty = true;
   return ATC_OK;
@@ -187,7 +199,7 @@ ItemShape shape_from(const atc_tuning* t, const ItemShape& base) {
   if (t->bisson_warp_max > 0) sh.warp_max = std::min(t->bisson_warp_max, kWarpMax);
   if (t->bisson_warp_chunk > 0) sh.warp_chunk = t->bisson_warp_chunk;
   if (t->bisson_block_chunk > 0) sh.block_chunk = t->bisson_block_chunk;
-  if (t->group_by_source > 0) sh.by_source = 1;
+  if (t->group_by_source > 0) sh.by_source = t->group_by_source >= 2 ? 2 : 1;
   if (sh.cutover > sh.warp_max) sh.cutover = sh.warp_max;
   return sh;
 }
@@ -206,6 +218,9 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
     ATC_TRY(dev_alloc(&b->plist, (size_t)m + 32));
     ATC_TRY(dev_alloc(&b->items, (size_t)cap_items));
     ATC_TRY(dev_alloc(&b->counters, 8));
+    ATC_TRY(dev_alloc(&b->items_r, (size_t)cap_items));
+    ATC_TRY(dev_alloc(&b->counters_r, 8));
+    ATC_TRY(dev_alloc(&b->vrows, (size_t)n + 1));
     ATC_TRY(dev_alloc(&b->vbase_d, (size_t)ng + 1));
     ATC_TRY(dev_alloc(&b->gcounts, (size_t)ng));
     size_t bytes = 0;
@@ -240,10 +255,35 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   GraphTags tags{b->vbase_d, ng, b->gcounts};
   // grouped at the source, a vertex's partners are its own row: the items index the CSR
   // itself and the grouping passes are skipped
-  const int64_t* gstart = sh.by_source ? b->off : b->gstart;
-  const int32_t* plist = sh.by_source ? b->cols : b->plist;
+  const int64_t* gstart = sh.by_source == 1 ? b->off : b->gstart;
+  const int32_t* plist = sh.by_source == 1 ? b->cols : b->plist;
   CompactItems witems{b->items, gstart, cap_items, false, sh};
   CompactItems bitems{b->items, gstart, cap_items, true, sh};
+  // mode 2: each graph counts by rows (every wedge tested at its source, W tests, no grouping)
+  // or grouped at the longer endpoint (sum of min(d+u, d+v) tests plus the grouping passes),
+  // whichever the per-graph cost model of the two kernels predicts faster (the per-call terms
+  // of the single-graph model do not apply inside one replay)
+  const bool mixed = sh.by_source == 2;
+  ItemShape shr = sh;
+  shr.by_source = 1;
+  shr.cutover = std::min(sh.cutover, 8);  // the rows items' sorted copy, as the single-graph Hu count
+  CompactItems witems_r{b->items_r, b->off, cap_items, false, shr};
+  CompactItems bitems_r{b->items_r, b->off, cap_items, true, shr};
+  int nrows = 0;
+  if (mixed) {
+    ATC_CK(cudaMemsetAsync(b->vrows, 0, (size_t)n + 1, s));
+    for (int q = 0; q < ng; ++q) {
+      const double m_q = (double)b->gm[q];
+      const bool rows = 1.097 * (double)b->gw[q] + 103.5 * m_q < 1.232 * (double)b->gwmin[q] + 117.5 * m_q;
+      if (rows && b->vbase[q + 1] > b->vbase[q]) {
+        ATC_CK(cudaMemsetAsync(b->vrows + b->vbase[q], 1, (size_t)(b->vbase[q + 1] - b->vbase[q]), s));
+        ++nrows;
+      }
+    }
+    ATC_CK(cudaStreamSynchronize(s));
+  }
+  b->rows_graphs = mixed ? nrows : (sh.by_source == 1 ? ng : 0);
+  const uint8_t* skip = mixed ? b->vrows : nullptr;
   cudaStream_t c = b->cap_stream;
   size_t bytes = 0;
   ATC_TRY(exclusive_scan_i32_to_i64_tmp(nullptr, &bytes, b->cnt, b->gstart, (size_t)n + 1, s));
@@ -253,16 +293,25 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   cudaMemsetAsync(b->cur, 0, sizeof(int32_t) * (n + 1), c);
   cudaMemsetAsync(b->counters, 0, sizeof(int) * 8, c);
   cudaMemsetAsync(b->gcounts, 0, sizeof(unsigned long long) * ng, c);
-  if (!sh.by_source) {
-    group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt);
+  if (sh.by_source != 1) {
+    group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt, skip);
     exclusive_scan_i32_to_i64_tmp(b->scan_tmp, &bytes, b->cnt, b->gstart, (size_t)n + 1, c);
-    group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist);
+    group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist, skip);
   }
-  group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, gstart, b->items, cap_items, b->counters, sh);
+  group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, gstart, b->items, cap_items, b->counters, sh, skip, 0);
   bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(g, plist, bitems, 0, b->counters + 1,
                                                                             b->counters + 5, words, tags, b->gcounts);
   bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(g, plist, witems, 0, b->counters,
                                                                        b->counters + 4, tags, b->gcounts);
+  if (mixed && nrows > 0) {
+    cudaMemsetAsync(b->counters_r, 0, sizeof(int) * 8, c);
+    group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->off, b->items_r, cap_items, b->counters_r, shr,
+                                                                b->vrows, 1);
+    bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(
+        g, b->cols, bitems_r, 0, b->counters_r + 1, b->counters_r + 5, words, tags, b->gcounts);
+    bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(
+        g, b->cols, witems_r, 0, b->counters_r, b->counters_r + 4, tags, b->gcounts);
+  }
   cudaError_t launch_err = cudaGetLastError();
   cudaError_t end_err = cudaStreamEndCapture(c, &b->graph);
   if (launch_err != cudaSuccess || end_err != cudaSuccess) {

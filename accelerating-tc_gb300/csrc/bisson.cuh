@@ -121,7 +121,8 @@ struct ItemShape {
   int warp_chunk;
   int block_chunk;
   int by_source;    // batches: 1 = every edge at its source (h = u, partners = its row: the
-                    // Hu-style wedge walk, no grouping passes), 0 = at the longer endpoint
+                    // Hu-style wedge walk, no grouping passes), 0 = at the longer endpoint,
+                    // 2 = chosen per graph by the cost model (batch.cu)
 };
 
 __host__ __device__ inline ItemShape default_shape(int cutover) {
@@ -266,17 +267,21 @@ __device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f) {
   }
 }
 
-__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt) {
+// skip (nullable): rows u with skip[u] != 0 are not grouped (their graph counts by rows).
+__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt, const uint8_t* skip) {
   for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
+    if (skip && ok) ok = !skip[u];
     const int32_t h = ok ? (longer_is_u(u, v, du, dv) ? u : v) : -1;
     const unsigned same = __match_any_sync(0xffffffffu, h);
     if (h >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&cnt[h], __popc(same));
   });
 }
 
-__global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
+__global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist,
+                                        const uint8_t* skip) {
   const int lane = threadIdx.x & 31;
   for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
+    if (skip && ok) ok = !skip[u];
     int32_t h = -1, p = 0;
     if (ok) {
       const bool hu = longer_is_u(u, v, du, dv);
@@ -293,14 +298,15 @@ __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_
 }
 
 // Compact items: counters[0] warp items (front), counters[1] block items (back),
-// counters[3] longest list among block items.
+// counters[3] longest list among block items.  sel (nullable): only vertices h with
+// sel[h] == want get items.
 __global__ void group_items_compact_kernel(CsrView g, const int64_t* gstart, int2* items, int64_t cap, int* counters,
-                                           ItemShape sh) {
+                                           ItemShape sh, const uint8_t* sel, uint8_t want) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t n_pad = (g.n + 31) & ~31ll;
   for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < n_pad; h += stride) {
     int64_t b = 0, e = 0, dh = 0;
-    if (h < g.n) {
+    if (h < g.n && (!sel || sel[h] == want)) {
       b = gstart[h];
       e = gstart[h + 1];
       dh = g.off[h + 1] - g.off[h];

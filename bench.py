@@ -570,7 +570,8 @@ def batch_params(count, seed):
 BATCH_CANDIDATES = [{}, {"bisson_warp_max": 128}, {"bisson_warp_max": 64, "bisson_cutover": 16},
                     {"bisson_warp_chunk": 256, "bisson_block_chunk": 1024},
                     {"bisson_warp_chunk": 2048, "bisson_block_chunk": 8192},
-                    {"bisson_cutover": 64}, {"group_by_source": 1}, {"group_by_source": 1, "bisson_cutover": 8}]
+                    {"bisson_cutover": 64}, {"group_by_source": 1}, {"group_by_source": 1, "bisson_cutover": 8},
+                    {"group_by_source": 2}, {"group_by_source": 2, "bisson_cutover": 64}]
 
 
 def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):

@@ -130,7 +130,8 @@ typedef struct atc_tuning {
   /* the bisson_* item shape applies to the Hu-style kernel too */
   int32_t group_by_source;   /* batches: 1 = every edge at its source, the items index the
                                 CSR rows (Hu-style wedge tests, no grouping passes); 0 = at
-                                the endpoint with the longer list (Bisson-style) */
+                                the endpoint with the longer list (Bisson-style); 2 = each
+                                graph the way the Hu/Bisson cost model predicts faster */
   int32_t kcl_dense;         /* k-cliques (atc_kcl_part_tuned): 0 = candidate sets of 65..1024
                                 members on the dense kernel from k = 5 on; -1 = every edge on
                                 the warp search */

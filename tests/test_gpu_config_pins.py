@@ -161,7 +161,8 @@ def test_batch_chunglu_subset_matches_oracle():
         b.add(csr)
         csr.free()
         want.append(oracle.tc_count(pairs.cpu().numpy()))
-    for t in (None, {"group_by_source": 1, "bisson_cutover": 8}):
+    for t in (None, {"group_by_source": 1, "bisson_cutover": 8}, {"group_by_source": 2},
+              {"group_by_source": 2, "bisson_cutover": 64}):
         got, _ = b.run(tuning=t)
         assert [int(x) for x in got] == want
     b.free()

@@ -537,7 +537,8 @@ def test_batch_counts_match_per_graph():
     assert counts2.tolist() == want
     for t in ({"bisson_cutover": 8, "bisson_warp_max": 64}, {"bisson_warp_chunk": 32, "bisson_block_chunk": 64},
               {"bisson_warp_max": 256, "bisson_cutover": 256}, {"group_by_source": 1},
-              {"group_by_source": 1, "bisson_warp_max": 64, "bisson_warp_chunk": 32}):
+              {"group_by_source": 1, "bisson_warp_max": 64, "bisson_warp_chunk": 32}, {"group_by_source": 2},
+              {"group_by_source": 2, "bisson_warp_max": 64, "bisson_warp_chunk": 32}):
         assert b.run(tuning=t)[0].tolist() == want, t
     best, ms = b.tune([{}, {"bisson_warp_max": 128}, {"bisson_block_chunk": 256}])
     assert 0 <= best < 3 and np.all(ms > 0)

@@ -5,6 +5,7 @@ permutation byte for byte, costFuncCal / verification figures as the tools print
 and the OrgTriangleCount triangle counts.
 """
 import hashlib
+import os
 
 import numpy as np
 import pytest
@@ -258,3 +259,29 @@ def test_oracle_rmat_generator_equals_libatc():
     import atc
     for scale, ef, seed in ((6, 4, 3), (10, 16, 1), (14, 8, 9)):
         assert np.array_equal(oracle.gen_rmat(scale, ef, seed, nthreads=3), atc.gen_rmat(scale, ef, seed))
+
+
+REF_GPU = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu_counts.json")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_GPU), reason="no recorded run of the reference GPU programs")
+def test_reference_gpu_programs_count_what_the_oracle_counts(golden):
+    """The counts the reference's own GPU programs (Hu, Bisson, Fox, TriCore, built for sm_103a,
+    recorded by tests/golden/make_refgpu_golden.py) printed on the benchmark graphs equal the
+    oracle's: the golden R-MAT scale 16 count, and the config pins at scales 20 and 24."""
+    import json
+    with open(REF_GPU) as f:
+        rec = json.load(f)["graphs"]
+    with open(os.path.join(os.path.dirname(REF_GPU), "config_pins.json")) as f:
+        pins = json.load(f)
+    want = {"rmat16": golden["cases"]["rmat_s16_ef16_seed1"]["triangles"],
+            "rmat20": pins["kcl"]["rmat20"]["cliques"]["3"], "rmat24": pins["rmat24"]["triangles"]}
+    seen = 0
+    for gname, g in rec.items():
+        for pname, p in g["programs"].items():
+            if "skipped" in p:
+                assert pname == "bisson" and gname == "rmat24"
+                continue
+            assert p["rc"] == 0 and p["count"] == want[gname], (gname, pname, p)
+            seen += 1
+    assert seen >= 4
