@@ -149,44 +149,6 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def gpu_numa(index):
-    """(NUMA node, CPU list) the GPU's PCI device reports, or (-1, None)."""
-    try:
-        bus = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
-                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=30).stdout.strip()
-    except (OSError, subprocess.SubprocessError):
-        return -1, None
-    if not bus:
-        return -1, None
-    dom, rest = bus.lower().split(":", 1)
-    path = "/sys/bus/pci/devices/%04x:%s" % (int(dom, 16) & 0xFFFF, rest)
-    try:
-        node = int(open(os.path.join(path, "numa_node")).read().strip())
-        cpus = open(os.path.join(path, "local_cpulist")).read().strip()
-    except (OSError, ValueError):
-        return -1, None
-    return node, cpus
-
-
-def place_host_memory_near(index):
-    """Makes the host memory this process allocates from now on prefer the GPU's NUMA node
-    (set_mempolicy MPOL_PREFERRED), so that pinned staging buffers sit next to the GPU rather
-    than wherever the kernel happens to find free pages.  Returns the node, or -1 when the
-    GPU reports none or the call is refused."""
-    import ctypes
-    node, _ = gpu_numa(index)
-    if node < 0 or node >= 64:
-        return -1
-    nr = {"aarch64": 237, "x86_64": 238}.get(os.uname().machine)
-    if nr is None:
-        return -1
-    mask = ctypes.c_ulong(1 << node)
-    libc = ctypes.CDLL(None, use_errno=True)
-    if libc.syscall(nr, 1, ctypes.byref(mask), ctypes.c_ulong(64)) != 0:  # MPOL_PREFERRED = 1
-        return -1
-    return node
-
-
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
