@@ -258,6 +258,27 @@ void keep_pool() {
   cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
 }
 
+// Copies the input pairs from pinned host memory to the device with the SMs: every thread
+// moves 16-byte pieces (two pairs) through the device's mapping of the host buffer over
+// NVLink-C2C.  The copy engines, which cudaMemcpyAsync uses, were measured to slow down
+// intermittently to ~20 GB/s on the GPU hosts after other processes had used and freed
+// much of the device memory, while SM reads of the same pinned buffer kept their speed
+// (about 200 GB/s, as a fast copy-engine transfer).
+__global__ void copy_pairs_kernel(const int2* __restrict__ src, uint64_t np, int2* __restrict__ dst) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+  if (vec) {
+    const uint64_t nq = np >> 1;
+    const int4* s4 = reinterpret_cast<const int4*>(src);
+    int4* d4 = reinterpret_cast<int4*>(dst);
+    for (uint64_t i = i0; i < nq; i += stride) d4[i] = s4[i];
+    if (i0 == 0 && (np & 1)) dst[np - 1] = src[np - 1];
+  } else {
+    for (uint64_t i = i0; i < np; i += stride) dst[i] = src[i];
+  }
+}
+
 }  // namespace
 
 atc_status build_simple_edges(const int2* pairs, uint64_t np, SimpleEdges* out, cudaStream_t s) {
@@ -510,7 +531,20 @@ extern "C" atc_status atc_pretc(const int32_t* pairs, uint64_t np, atc_dir dir, 
   }
   {
     Phase ph_copy("pretc.h2d", st);
-    if (np) ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
+    // pinned (page-locked) host memory has a device mapping: the SMs copy it; pageable memory
+    // goes through cudaMemcpyAsync
+    cudaPointerAttributes attr{};
+    const void* mapped = nullptr;
+    if (np && cudaPointerGetAttributes(&attr, pairs) == cudaSuccess && attr.type == cudaMemoryTypeHost)
+      mapped = attr.devicePointer;
+    cudaGetLastError();  // a failed query only selects the copy path
+    if (mapped) {
+      copy_pairs_kernel<<<grid_for((int64_t)(np >> 1) + 1, 256, 16), 256, 0, st>>>(
+          static_cast<const int2*>(mapped), np, d.p);
+      ATC_CK(cudaGetLastError());
+    } else if (np) {
+      ATC_CK(cudaMemcpyAsync(d.p, pairs, sizeof(int2) * np, cudaMemcpyHostToDevice, st));
+    }
   }
   return pretc_impl(d.p, np, dir, order, t, out, perm_out, st);
 } ATC_CATCH

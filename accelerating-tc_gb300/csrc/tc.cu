@@ -329,13 +329,69 @@ struct SortedProber {
   __device__ __forceinline__ unsigned finish() { return 0u; }
 };
 
+// ---- 1-D bulk copies into shared memory (the TMA unit's untiled mode) -------------
+// One thread issues cp.async.bulk of a whole list; its completion is counted in bytes on an
+// mbarrier that every thread of the copy's group waits on.  Source and destination start on
+// 16-byte boundaries and the size is a multiple of 16 bytes: a list is copied from the
+// 16-byte boundary at or below its first element to the one at or above its end (the CSR's
+// cols carry 16 ints of padding, so the rounded end stays inside the allocation), and read
+// from the offset of its first element.  Every wait is bounded: a wait that runs out records
+// an error for the host (ATC_ERR_TIMEOUT) and the kernel stops counting.
+constexpr uint32_t kBulkWaitPolls = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+// Issued by one thread: the byte count the barrier's current phase waits for, then the copy.
+// The proxy fence orders the group's earlier ordinary reads of `dst` before the async write.
+__device__ __forceinline__ void bulk_list_to_smem(int32_t* dst, const int32_t* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Waits for phase `parity` of the barrier to complete; false if kBulkWaitPolls polls did not see it.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kBulkWaitPolls; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// The 16-byte-aligned window [a0, a1) of cols holding the list [hb, hb + dh).
+__device__ __forceinline__ void bulk_window(int64_t hb, int64_t dh, int64_t* a0, uint32_t* bytes) {
+  *a0 = hb & ~3ll;
+  *bytes = (uint32_t)(((hb + dh + 3) & ~3ll) - *a0) * 4u;
+}
+
+// bulk: stage N+(h) with bulk copies (device-resident cols); otherwise with loads (cols in
+// mapped host memory).  err: set to 1 when a bulk wait runs out.
 template <int KIND>
 __global__ void __launch_bounds__(kBgWarps * 32) sorted_warp_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                     const GroupItem* __restrict__ items, int nitems,
-                                                                    int* next, unsigned long long* out) {
-  __shared__ int32_t T[kBgWarps][kWarpMax];
+                                                                    int* next, bool bulk, int* err,
+                                                                    unsigned long long* out) {
+  __shared__ __align__(16) int32_t T[kBgWarps][kWarpMax + 8];
   __shared__ int32_t piv[kBgWarps][32];
+  __shared__ __align__(8) uint64_t bar[kBgWarps];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) mbar_init(&bar[w]);
+  __syncwarp();
+  uint32_t phase = 0;
   unsigned long long total = 0;
   for (;;) {
     int it = 0;
@@ -345,13 +401,29 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_warp_kernel(CsrView g, c
     const GroupItem gi = items[it];
     const int64_t hb = g.off[gi.h];
     const int dh = (int)(g.off[gi.h + 1] - hb);  // 1 .. kWarpMax
-    for (int j = lane; j < dh; j += 32) T[w][j] = __ldg(g.cols + hb + j);
-    __syncwarp();
-    piv[w][lane] = T[w][(lane * dh) >> 5];
+    const int32_t* L = T[w];
+    if (bulk) {
+      int64_t a0;
+      uint32_t bytes;
+      bulk_window(hb, dh, &a0, &bytes);
+      if (lane == 0) bulk_list_to_smem(T[w], g.cols + a0, bytes, &bar[w]);
+      const bool ok = mbar_wait(&bar[w], phase);
+      phase ^= 1u;
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicExch(err, 1);
+        mbar_wait(&bar[w], phase ^ 1u);  // once more for the copy in flight, then stop
+        break;
+      }
+      L = T[w] + (hb - a0);
+    } else {
+      for (int j = lane; j < dh; j += 32) T[w][j] = __ldg(g.cols + hb + j);
+      __syncwarp();
+    }
+    piv[w][lane] = L[(lane * dh) >> 5];
     __syncwarp();
     int64_t cur = gi.b;
     auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
-    SortedProber<KIND> pr{T[w], piv[w], dh, T[w][dh - 1], 0, INT32_MIN, 16};
+    SortedProber<KIND> pr{L, piv[w], dh, L[dh - 1], 0, INT32_MIN, 16};
     total += stream_partners(g, plist, gi.e, lane, nb, pr);
     __syncwarp();  // the next item overwrites the copy
   }
@@ -361,13 +433,17 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_warp_kernel(CsrView g, c
 template <int KIND>
 __global__ void __launch_bounds__(kBgWarps * 32) sorted_block_kernel(CsrView g, const int32_t* __restrict__ plist,
                                                                      const GroupItem* __restrict__ items, int nitems,
-                                                                     int* next, uint32_t tab_words,
-                                                                     unsigned long long* out) {
-  extern __shared__ __align__(16) int32_t T[];  // tab_words
+                                                                     int* next, uint32_t tab_words, bool bulk,
+                                                                     int* err, unsigned long long* out) {
+  extern __shared__ __align__(16) int32_t T[];  // tab_words + 8
   __shared__ int32_t piv[32];
   __shared__ int cur_item;
   __shared__ unsigned long long bnext;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ __align__(8) uint64_t bar;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) mbar_init(&bar);
+  __syncthreads();
+  uint32_t phase = 0;
   unsigned long long total = 0;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -381,8 +457,24 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_block_kernel(CsrView g, 
     const int64_t hb = g.off[gi.h];
     const int64_t dh = g.off[gi.h + 1] - hb;
     const bool staged = dh <= (int64_t)tab_words;
-    if (staged)
+    const int32_t* L = g.cols + hb;
+    if (staged && bulk) {
+      int64_t a0;
+      uint32_t bytes;
+      bulk_window(hb, dh, &a0, &bytes);
+      if (threadIdx.x == 0) bulk_list_to_smem(T, g.cols + a0, bytes, &bar);
+      const bool ok = __syncthreads_and(mbar_wait(&bar, phase));
+      phase ^= 1u;
+      if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        mbar_wait(&bar, phase ^ 1u);  // once more for the copy in flight, then stop
+        break;
+      }
+      L = T + (hb - a0);
+    } else if (staged) {
       for (int64_t j = threadIdx.x; j < dh; j += blockDim.x) T[j] = __ldg(g.cols + hb + j);
+      L = T;
+    }
     if (threadIdx.x < 32) piv[threadIdx.x] = __ldg(g.cols + hb + (((int64_t)threadIdx.x * dh) >> 5));
     __syncthreads();
     auto nb = [&]() {
@@ -390,7 +482,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_block_kernel(CsrView g, 
       if (lane == 0) r = atomicAdd(&bnext, 32ull);
       return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
     };
-    SortedProber<KIND> pr{staged ? T : g.cols + hb, piv, (int)dh, __ldg(g.cols + hb + dh - 1), 0, INT32_MIN, 16};
+    SortedProber<KIND> pr{L, piv, (int)dh, __ldg(g.cols + hb + dh - 1), 0, INT32_MIN, 16};
     total += stream_partners(g, plist, gi.e, lane, nb, pr);
     __syncthreads();  // the next item overwrites the copy
   }
@@ -649,8 +741,10 @@ static atc_status run_bisson(const CsrView& g, const atc_tuning* t, unsigned lon
 
 // TriCore-style (KIND 0) and Fox-style (KIND 1) searches of the staged longer lists.
 // max_outdeg sizes the block kernels' shared copy (lists above kTabWords stay in global).
+// bulk: the lists are staged by TMA bulk copies (cols in device memory); with cols in mapped
+// host memory they are staged with loads.
 template <int KIND>
-static atc_status run_sorted(const CsrView& g, int max_outdeg, unsigned long long* ctr, cudaStream_t s,
+static atc_status run_sorted(const CsrView& g, int max_outdeg, bool bulk, unsigned long long* ctr, cudaStream_t s,
                              int* launches) {
   ItemShape sh = default_shape(kWarpMax);
   std::optional<Phase> ph;
@@ -662,13 +756,14 @@ static atc_status run_sorted(const CsrView& g, int max_outdeg, unsigned long lon
   if (gr.hc[1]) {
     uint32_t words = (uint32_t)std::min(std::max(max_outdeg, kWarpMax + 1), kTabWords);
     words = (words + 31) & ~31u;
-    const size_t smem = sizeof(int32_t) * words;
+    const size_t smem = sizeof(int32_t) * (words + 8);  // + the bulk window's rounding
     ATC_CK(cudaFuncSetAttribute((const void*)sorted_block_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
     const int bps = blocks_per_sm((const void*)sorted_block_kernel<KIND>, kBgWarps * 32, smem);
     const int grid = std::min(gr.hc[1], sm_count() * bps);
     sorted_block_kernel<KIND><<<grid, kBgWarps * 32, smem, s>>>(g, gr.plist.p, gr.bitems.p, gr.hc[1],
-                                                                 gr.counters.p + 5, words, ctr);
+                                                                 gr.counters.p + 5, words, bulk, gr.counters.p + 7,
+                                                                 ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
   }
@@ -676,9 +771,16 @@ static atc_status run_sorted(const CsrView& g, int max_outdeg, unsigned long lon
     const int bps = blocks_per_sm((const void*)sorted_warp_kernel<KIND>, kBgWarps * 32, 0);
     const int grid = (int)std::min<int64_t>((gr.hc[0] + kBgWarps - 1) / kBgWarps, (int64_t)sm_count() * bps);
     sorted_warp_kernel<KIND><<<grid, kBgWarps * 32, 0, s>>>(g, gr.plist.p, gr.witems.p, gr.hc[0],
-                                                            gr.counters.p + 4, ctr);
+                                                            gr.counters.p + 4, bulk, gr.counters.p + 7, ctr);
     ATC_CK(cudaGetLastError());
     *launches += 1;
+  }
+  int err = 0;
+  ATC_CK(cudaMemcpyAsync(&err, gr.counters.p + 7, sizeof(int), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (err) {
+    set_error("a bulk copy into shared memory did not complete within its wait limit");
+    return ATC_ERR_TIMEOUT;
   }
   return ATC_OK;
 }
@@ -898,11 +1000,11 @@ static atc_status tc_window(const atc_csr* csr, atc_kernel kernel, const atc_tun
       case ATC_KERNEL_BISSON: ATC_TRY(run_bisson(g, tuning, ctr, s, &launches)); break;
       case ATC_KERNEL_FOX:
         if (tuning && tuning->edge_kernels) ATC_TRY(run_fox(g, tuning, ctr, s, &launches));
-        else ATC_TRY(run_sorted<1>(g, csr->max_outdeg, ctr, s, &launches));
+        else ATC_TRY(run_sorted<1>(g, csr->max_outdeg, pv->host_cols == nullptr, ctr, s, &launches));
         break;
       default:
         if (tuning && tuning->edge_kernels) ATC_TRY(run_tricore(g, tuning, ctr, s, &launches));
-        else ATC_TRY(run_sorted<0>(g, csr->max_outdeg, ctr, s, &launches));
+        else ATC_TRY(run_sorted<0>(g, csr->max_outdeg, pv->host_cols == nullptr, ctr, s, &launches));
         break;
     }
     tm.stop(s);
