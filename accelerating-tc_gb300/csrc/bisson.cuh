@@ -232,8 +232,10 @@ struct CompactItems {
 // done with shuffles.  Every lane has an edge in every round but the last, whatever the
 // row lengths (a warp per row would leave most lanes idle on short rows).  Same grouping
 // rule as the per-edge passes.  f(u, v, du, dv, valid) is called by all 32 lanes.
+// skip (nullable): rows u with skip[u] != 0 are passed over; a block of 32 such rows is not
+// read at all (the graphs of a batch are contiguous vertex ranges).
 template <class F>
-__device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f) {
+__device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f, const uint8_t* skip = nullptr) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t blocks = (g.n + 31) >> 5;
@@ -241,6 +243,7 @@ __device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f) {
     const int64_t u0 = rb << 5;
     const int64_t row = u0 + lane;
     const int64_t last = min(u0 + 32, g.n);
+    if (skip && __all_sync(0xffffffffu, row >= last || skip[row])) continue;
     const int64_t start = __ldg(g.off + min(row, last));  // rows past the end start at the block's end
     const int64_t stop = __shfl_sync(0xffffffffu, __ldg(g.off + last), 0);
     const int64_t first = __shfl_sync(0xffffffffu, start, 0);
@@ -274,7 +277,7 @@ __global__ void group_count_vc_kernel(CsrView g, int32_t* cnt, const uint8_t* sk
     const int32_t h = ok ? (longer_is_u(u, v, du, dv) ? u : v) : -1;
     const unsigned same = __match_any_sync(0xffffffffu, h);
     if (h >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&cnt[h], __popc(same));
-  });
+  }, skip);
 }
 
 __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist,
@@ -294,7 +297,7 @@ __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_
     if (h >= 0 && lane == lead) at = atomicAdd(&cur[h], __popc(same));
     at = __shfl_sync(0xffffffffu, at, lead);
     if (h >= 0) plist[gstart[h] + at + __popc(same & ((1u << lane) - 1))] = p;
-  });
+  }, skip);
 }
 
 // Compact items: counters[0] warp items (front), counters[1] block items (back),
