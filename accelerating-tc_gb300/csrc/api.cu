@@ -51,7 +51,8 @@ namespace {
 struct PhaseRec {
   char name[40];
   int depth;
-  cudaEvent_t a, b;
+  cudaEvent_t a, b;  // both null: `ms` holds the time (phase_add)
+  float ms;
 };
 struct PhaseLog {
   bool on = false;
@@ -68,6 +69,18 @@ struct PhaseLog {
 };
 thread_local PhaseLog g_phases;
 }  // namespace
+
+bool phase_timing_on() { return g_phases.on; }
+
+void phase_add(const char* name, float ms) {
+  PhaseLog& L = g_phases;
+  if (!L.on) return;
+  PhaseRec r{};
+  snprintf(r.name, sizeof(r.name), "%s", name);
+  r.depth = L.depth;
+  r.ms = ms;
+  L.recs.push_back(r);
+}
 
 Phase::Phase(const char* name, cudaStream_t s) : s_(s) {
   nvtxRangePushA(name);
@@ -117,9 +130,11 @@ extern "C" atc_status atc_phase_times(atc_phase_time* out, int32_t cap, int32_t*
   int32_t k = 0;
   for (auto& r : L.recs) {
     if (k >= cap) break;
-    float ms = 0.f;
-    ATC_CK(cudaEventSynchronize(r.b));
-    ATC_CK(cudaEventElapsedTime(&ms, r.a, r.b));
+    float ms = r.ms;
+    if (r.a) {
+      ATC_CK(cudaEventSynchronize(r.b));
+      ATC_CK(cudaEventElapsedTime(&ms, r.a, r.b));
+    }
     atc_phase_time& o = out[k++];
     memset(&o, 0, sizeof(o));
     snprintf(o.name, sizeof(o.name), "%s", r.name);

@@ -27,6 +27,7 @@ struct atc_batch {
   int32_t max_outdeg = 0;
   bool dirty = true;
   int rows_graphs = 0;  // graphs of the last built pipeline counted by rows
+  int launches = 0;     // kernel launches of one replay of the built pipeline
   atc::ItemShape shape = atc::default_shape(32);
   // counting pipeline, sized for the union when built
   int32_t* cnt = nullptr;
@@ -37,6 +38,9 @@ struct atc_batch {
   int* counters = nullptr;
   int2* items_r = nullptr;   // mode 2: the rows items of the graphs counted by rows
   int* counters_r = nullptr;
+  int2* big = nullptr;       // block items of lists longer than kBlockSmallList
+  int2* big_r = nullptr;     // the same for the rows items
+  int64_t big_cap = 0;
   uint8_t* vrows = nullptr;  // mode 2: 1 for the vertices of graphs counted by rows
   int64_t* vbase_d = nullptr;
   unsigned long long* gcounts = nullptr;
@@ -47,10 +51,18 @@ struct atc_batch {
   cudaStream_t cap_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // event nodes of the replay: stage k runs from stage_ev[k] to stage_ev[k + 1]
+  std::vector<cudaEvent_t> stage_ev;
+  std::vector<const char*> stage_name;
 };
 
 namespace atc {
 namespace {
+
+// counters of one replay: [0] warp items, [1] block items, [2] block items of long lists,
+// [3] longest list among [1], [4..6] the counting kernels' item cursors, [8], [9] the
+// grouping passes' row-block queues
+constexpr int kBatchCounters = 16;
 
 __global__ void batch_copy_kernel(const int64_t* off_g, const int32_t* cols_g, int64_t n_g, int64_t m_g,
                                   int64_t vbase, int64_t ebase, int64_t* off_u, int32_t* cols_u) {
@@ -67,7 +79,7 @@ void free_pipeline(atc_batch* b) {
   b->exec = nullptr;
   b->graph = nullptr;
   void* bufs[] = {b->cnt, b->cur, b->gstart, b->plist, b->items, b->counters, b->vbase_d, b->gcounts, b->scan_tmp,
-                  b->items_r, b->counters_r, b->vrows};
+                  b->items_r, b->counters_r, b->vrows, b->big, b->big_r};
   for (void* p : bufs)
     if (p) cudaFree(p);
   b->cnt = b->cur = b->plist = nullptr;
@@ -77,6 +89,8 @@ void free_pipeline(atc_batch* b) {
   b->items_r = nullptr;
   b->counters_r = nullptr;
   b->vrows = nullptr;
+  b->big = b->big_r = nullptr;
+  b->big_cap = 0;
   b->gcounts = nullptr;
   b->scan_tmp = nullptr;
   b->built_n = b->built_m = -1;
@@ -180,6 +194,7 @@ extern "C" atc_status atc_batch_destroy(atc_batch* b) try {
   if (b->off) cudaFree(b->off);
   if (b->cols) cudaFree(b->cols);
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+  for (cudaEvent_t e : b->stage_ev) cudaEventDestroy(e);
   delete b;
   return ATC_OK;
 } ATC_CATCH
@@ -210,17 +225,23 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   const int64_t n = b->n, m = b->m;
   const int ng = (int)(b->vbase.size() - 1);
   const int64_t cap_items = max_items(n, m, std::min(sh.warp_chunk, sh.block_chunk));
-  if (b->built_n != n || b->built_m != m || b->built_graphs != ng || b->items_cap < cap_items) {
+  // block items of lists longer than kBlockSmallList: one per such list (at most
+  // m / (kBlockSmallList + 1) of them) plus one per chunk boundary
+  const int64_t big_cap = m / (kBlockSmallList + 1) + m / sh.block_chunk + 1;
+  if (b->built_n != n || b->built_m != m || b->built_graphs != ng || b->items_cap < cap_items ||
+      b->big_cap < big_cap) {
     free_pipeline(b);
     ATC_TRY(dev_alloc(&b->cnt, (size_t)n + 1));
     ATC_TRY(dev_alloc(&b->cur, (size_t)n + 1));
     ATC_TRY(dev_alloc(&b->gstart, (size_t)n + 1));
     ATC_TRY(dev_alloc(&b->plist, (size_t)m + 32));
     ATC_TRY(dev_alloc(&b->items, (size_t)cap_items));
-    ATC_TRY(dev_alloc(&b->counters, 8));
+    ATC_TRY(dev_alloc(&b->counters, kBatchCounters));
     ATC_TRY(dev_alloc(&b->items_r, (size_t)cap_items));
     ATC_TRY(dev_alloc(&b->counters_r, 8));
     ATC_TRY(dev_alloc(&b->vrows, (size_t)n + 1));
+    ATC_TRY(dev_alloc(&b->big, (size_t)big_cap));
+    ATC_TRY(dev_alloc(&b->big_r, (size_t)big_cap));
     ATC_TRY(dev_alloc(&b->vbase_d, (size_t)ng + 1));
     ATC_TRY(dev_alloc(&b->gcounts, (size_t)ng));
     size_t bytes = 0;
@@ -231,6 +252,7 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
     b->built_m = m;
     b->built_graphs = ng;
     b->items_cap = cap_items;
+    b->big_cap = big_cap;
   } else if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     cudaGraphDestroy(b->graph);
@@ -241,14 +263,20 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   ATC_CK(cudaStreamSynchronize(s));
   if (!b->cap_stream) ATC_CK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
 
+  // block tables: lists up to kBlockSmallList at load factor 1/4 (at most 32 KB), and the
+  // full 64 KB table for the longer lists, launched apart so that the short lists' CTAs are
+  // not held to the occupancy of the largest table
+  const void* kblock = (const void*)bisson_block_kernel<CompactItems, kDefaultSlots>;
   uint32_t words = 64;
-  const uint32_t want = 4u * (uint32_t)std::min(std::max(b->max_outdeg, 1), kHashMax);
+  const uint32_t want = 4u * (uint32_t)std::min(std::max(b->max_outdeg, 1), kBlockSmallList);
   while (words < want) words <<= 1;
-  if (b->max_outdeg > kHashMax) words = kTabWords;
-  size_t smem = sizeof(int32_t) * words;
-  ATC_CK(cudaFuncSetAttribute((const void*)bisson_block_kernel<CompactItems, kDefaultSlots>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int grid_block = sm_count() * blocks_per_sm((const void*)bisson_block_kernel<CompactItems, kDefaultSlots>, kBgWarps * 32, smem);
+  const bool any_big = b->max_outdeg > kBlockSmallList;
+  const uint32_t words_big = kTabWords;
+  const size_t smem = sizeof(int32_t) * words, smem_big = sizeof(int32_t) * words_big;
+  ATC_CK(cudaFuncSetAttribute(kblock, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(any_big ? smem_big : smem)));
+  const int grid_block = sm_count() * blocks_per_sm(kblock, kBgWarps * 32, smem);
+  const int grid_big = sm_count() * blocks_per_sm(kblock, kBgWarps * 32, smem_big);
   const int grid_warp = sm_count() * blocks_per_sm((const void*)bisson_warp_kernel<CompactItems, kDefaultSlots>, kBgWarps * 32, 0);
 
   CsrView g = csr_view(b->off, b->cols, nullptr, n, m);
@@ -257,8 +285,9 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   // itself and the grouping passes are skipped
   const int64_t* gstart = sh.by_source == 1 ? b->off : b->gstart;
   const int32_t* plist = sh.by_source == 1 ? b->cols : b->plist;
-  CompactItems witems{b->items, gstart, cap_items, false, sh};
-  CompactItems bitems{b->items, gstart, cap_items, true, sh};
+  CompactItems witems{b->items, gstart, cap_items, false, false, sh};
+  CompactItems bitems{b->items, gstart, cap_items, true, true, sh};
+  CompactItems litems{b->big, gstart, big_cap, false, true, sh};
   // mode 2: each graph counts by rows (every wedge tested at its source, W tests, no grouping)
   // or grouped at the longer endpoint (sum of min(d+u, d+v) tests plus the grouping passes),
   // whichever the per-graph cost model of the two kernels predicts faster (the per-call terms
@@ -267,8 +296,9 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   ItemShape shr = sh;
   shr.by_source = 1;
   shr.cutover = std::min(sh.cutover, 8);  // the rows items' sorted copy, as the single-graph Hu count
-  CompactItems witems_r{b->items_r, b->off, cap_items, false, shr};
-  CompactItems bitems_r{b->items_r, b->off, cap_items, true, shr};
+  CompactItems witems_r{b->items_r, b->off, cap_items, false, false, shr};
+  CompactItems bitems_r{b->items_r, b->off, cap_items, true, true, shr};
+  CompactItems litems_r{b->big_r, b->off, big_cap, false, true, shr};
   int nrows = 0;
   if (mixed) {
     ATC_CK(cudaMemsetAsync(b->vrows, 0, (size_t)n + 1, s));
@@ -288,29 +318,69 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   size_t bytes = 0;
   ATC_TRY(exclusive_scan_i32_to_i64_tmp(nullptr, &bytes, b->cnt, b->gstart, (size_t)n + 1, s));
 
+  // event nodes between the stages (read by atc_phase_times after a replay)
+  constexpr int kMaxStages = 12;
+  while (b->stage_ev.size() < (size_t)kMaxStages + 1) {
+    cudaEvent_t e = nullptr;
+    ATC_CK(cudaEventCreate(&e));
+    b->stage_ev.push_back(e);
+  }
+  b->stage_name.clear();
+  int kernels = 0;
+  auto stage = [&](const char* name) {
+    b->stage_name.push_back(name);
+    cudaEventRecordWithFlags(b->stage_ev[b->stage_name.size()], c, cudaEventRecordExternal);
+  };
+
   ATC_CK(cudaStreamBeginCapture(c, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecordWithFlags(b->stage_ev[0], c, cudaEventRecordExternal);
   cudaMemsetAsync(b->cnt, 0, sizeof(int32_t) * (n + 1), c);
   cudaMemsetAsync(b->cur, 0, sizeof(int32_t) * (n + 1), c);
-  cudaMemsetAsync(b->counters, 0, sizeof(int) * 8, c);
+  cudaMemsetAsync(b->counters, 0, sizeof(int) * kBatchCounters, c);
   cudaMemsetAsync(b->gcounts, 0, sizeof(unsigned long long) * ng, c);
+  stage("batch.reset");
   if (sh.by_source != 1) {
-    group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt, skip);
+    group_count_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->cnt, skip, b->counters + 8);
     exclusive_scan_i32_to_i64_tmp(b->scan_tmp, &bytes, b->cnt, b->gstart, (size_t)n + 1, c);
-    group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist, skip);
+    group_scatter_vc_kernel<<<grid_for(n * 32, 256), 256, 0, c>>>(g, b->gstart, b->cur, b->plist, skip,
+                                                                 b->counters + 9);
+    kernels += 4;  // two grouping passes and the scan's two kernels
+    stage("batch.group");
   }
-  group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, gstart, b->items, cap_items, b->counters, sh, skip, 0);
+  group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, gstart, b->items, cap_items, b->big, b->counters, sh,
+                                                              skip, 0);
+  kernels += 3;  // items, block, warp
+  stage("batch.items");
   bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(g, plist, bitems, 0, b->counters + 1,
                                                                             b->counters + 5, words, tags, b->gcounts);
+  stage("batch.block");
+  if (any_big) {
+    bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_big, kBgWarps * 32, smem_big, c>>>(
+        g, plist, litems, 0, b->counters + 2, b->counters + 6, words_big, tags, b->gcounts);
+    kernels += 1;
+    stage("batch.block.long");
+  }
   bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(g, plist, witems, 0, b->counters,
                                                                        b->counters + 4, tags, b->gcounts);
+  stage("batch.warp");
   if (mixed && nrows > 0) {
     cudaMemsetAsync(b->counters_r, 0, sizeof(int) * 8, c);
-    group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->off, b->items_r, cap_items, b->counters_r, shr,
-                                                                b->vrows, 1);
+    group_items_compact_kernel<<<grid_for(n, 256), 256, 0, c>>>(g, b->off, b->items_r, cap_items, b->big_r,
+                                                                b->counters_r, shr, b->vrows, 1);
+    kernels += 3;
+    stage("batch.rows.items");
     bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_block, kBgWarps * 32, smem, c>>>(
         g, b->cols, bitems_r, 0, b->counters_r + 1, b->counters_r + 5, words, tags, b->gcounts);
+    stage("batch.rows.block");
+    if (any_big) {
+      bisson_block_kernel<CompactItems, kDefaultSlots><<<grid_big, kBgWarps * 32, smem_big, c>>>(
+          g, b->cols, litems_r, 0, b->counters_r + 2, b->counters_r + 6, words_big, tags, b->gcounts);
+      kernels += 1;
+      stage("batch.rows.block.long");
+    }
     bisson_warp_kernel<CompactItems, kDefaultSlots><<<grid_warp, kBgWarps * 32, 0, c>>>(
         g, b->cols, witems_r, 0, b->counters_r, b->counters_r + 4, tags, b->gcounts);
+    stage("batch.rows.warp");
   }
   cudaError_t launch_err = cudaGetLastError();
   cudaError_t end_err = cudaStreamEndCapture(c, &b->graph);
@@ -322,6 +392,7 @@ atc_status build_pipeline(atc_batch* b, const ItemShape& sh, cudaStream_t s) {
   }
   ATC_CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
   b->built_shape = sh;
+  b->launches = kernels;
   b->dirty = false;
   return ATC_OK;
 }
@@ -336,6 +407,13 @@ atc_status run_once(atc_batch* b, const ItemShape& sh, uint64_t* counts, float* 
   if (counts && ng) ATC_CK(cudaMemcpyAsync(counts, b->gcounts, sizeof(uint64_t) * ng, cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   if (ms) *ms = tm.ms();
+  if (phase_timing_on()) {
+    for (size_t k = 0; k < b->stage_name.size(); ++k) {
+      float t = 0.f;
+      ATC_CK(cudaEventElapsedTime(&t, b->stage_ev[k], b->stage_ev[k + 1]));
+      phase_add(b->stage_name[k], t);
+    }
+  }
   return ATC_OK;
 }
 
@@ -361,7 +439,7 @@ extern "C" atc_status atc_batch_run(atc_batch* b, const atc_tuning* t, uint64_t*
     stats->kernel_ms = ms;
     stats->total_ms = ms;
     stats->kernel_used = sh.by_source ? ATC_KERNEL_HU : ATC_KERNEL_BISSON;
-    stats->launches = 6;
+    stats->launches = b->launches;
   }
   return ATC_OK;
 } ATC_CATCH

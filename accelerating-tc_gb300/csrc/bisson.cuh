@@ -53,6 +53,9 @@ constexpr int kWarpChunk = 512;     // partners per warp item
 constexpr int kBlockChunk = 2048;   // partners per block item
 constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
 constexpr int kHashMax = kTabWords / 4;
+constexpr int kBlockSmallList = 2048;  // batches: block items of lists up to this length run in
+                                       // tables of at most 32 KB (six CTAs per SM), longer ones in
+                                       // a launch of their own with the 64 KB table (three)
 constexpr int kWarpGrab = 4;     // warp items taken per atomic
 constexpr int kDefaultSlots = 4;  // hash slots per bucket unless tuned (one 16-byte shared load)
 
@@ -207,16 +210,17 @@ struct CompactItems {
   const int2* p;
   const int64_t* gstart;
   int64_t cap;
-  bool from_back;  // block items
+  bool from_back;  // items stored from the back of p (the block items of lists up to kBlockSmallList)
+  bool block;      // block items
   ItemShape sh;
   __device__ __forceinline__ GroupItem get(const CsrView& g, int i) const {
     int2 c = from_back ? p[cap - 1 - i] : p[i];
     int64_t b0 = gstart[c.x], e0 = gstart[c.x + 1];
-    int64_t chunk = from_back ? sh.block_chunk : sh.warp_chunk;
+    int64_t chunk = block ? sh.block_chunk : sh.warp_chunk;
     int64_t b = b0 + (int64_t)c.y * chunk, e = min(e0, b + chunk);
     int64_t hb = g.off[c.x], dh = g.off[c.x + 1] - hb;
     int32_t mode;
-    if (!from_back) {
+    if (!block) {
       mode = dh <= sh.cutover ? 0 : 1;
     } else {
       int32_t span = g.cols[hb + dh - 1] - g.cols[hb];
@@ -234,12 +238,27 @@ struct CompactItems {
 // rule as the per-edge passes.  f(u, v, du, dv, valid) is called by all 32 lanes.
 // skip (nullable): rows u with skip[u] != 0 are passed over; a block of 32 such rows is not
 // read at all (the graphs of a batch are contiguous vertex ranges).
+// queue (nullable, zeroed): row blocks are handed out in order from this counter,
+// kRowGrab at a time, instead of by a grid stride.  Over a union of many graphs the warps
+// of a grid stride drift apart by many graphs' worth of rows, and the random reads of
+// degrees and group counters then spread over all of them; the queue keeps every warp
+// within a few graphs.
+constexpr int kRowGrab = 4;
 template <class F>
-__device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f, const uint8_t* skip = nullptr) {
+__device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f, const uint8_t* skip = nullptr,
+                                                    int* queue = nullptr) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t blocks = (g.n + 31) >> 5;
-  for (int64_t rb = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; rb < blocks; rb += warps) {
+  int64_t rb = queue ? 0 : (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5, lim = 0;
+  for (;; rb = queue ? rb + 1 : rb + warps) {
+    if (queue && rb >= lim) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(queue, kRowGrab);
+      rb = __shfl_sync(0xffffffffu, base, 0);
+      lim = rb + kRowGrab;
+    }
+    if (rb >= blocks) break;
     const int64_t u0 = rb << 5;
     const int64_t row = u0 + lane;
     const int64_t last = min(u0 + 32, g.n);
@@ -271,17 +290,17 @@ __device__ __forceinline__ void for_row_block_edges(const CsrView& g, F f, const
 }
 
 // skip (nullable): rows u with skip[u] != 0 are not grouped (their graph counts by rows).
-__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt, const uint8_t* skip) {
+__global__ void group_count_vc_kernel(CsrView g, int32_t* cnt, const uint8_t* skip, int* queue) {
   for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
     if (skip && ok) ok = !skip[u];
     const int32_t h = ok ? (longer_is_u(u, v, du, dv) ? u : v) : -1;
     const unsigned same = __match_any_sync(0xffffffffu, h);
     if (h >= 0 && (int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&cnt[h], __popc(same));
-  }, skip);
+  }, skip, queue);
 }
 
 __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist,
-                                        const uint8_t* skip) {
+                                        const uint8_t* skip, int* queue) {
   const int lane = threadIdx.x & 31;
   for_row_block_edges(g, [&](int32_t u, int32_t v, int64_t du, int64_t dv, bool ok) {
     if (skip && ok) ok = !skip[u];
@@ -297,14 +316,15 @@ __global__ void group_scatter_vc_kernel(CsrView g, const int64_t* gstart, int32_
     if (h >= 0 && lane == lead) at = atomicAdd(&cur[h], __popc(same));
     at = __shfl_sync(0xffffffffu, at, lead);
     if (h >= 0) plist[gstart[h] + at + __popc(same & ((1u << lane) - 1))] = p;
-  }, skip);
+  }, skip, queue);
 }
 
-// Compact items: counters[0] warp items (front), counters[1] block items (back),
-// counters[3] longest list among block items.  sel (nullable): only vertices h with
-// sel[h] == want get items.
-__global__ void group_items_compact_kernel(CsrView g, const int64_t* gstart, int2* items, int64_t cap, int* counters,
-                                           ItemShape sh, const uint8_t* sel, uint8_t want) {
+// Compact items: counters[0] warp items (front of `items`), counters[1] block items of lists
+// up to kBlockSmallList (back of `items`), counters[2] block items of longer lists (front of
+// `big`), counters[3] longest list among the block items in `items`.  sel (nullable): only
+// vertices h with sel[h] == want get items.
+__global__ void group_items_compact_kernel(CsrView g, const int64_t* gstart, int2* items, int64_t cap, int2* big,
+                                           int* counters, ItemShape sh, const uint8_t* sel, uint8_t want) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t n_pad = (g.n + 31) & ~31ll;
   for (int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; h < n_pad; h += stride) {
@@ -318,11 +338,16 @@ __global__ void group_items_compact_kernel(CsrView g, const int64_t* gstart, int
     const bool warp = dh <= sh.warp_max;
     const int kw = any && warp ? (int)((e - b + sh.warp_chunk - 1) / sh.warp_chunk) : 0;
     const int kb = any && !warp ? (int)((e - b + sh.block_chunk - 1) / sh.block_chunk) : 0;
+    const bool large = dh > kBlockSmallList;
     const int atw = warp_reserve(&counters[0], kw);
-    const int atb = warp_reserve(&counters[1], kb);
+    const int atb = warp_reserve(&counters[1], large ? 0 : kb);
+    const int atl = warp_reserve(&counters[2], large ? kb : 0);
     for (int c = 0; c < kw; ++c) items[(int64_t)atw + c] = make_int2((int32_t)h, c);
-    if (kb) atomicMax(&counters[3], (int)min(dh, (int64_t)kHashMax));
-    for (int c = 0; c < kb; ++c) items[cap - 1 - ((int64_t)atb + c)] = make_int2((int32_t)h, c);
+    if (kb && !large) atomicMax(&counters[3], (int)dh);
+    for (int c = 0; c < kb; ++c) {
+      if (large) big[(int64_t)atl + c] = make_int2((int32_t)h, c);
+      else items[cap - 1 - ((int64_t)atb + c)] = make_int2((int32_t)h, c);
+    }
   }
 }
 

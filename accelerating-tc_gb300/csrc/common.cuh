@@ -68,6 +68,12 @@ int sm_count();
 // Unlimited unless a budget was set.
 bool alloc_budget_take(size_t bytes);
 
+// Phase timing on for the calling thread (atc_phase_timing).
+bool phase_timing_on();
+// Records a phase whose device time was measured elsewhere (stages of a CUDA-graph replay,
+// timed by event nodes inside the graph), nested in the phases open on the calling thread.
+void phase_add(const char* name, float ms);
+
 // A named phase of a call: an NVTX range (visible to Nsight tools and ncu's NVTX filters)
 // and, when phase timing is on for the calling thread (atc_phase_timing), a pair of CUDA
 // events on the phase's stream, read back by atc_phase_times.  Phases nest; a phase is

@@ -597,6 +597,7 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
     plain_dev = [[] for _ in kfixed]  # device time of the counting kernels of each call
     plain_counts = []
     dirs = []
+    gstats = []  # (m, W, sum of min) of every graph as added
     wmin_adir = wmin_sel = 0
     # the per-graph calls are timed with L2 flushed before each (a graph counted right after
     # it was built or warmed would otherwise be read from L2, which a pass over many graphs,
@@ -626,6 +627,7 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
             if alt.wedges_min < csr.wedges_min:
                 chosen, dsel = alt, "degree"
         wmin_sel += chosen.wedges_min
+        gstats.append((chosen.m, chosen.wedges, chosen.wedges_min))
         dirs.append(dsel)
         batch.add(chosen, stream=sp)
         csr.free()
@@ -646,7 +648,26 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
         _, st = batch.run(stream=sp)
         times.append(st.kernel_ms)
     batch_ms = statistics.mean(times)
+    # the replay's stages, from the event nodes between them
+    atc.phase_timing(True)
+    try:
+        batch.run(stream=sp)
+        stages = {name: round(ms, 3) for name, _, ms in atc.phase_times() if name.startswith("batch.")}
+    finally:
+        atc.phase_timing(False)
     batch.free()
+    # the batch's per-graph item mode (group_by_source = 2) by the library's cost model, and the
+    # per-graph device times of the matching kernels, for the stages of the replay to be read against
+    split = None
+    names = [kf.name.lower() for kf in kfixed]
+    if "hu" in names and "bisson" in names:
+        hu_dev, bi_dev = plain_dev[names.index("hu")], plain_dev[names.index("bisson")]
+        rows = [1.097 * w + 103.5 * m < 1.232 * wm + 117.5 * m for m, w, wm in gstats]
+        split = {"rows_graphs": int(sum(rows)), "rows_edges": int(sum(g[0] for g, r in zip(gstats, rows) if r)),
+                 "hu_device_ms_rows_graphs": float(sum(t for t, r in zip(hu_dev, rows) if r)),
+                 "bisson_device_ms_grouped_graphs": float(sum(t for t, r in zip(bi_dev, rows) if not r)),
+                 "bisson_device_ms_rows_graphs": float(sum(t for t, r in zip(bi_dev, rows) if r)),
+                 "hu_device_ms_grouped_graphs": float(sum(t for t, r in zip(hu_dev, rows) if not r))}
     return {
         "metric": "graphs/s, batched (one CUDA-graph replay, autotuned items) vs per-graph loop",
         "unit": "graphs/s", "dtype": "int32", "data": "synthetic Chung-Lu graphs generated on the device",
@@ -658,11 +679,12 @@ def batch_leg(a, indices, plain_kernels, sp, stream=None, candidates=None):
                                     "edges_per_s": m_all / (sum(ms) * 1e-3), "device_ms_total": sum(dv)}
                   for kf, ms, dv in zip(kfixed, plain_ms, plain_dev)},
         "plain_device_best_of_kernels_ms": float(sum(min(x) for x in zip(*plain_dev))) if plain_dev else None,
+        "mode_split": split,
         "plain_note": "atc_tc per graph on its resident A-direction CSR, host-synchronised per call, L2 flushed "
                       "(256 MB written) before each timed call",
         "batched": {"ms_per_replay": batch_ms, "graphs_per_s": ng / (batch_ms * 1e-3),
                     "edges_per_s": m_all / (batch_ms * 1e-3), "tuned": cands[best],
-                    "tune_ms": [float(x) for x in tune_ms],
+                    "tune_ms": [float(x) for x in tune_ms], "stages_ms": stages,
                     "selection": "work estimate" if getattr(a, "batch_select", False) else "none",
                     "degree_chosen": dirs.count("degree"), "wedges_min_adirection": wmin_adir,
                     "wedges_min_selected": wmin_sel},

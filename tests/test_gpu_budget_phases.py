@@ -100,3 +100,33 @@ def test_phase_times_nest_and_add_up():
             j += 1
         assert child <= ms * 1.05 + 0.05, (name, ms, child)
         i = j
+
+
+@pytest.mark.parametrize("tuning", [None, {"group_by_source": 1}, {"group_by_source": 2}])
+def test_batch_replay_stages(tuning):
+    """The stages of a batch replay are timed by event nodes inside its CUDA graph and
+    recorded under the call's phase; they fit inside it and the counts stay exact."""
+    graphs = [atc.rmat_graph(9 + i % 4, 8, 20 + i) for i in range(8)]
+    want = [oracle.tc_count(g) for g in graphs]
+    b = atc.Batch()
+    for g in graphs:
+        csr = atc.pretc(g, atc.Dir.ADIRECTION)
+        b.add(csr)
+        csr.free()
+    atc.phase_timing(True)
+    try:
+        got, st = b.run(tuning=tuning)
+        ph = atc.phase_times()
+    finally:
+        atc.phase_timing(False)
+    b.free()
+    assert [int(x) for x in got] == want
+    assert ph[0][0] == "batch" and ph[0][1] == 0, ph
+    stages = ph[1:]
+    names = [n for n, _, _ in stages]
+    assert all(d == 1 for _, d, _ in stages), ph
+    assert names[0] == "batch.reset" and "batch.items" in names and "batch.block" in names and "batch.warp" in names
+    assert ("batch.group" in names) == (tuning is None or tuning["group_by_source"] != 1)
+    assert all(ms >= 0 for _, _, ms in stages)
+    assert sum(ms for _, _, ms in stages) <= ph[0][2] * 1.05 + 0.05
+    assert st.launches >= 3
