@@ -50,6 +50,8 @@ class Order(enum.IntEnum):
     AORDER_V2 = 3
     GRO = 4
     ADIRECTION_BISSON = 5
+    NAIVE_SHUFFLED = 6
+    RANDOM = 7
 
 
 class Relabel(enum.IntEnum):
@@ -58,6 +60,9 @@ class Relabel(enum.IntEnum):
     OUTDEG_DESC = 2
     GRO = 3
     ADIRECTION_BISSON = 4
+    NAIVE_SHUFFLED = 5
+    OUTDEG_SHUFFLED = 6
+    RANDOM = 7
 
 
 class Kernel(enum.IntEnum):
@@ -644,7 +649,8 @@ def adirection_par(edges_u64, compat=False, stream=None):
 
 
 def relabel(pairs, kind, stream=None):
-    """(lookup, normal, relabeled) as A-order-v2 / relabel-naive / relabel4lpOut compute them."""
+    """(lookup, normal, relabeled) as A-order-v2 / relabel-naive / relabel4lpOut /
+    relabel-random / GRO / Bisson's A-direction compute them (atc_relabel_kind)."""
     p = _pairs(pairs)
     n_v = int(p.max()) + 1 if p.size else 1
     lookup = np.empty(n_v, dtype=np.int32)

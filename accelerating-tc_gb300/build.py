@@ -41,6 +41,9 @@ CLI_PROGRAMS = {
     "a_order": "order_main.cpp",
     "bisson_a_direction": "order_main.cpp",
     "a_order_v2": "order_main.cpp",
+    "relabel_naive": "order_main.cpp",
+    "relabel4lp_out": "order_main.cpp",
+    "relabel_random": "order_main.cpp",
     "kcl": "kcl_main.cpp",
     "cost_func_cal": "order_main.cpp",
     "kcore_direction": "order_main.cpp",

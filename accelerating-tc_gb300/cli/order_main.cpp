@@ -9,6 +9,13 @@
 //        writes normal and reordered in the working directory
 //   a_order_v2 <edges.bin>           vertex_ordering/A-order/A-order-v2.cpp:14-193
 //        writes naive (and the empty degreeOrder) in the working directory
+//   relabel_naive <edges.bin>        vertex_ordering/A-order/relabel-naive.cpp:14-193
+//        writes naive (the shuffled 64-column mix) and degreeOrder
+//   relabel4lp_out <edges.txt>       vertex_ordering/A-order/relabel4lpOut.cpp:13-151 ("src dst"
+//        text lines, e.g. A-direction-seri's lpBasedGraph); writes normal, bad and good
+//   relabel_random <edges.bin>       vertex_ordering/A-order/relabel-random.cpp:13-124
+//        writes normal, bad (every id shuffled) and good; prints the runtime degree of the
+//        vertex at each position of the shuffle but the last
 //   cost_func_cal <edges.bin> <k>    tools/costFuncCal.cpp:15-95 (prints the three costs)
 //   Peel <in> <out> [--compat]       edge_directing/A-direction-parallel/peel.cu:130-317 (uint64
 //        edges, src = x >> 32; --compat keeps the program's minor-priority term, peel.cu:49)
@@ -46,6 +53,19 @@ static bool read_pairs(const char* path, std::vector<int32_t>& pairs) {
   return got == n;
 }
 
+// "src dst" text lines, read until the first line that does not parse (relabel4lpOut.cpp:20)
+static bool read_text_pairs(const char* path, std::vector<int32_t>& pairs) {
+  FILE* f = fopen(path, "r");
+  if (!f) return false;
+  int a = 0, b = 0;
+  while (fscanf(f, "%d %d", &a, &b) == 2) {
+    pairs.push_back(a);
+    pairs.push_back(b);
+  }
+  fclose(f);
+  return true;
+}
+
 static bool write_pairs(const char* path, const int32_t* p, size_t n) {
   FILE* f = fopen(path, "wb");
   if (!f) return false;
@@ -67,6 +87,9 @@ static const int kMinArgc = 3;
 #elif defined(ATC_PROGRAM_REORDER)
 static const char* const kArgs = "<graph.u64>";
 static const int kMinArgc = 2;
+#elif defined(ATC_PROGRAM_RELABEL4LP_OUT)
+static const char* const kArgs = "<edges.txt>";
+static const int kMinArgc = 2;
 #else
 static const char* const kArgs = "<edges.bin>";
 static const int kMinArgc = 2;
@@ -75,7 +98,12 @@ static const int kMinArgc = 2;
 int main(int argc, char** argv) {
   if (argc < kMinArgc) { fprintf(stderr, "usage: %s %s\n", argv[0], kArgs); return 2; }
   std::vector<int32_t> pairs;
-  if (!read_pairs(argv[1], pairs)) { fprintf(stderr, "cannot read %s\n", argv[1]); return 1; }
+#if defined(ATC_PROGRAM_RELABEL4LP_OUT)
+  const bool read_ok = read_text_pairs(argv[1], pairs);
+#else
+  const bool read_ok = read_pairs(argv[1], pairs);
+#endif
+  if (!read_ok) { fprintf(stderr, "cannot read %s\n", argv[1]); return 1; }
   uint64_t np = pairs.size() / 2;
   atc_status s = atc_init(0);
   if (s != ATC_OK) return fail("atc_init", s);
@@ -121,6 +149,41 @@ int main(int argc, char** argv) {
   s = atc_relabel(pairs.data(), np, ATC_RELABEL_AORDER_V2, lookup.data(), nullptr, naive.data(), nullptr);
   if (s != ATC_OK) return fail("atc_relabel", s);
   if (!write_pairs("naive", naive.data(), np) || !write_pairs("degreeOrder", naive.data(), 0)) return 1;
+#elif defined(ATC_PROGRAM_RELABEL_NAIVE) || defined(ATC_PROGRAM_RELABEL4LP_OUT) || defined(ATC_PROGRAM_RELABEL_RANDOM)
+#if defined(ATC_PROGRAM_RELABEL_NAIVE)
+  const atc_relabel_kind good_kind = ATC_RELABEL_DEGREE_DESC, bad_kind = ATC_RELABEL_NAIVE_SHUFFLED;
+#elif defined(ATC_PROGRAM_RELABEL4LP_OUT)
+  const atc_relabel_kind good_kind = ATC_RELABEL_OUTDEG_DESC, bad_kind = ATC_RELABEL_OUTDEG_SHUFFLED;
+#else
+  const atc_relabel_kind good_kind = ATC_RELABEL_DEGREE_DESC, bad_kind = ATC_RELABEL_RANDOM;
+#endif
+  int32_t mx = 0;
+  for (int32_t x : pairs) mx = x > mx ? x : mx;
+  const size_t nv = (size_t)mx + 1;
+  std::vector<int32_t> good_lookup(nv), bad_lookup(nv), normal(pairs.size() + 2), good(pairs.size() + 2),
+      bad(pairs.size() + 2);
+  s = atc_relabel(pairs.data(), np, good_kind, good_lookup.data(), nullptr, good.data(), nullptr);
+  if (s != ATC_OK) return fail("atc_relabel", s);
+  s = atc_relabel(pairs.data(), np, bad_kind, bad_lookup.data(), normal.data(), bad.data(), nullptr);
+  if (s != ATC_OK) return fail("atc_relabel", s);
+  // the runtime degree: out-degree of the (oriented) pairs
+  std::vector<int32_t> rt(nv, 0);
+  for (uint64_t i = 0; i < np; ++i) rt[normal[2 * i]]++;
+  std::cout << "the max runtime degree is " << *std::max_element(rt.begin(), rt.end()) << std::endl;
+#if defined(ATC_PROGRAM_RELABEL_NAIVE)
+  std::cout << "the reorder time is 0 s." << std::endl;
+  if (!write_pairs("naive", bad.data(), np) || !write_pairs("degreeOrder", good.data(), np)) return 1;
+#else
+#if defined(ATC_PROGRAM_RELABEL_RANDOM)
+  std::vector<int32_t> at(nv);  // the vertex at each position of the shuffle
+  for (size_t v = 0; v < nv; ++v) at[bad_lookup[v]] = (int32_t)v;
+  for (size_t i = 0; i + 1 < nv; ++i) std::cout << rt[at[i]] << "\n";
+  std::cout.flush();
+#endif
+  if (!write_pairs("normal", normal.data(), np) || !write_pairs("bad", bad.data(), np) ||
+      !write_pairs("good", good.data(), np))
+    return 1;
+#endif
 #elif defined(ATC_PROGRAM_COST_FUNC_CAL)
   float c[3];
   s = atc_costfunc(pairs.data(), np, atoi(argv[2]), c, nullptr);

@@ -192,6 +192,31 @@ __global__ void rank_lookup_kernel(const uint64_t* sorted, int B, int64_t n, int
   }
 }
 
+// The shuffled relabellings' deal (relabel-naive.cpp:102-150 with mix = 64,
+// relabel4lpOut.cpp:82-110 with mix = 40): entry q of the descending list goes to position
+// i + mix*j of column i = q / chunk (chunk = n / mix), j = q mod chunk in the even columns
+// and chunk-1 - (q mod chunk) in the odd ones, which are read backwards; entries from
+// mix*chunk on keep their place.  dealt[position] = id.
+__global__ void mix_deal_kernel(const uint64_t* sorted, int B, int64_t n, int mix, int32_t* dealt) {
+  const uint64_t mask = (1ull << B) - 1;
+  const int64_t chunk = n / mix;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = n - 1 - r;
+    int64_t pos = q;
+    if (q < mix * chunk) {
+      const int64_t i = q / chunk, jj = q - i * chunk;
+      pos = i + mix * ((i & 1) ? chunk - 1 - jj : jj);
+    }
+    dealt[pos] = (int32_t)(sorted[r] & mask);
+  }
+}
+
+// inv[perm[p]] = p (badLookUpTable, relabel-naive.cpp:154-158)
+__global__ void inverse_kernel(const int32_t* perm, int64_t n, int32_t* inv) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    inv[perm[p]] = (int32_t)p;
+}
+
 __global__ void rt_hist_kernel(const int32_t* rt, int64_t n, int32_t* hist, int* maxrt) {
   int best = 0;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -332,14 +357,15 @@ void bucket_heap(const std::vector<int64_t>& hist, int maxrt, int64_t S, int64_t
 atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int kind,
                           int32_t* lookup, int2* oriented, cudaStream_t s) {
   if (n_v <= 0) return ATC_OK;
-  ATC_CHECK_ARG(kind != ATC_RELABEL_OUTDEG_DESC || pairs != nullptr, "OUTDEG_DESC needs pairs");
+  const bool as_given = kind == ATC_RELABEL_OUTDEG_DESC || kind == ATC_RELABEL_OUTDEG_SHUFFLED;
+  ATC_CHECK_ARG(!as_given || pairs != nullptr, "OUTDEG_DESC / OUTDEG_SHUFFLED need pairs");
   DevBuf<int32_t> deg, rt;
   DevBuf<int> mx;
   ATC_TRY(rt.alloc(n_v, s));
   ATC_TRY(mx.alloc(1, s));
   ATC_CK(cudaMemsetAsync(rt.p, 0, sizeof(int32_t) * n_v, s));
   ATC_CK(cudaMemsetAsync(mx.p, 0, sizeof(int), s));
-  if (ne && kind == ATC_RELABEL_OUTDEG_DESC) {
+  if (ne && as_given) {
     outdeg_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, ne, rt.p, oriented);
   } else if (ne) {
     ATC_TRY(deg.alloc(n_v, s));
@@ -350,6 +376,14 @@ atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uin
     rt_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, keys, bits, ne, deg.p, rt.p, oriented);
   }
   ATC_CK(cudaGetLastError());
+  if (kind == ATC_RELABEL_RANDOM) {  // the degree list plays no part (relabel-random.cpp:77-89)
+    DevBuf<int32_t> perm;
+    ATC_TRY(perm.alloc(n_v, s));
+    ATC_TRY(shuffle_ids(perm.p, n_v, s));
+    inverse_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(perm.p, n_v, lookup);
+    ATC_CK(cudaGetLastError());
+    return ATC_OK;
+  }
   rt_hist_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(rt.p, n_v, nullptr, mx.p);
   ATC_CK(cudaGetLastError());
   int maxrt = 0;
@@ -364,6 +398,17 @@ atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uin
   uint64_t* a = ka.p;
   uint64_t* b = kb.p;
   ATC_TRY(sort_keys_u64(a, b, n_v, 0, B + rb, s));
+  if (kind == ATC_RELABEL_NAIVE_SHUFFLED || kind == ATC_RELABEL_OUTDEG_SHUFFLED) {
+    const int mix = kind == ATC_RELABEL_NAIVE_SHUFFLED ? 64 : 40;
+    DevBuf<int32_t> dealt;
+    ATC_TRY(dealt.alloc(n_v, s));
+    mix_deal_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(a, B, n_v, mix, dealt.p);
+    ATC_CK(cudaGetLastError());
+    ATC_TRY(shuffle_blocks(dealt.p, n_v / mix, mix, s));
+    inverse_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(dealt.p, n_v, lookup);
+    ATC_CK(cudaGetLastError());
+    return ATC_OK;
+  }
   rank_lookup_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(a, B, n_v, kind, lookup);
   ATC_CK(cudaGetLastError());
   return ATC_OK;
@@ -523,7 +568,7 @@ extern "C" atc_status atc_relabel(const int32_t* pairs, uint64_t np, atc_relabel
                                   int32_t* normal, int32_t* relabeled, atc_stream st) try {
   ATC_CHECK_ARG(lookup != nullptr, "lookup is NULL");
   ATC_CHECK_ARG(np == 0 || pairs != nullptr, "pairs is NULL");
-  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_ADIRECTION_BISSON, "unknown atc_relabel_kind");
+  ATC_CHECK_ARG(kind >= ATC_RELABEL_DEGREE_DESC && kind <= ATC_RELABEL_RANDOM, "unknown atc_relabel_kind");
   cudaStream_t s = as_stream(st);
   int maxid = 0;  // the programs start maxNodeId at 0, so an empty list has one vertex
   for (uint64_t i = 0; i < 2 * np; ++i) {

@@ -82,6 +82,16 @@ atc_status aorder_lookup(const int2* pairs, const uint64_t* keys, int bits, uint
 atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uint64_t ne, int64_t n_v, int kind,
                           int32_t* lookup, int2* oriented, cudaStream_t s);
 
+// The C library's rand() stream in its seed-1 state and std::random_shuffle over it
+// (csrc/shuffle.cu).  rand_stream: out[k] = the value of call k, k < count (device).
+// shuffle_blocks: random_shuffle of each block [b*width, (b+1)*width) of a, b < nblocks, in
+// block order, one stream (width <= kMaxShuffleWidth).  shuffle_ids: out[p] = the id at
+// position p after random_shuffle of the ids 0..n-1.
+constexpr int kMaxShuffleWidth = 64;
+atc_status rand_stream(uint32_t* out, int64_t count, cudaStream_t s);
+atc_status shuffle_blocks(int32_t* a, int64_t nblocks, int width, cudaStream_t s);
+atc_status shuffle_ids(int32_t* out, int64_t n, cudaStream_t s);
+
 // Edge range [range[0], range[1]) of part `part` of `nparts` contiguous ranges of equal work
 // (sum over the edges of min(outdeg u, outdeg v) + 1) of a CSR built by the library.
 atc_status part_edge_range(const atc_csr* csr, uint32_t part, uint32_t nparts, int64_t* range, cudaStream_t s);

@@ -334,7 +334,7 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
                              atc_csr* out, int32_t* perm_out, cudaStream_t s) {
   ATC_CHECK_ARG(out != nullptr, "out is NULL");
   ATC_CHECK_ARG(dir >= ATC_DIR_ID && dir <= ATC_DIR_ADIRECTION_PAR, "unknown atc_dir");
-  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_ADIRECTION_BISSON, "unknown atc_order");
+  ATC_CHECK_ARG(order >= ATC_ORDER_NONE && order <= ATC_ORDER_RANDOM, "unknown atc_order");
   *out = atc_csr{};
   bool prune = t && t->prune_deg1;
   SimpleEdges e;
@@ -392,10 +392,13 @@ static atc_status pretc_impl(const int2* pairs, uint64_t np, atc_dir dir, atc_or
         ATC_CK(cudaGetLastError());
       }
       ATC_TRY(gro_lookup(sym.p, 2 * (uint64_t)e.m, n_v, perm.p, s));
-    } else
-      ATC_TRY(relabel_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v,
-                             order == ATC_ORDER_DEGREE_DESC ? ATC_RELABEL_DEGREE_DESC : ATC_RELABEL_AORDER_V2, perm.p,
-                             nullptr, s));
+    } else {
+      const int kind = order == ATC_ORDER_DEGREE_DESC    ? ATC_RELABEL_DEGREE_DESC
+                       : order == ATC_ORDER_AORDER_V2    ? ATC_RELABEL_AORDER_V2
+                       : order == ATC_ORDER_NAIVE_SHUFFLED ? ATC_RELABEL_NAIVE_SHUFFLED
+                                                           : ATC_RELABEL_RANDOM;
+      ATC_TRY(relabel_lookup(nullptr, e.keys.p, e.bits, (uint64_t)e.m, n_v, kind, perm.p, nullptr, s));
+    }
     ph.reset();
   }
   ph.emplace("pretc.direction", s);

@@ -75,7 +75,11 @@ typedef enum atc_order {
   /* Bisson's A-direction relabelling of the simple graph (Bisson/A-direction.cpp,
      ATC_RELABEL_ADIRECTION_BISSON); with ATC_DIR_ID it is the program's A-direction
      pipeline for Bisson and Fox */
-  ATC_ORDER_ADIRECTION_BISSON = 5
+  ATC_ORDER_ADIRECTION_BISSON = 5,
+  /* relabel-naive's shuffled 64-column mix of the DEGREE_DESC list (ATC_RELABEL_NAIVE_SHUFFLED) */
+  ATC_ORDER_NAIVE_SHUFFLED = 6,
+  /* relabel-random's random relabelling (ATC_RELABEL_RANDOM) */
+  ATC_ORDER_RANDOM = 7
 } atc_order;
 
 /* Rank relabellings of vertex_ordering/A-order (atc_relabel). */
@@ -101,7 +105,20 @@ typedef enum atc_relabel_kind {
      program's position-indexed degreeRecord (:118) reproduced.  Counting the relabelled
      graph with ATC_DIR_ID realises the A-direction orientation as an id order, which is
      how the program feeds Bisson's kernel.  `normal` = the pairs as given. */
-  ATC_RELABEL_ADIRECTION_BISSON = 4
+  ATC_RELABEL_ADIRECTION_BISSON = 4,
+  /* relabel-naive's "naive" (vertex_ordering/A-order/relabel-naive.cpp:77-177): the
+     DEGREE_DESC list dealt into 64 columns of chunk = n/64 positions (position i + 64 j of
+     column i takes entry i*chunk + j; odd columns are read backwards), then every block of
+     64 positions shuffled by std::random_shuffle with the C library's rand() in its seed-1
+     state (the program never seeds it); the last n % 64 positions keep the list's order. */
+  ATC_RELABEL_NAIVE_SHUFFLED = 5,
+  /* relabel4lpOut's "bad" (relabel4lpOut.cpp:57-136): the OUTDEG_DESC list dealt into 40
+     columns the same way and its blocks of 40 shuffled; `normal` = the pairs as given. */
+  ATC_RELABEL_OUTDEG_SHUFFLED = 6,
+  /* relabel-random's "bad" (relabel-random.cpp:76-108): std::random_shuffle of the ids
+     0..max with the C library's rand() in its seed-1 state; `normal` = the degree-oriented
+     pairs, as for DEGREE_DESC. */
+  ATC_RELABEL_RANDOM = 7
 } atc_relabel_kind;
 
 typedef enum atc_kernel {

@@ -20,6 +20,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <iterator>
 #include <thread>
@@ -1023,43 +1024,74 @@ void orc_adirection_par(const uint64_t* edges, uint64_t ne, int compat, uint64_t
   if (iterations) *iterations = (int32_t)it;
 }
 
+// std::random_shuffle(first, first + len) as libstdc++ writes it (bits/stl_algo.h): for
+// i = 1 .. len-1, swap a[i] with a[rand() % (i + 1)], rand() being the C library's.
+static void orc_random_shuffle(int* a, int64_t len) {
+  for (int64_t i = 1; i < len; ++i) {
+    const int64_t j = std::rand() % (i + 1);
+    if (i != j) std::swap(a[i], a[j]);
+  }
+}
+
 // Rank relabellings of vertex_ordering/A-order: kind 0 = "good" of relabel-naive.cpp /
 // relabel-random.cpp (:29-74), kind 1 = "naive" of A-order-v2.cpp (:29-160), kind 2 =
-// "good" of relabel4lpOut.cpp (:27-54, out-degree as given).  Degrees count repeats;
-// the degree orientation flips a pair when src has the larger degree or equal degree and
-// the smaller id.  lookup: maxNodeId + 1 ints (maxNodeId starts at 0); normal: np pairs.
+// "good" of relabel4lpOut.cpp (:27-54, out-degree as given), kind 5 = "naive" of
+// relabel-naive.cpp (:77-177: 64 columns, odd ones backwards, blocks of 64 shuffled),
+// kind 6 = "bad" of relabel4lpOut.cpp (:57-136: the same with 40 and out-degree as given),
+// kind 7 = "bad" of relabel-random.cpp (:76-108: every id shuffled).  The shuffles use the
+// C library's rand() from its seed-1 state (srand(1) here; the programs never seed it).
+// Degrees count repeats; the degree orientation flips a pair when src has the larger
+// degree or equal degree and the smaller id.  lookup: maxNodeId + 1 ints (maxNodeId starts
+// at 0); normal: np pairs.
 void orc_relabel(const int32_t* pairs, uint64_t np, int kind, int32_t* lookup, int32_t* normal) {
   int max_node = 0;
   for (uint64_t i = 0; i < 2 * np; ++i) max_node = std::max(max_node, pairs[i]);
   const int n = max_node + 1;
+  const bool as_given = kind == 2 || kind == 6;
   std::vector<int> degree(n, 0), rt(n, 0);
   for (uint64_t i = 0; i < np; ++i) {
     degree[pairs[2 * i]]++;
-    if (kind != 2) degree[pairs[2 * i + 1]]++;
+    if (!as_given) degree[pairs[2 * i + 1]]++;
   }
   for (uint64_t i = 0; i < np; ++i) {
     int src = pairs[2 * i], dst = pairs[2 * i + 1];
-    if (kind != 2 && (degree[src] > degree[dst] || (degree[src] == degree[dst] && src < dst))) std::swap(src, dst);
+    if (!as_given && (degree[src] > degree[dst] || (degree[src] == degree[dst] && src < dst))) std::swap(src, dst);
     normal[2 * i] = src;
     normal[2 * i + 1] = dst;
     rt[src]++;
   }
-  if (kind == 2) rt = degree;
+  if (as_given) rt = degree;
+  if (kind == 7) {
+    std::vector<int> bad(n);
+    for (int i = 0; i < n; ++i) bad[i] = i;
+    std::srand(1);
+    orc_random_shuffle(bad.data(), n);
+    for (int i = 0; i < n; ++i) lookup[bad[i]] = i;
+    return;
+  }
   int max_rt = 0;
   for (int v = 0; v < n; ++v) max_rt = std::max(max_rt, rt[v]);
   std::vector<std::vector<int>> bucket(max_rt + 1);
   for (int v = 0; v < n; ++v) bucket[rt[v]].push_back(v);
   std::vector<int> order;  // ascending (rt, id)
   for (int r = 0; r <= max_rt; ++r) order.insert(order.end(), bucket[r].begin(), bucket[r].end());
-  if (kind != 1) {
+  if (kind == 0 || kind == 2) {
     for (int i = 0; i < n; ++i) lookup[order[i]] = n - 1 - i;
     return;
   }
   std::reverse(order.begin(), order.end());
-  const int mix = 40, chunk = n / mix;
+  const bool shuffled = kind == 5 || kind == 6;
+  const int mix = kind == 5 ? 64 : 40, chunk = n / mix;
   std::vector<int> distri(n, 0);
-  for (int i = 0; i < mix; ++i)
-    for (int j = 0; j < chunk; ++j) distri[i + j * mix] = order[i * chunk + j];
+  for (int i = 0; i < mix; ++i) {
+    const bool backwards = shuffled && (i & 1);
+    for (int j = 0; j < chunk; ++j)
+      distri[i + j * mix] = backwards ? order[(i + 1) * chunk - 1 - j] : order[i * chunk + j];
+  }
+  if (shuffled) {
+    std::srand(1);
+    for (int i = 0; i < chunk; ++i) orc_random_shuffle(distri.data() + (int64_t)i * mix, mix);
+  }
   for (int i = n - n % mix; i < n; ++i) distri[i] = order[i];
   for (int i = 0; i < n; ++i) lookup[distri[i]] = i;
 }

@@ -203,7 +203,8 @@ def core_numbers(pairs):
 
 
 def relabel(pairs, kind):
-    """(lookup, normal, relabeled) of A-order-v2 / relabel-naive / relabel4lpOut."""
+    """(lookup, normal, relabeled) of A-order-v2 / relabel-naive / relabel4lpOut /
+    relabel-random (kinds as atc_relabel_kind: 0, 1, 2, 5, 6, 7)."""
     p = _pairs(pairs)
     n = int(p.max()) + 1 if p.size else 1
     lookup = np.empty(n, dtype=np.int32)

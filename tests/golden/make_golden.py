@@ -12,7 +12,10 @@ case the script records what the reference programs output:
   aorder_raw   A-order E.bin                 -> normal / reordered on the raw input
   aorder_v2    A-order-v2 lpBasedGraph.bin   -> naive (the 40-column mix, relabelled)
   relabel_good relabel-naive lpBasedGraph.bin -> degreeOrder (descending runtime degree)
+  relabel_naive relabel-naive lpBasedGraph.bin -> naive (64 columns, blocks of 64 shuffled)
   relabel4lp   relabel4lpOut lpBasedGraph   -> good (descending out-degree as given; text input)
+  relabel4lp_bad relabel4lpOut lpBasedGraph -> bad (40 columns, blocks of 40 shuffled)
+  relabel_random relabel-random lpBasedGraph.bin -> bad (every id shuffled)
   costfunc     costFuncCal lpBasedGraph.bin k -> three printed floats, k = 1, 2
   verification verification lpBasedGraph    -> two printed floats (text input)
   triangles    OrgTriangleCount on E symmetrised (x86 only; int result, small graphs)
@@ -148,9 +151,14 @@ def case(name, pairs):
         r = run([os.path.join(REF, "relabel-naive"), lpb], d)
         assert r.returncode == 0, r.stdout
         out["relabel_good"] = record(read_pairs(os.path.join(d, "degreeOrder")))
+        out["relabel_naive"] = record(read_pairs(os.path.join(d, "naive")))
         r = run([os.path.join(REF, "relabel4lpOut"), os.path.join(d, "lpBasedGraph")], d)
         assert r.returncode == 0, r.stdout
         out["relabel4lp"] = record(read_pairs(os.path.join(d, "good")))
+        out["relabel4lp_bad"] = record(read_pairs(os.path.join(d, "bad")))
+        r = run([os.path.join(REF, "relabel-random"), lpb], d)
+        assert r.returncode == 0, r.stdout
+        out["relabel_random"] = record(read_pairs(os.path.join(d, "bad")))
 
         cf = {}
         for k in (1, 2):

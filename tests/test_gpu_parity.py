@@ -97,7 +97,10 @@ def test_aorder_matches_reference(golden, name, which):
 
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("which,kind", [("aorder_v2", atc.Relabel.AORDER_V2), ("relabel_good", atc.Relabel.DEGREE_DESC),
-                                        ("relabel4lp", atc.Relabel.OUTDEG_DESC)])
+                                        ("relabel4lp", atc.Relabel.OUTDEG_DESC),
+                                        ("relabel_naive", atc.Relabel.NAIVE_SHUFFLED),
+                                        ("relabel4lp_bad", atc.Relabel.OUTDEG_SHUFFLED),
+                                        ("relabel_random", atc.Relabel.RANDOM)])
 def test_relabel_matches_reference(golden, name, which, kind):
     c = golden["cases"][name]
     src = oracle.adirection(golden_input(c))
@@ -105,6 +108,30 @@ def test_relabel_matches_reference(golden, name, which, kind):
     assert rel.shape[0] == c[which]["count"] and sha(rel) == c[which]["sha256"]
     olookup, onormal, _ = oracle.relabel(src, kind)
     assert np.array_equal(lookup, olookup) and np.array_equal(normal, onormal)
+
+
+@pytest.mark.parametrize("kind", [atc.Relabel.NAIVE_SHUFFLED, atc.Relabel.OUTDEG_SHUFFLED, atc.Relabel.RANDOM])
+def test_shuffled_relabellings_at_scale(kind):
+    """The device's rand() stream (every thread jumping ahead to its own stretch) and its
+    replay of the shuffles against the oracle, which calls the C library's rand(), on R-MAT
+    scale 20 (a million ids: about 500 stretches of the stream) and on an id range with a
+    ragged tail (n mod 64 and n mod 40 both non-zero)."""
+    for g in (atc.rmat_graph(20, 16, 1), np.array([(0, 1), (1, 2), (2, 0), (5, 1234566)], dtype=np.int32)):
+        src = oracle.adirection(g) if g.shape[0] > 4 else g
+        lookup, normal, rel = atc.relabel(src, kind)
+        olookup, onormal, orel = oracle.relabel(src, int(kind))
+        assert np.array_equal(lookup, olookup) and np.array_equal(normal, onormal) and np.array_equal(rel, orel)
+        assert np.array_equal(np.sort(lookup), np.arange(lookup.size))
+
+
+@pytest.mark.parametrize("order", [atc.Order.NAIVE_SHUFFLED, atc.Order.RANDOM])
+def test_pretc_shuffled_orders_count_exactly(order):
+    g = atc.rmat_graph(14, 16, 3)
+    csr = atc.pretc(g, atc.Dir.ADIRECTION, order)
+    want = oracle.tc_count(g)
+    for k in (atc.Kernel.HU, atc.Kernel.BISSON, atc.Kernel.FOX, atc.Kernel.TRICORE):
+        assert atc.tc(csr, k)[0] == want, k
+    csr.free()
 
 
 def pack_u64(pairs):
@@ -434,6 +461,30 @@ def test_cli_dropins(tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert np.array_equal(np.fromfile(tmp_path / "naive", dtype=np.int32).reshape(-1, 2), oracle.relabel(lp, 1)[2])
+    # the shuffled relabellings: relabel-naive, relabel4lpOut (text input), relabel-random
+    def pairs_file(name):
+        return np.fromfile(tmp_path / name, dtype=np.int32).reshape(-1, 2)
+    r = subprocess.run([os.path.join(bindir, "relabel_naive"), str(tmp_path / "lpBasedGraph.bin")], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(pairs_file("naive"), oracle.relabel(lp, 5)[2])
+    assert np.array_equal(pairs_file("degreeOrder"), oracle.relabel(lp, 0)[2])
+    rt = np.bincount(oracle.relabel(lp, 0)[1][:, 0], minlength=int(lp.max()) + 1)
+    assert "the max runtime degree is %d" % rt.max() in r.stdout
+    r = subprocess.run([os.path.join(bindir, "relabel4lp_out"), str(tmp_path / "lpBasedGraph")], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(pairs_file("normal"), lp)
+    assert np.array_equal(pairs_file("bad"), oracle.relabel(lp, 6)[2])
+    assert np.array_equal(pairs_file("good"), oracle.relabel(lp, 2)[2])
+    r = subprocess.run([os.path.join(bindir, "relabel_random"), str(tmp_path / "lpBasedGraph.bin")], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lookup7, normal7, bad7 = oracle.relabel(lp, 7)
+    assert np.array_equal(pairs_file("normal"), normal7) and np.array_equal(pairs_file("bad"), bad7)
+    assert np.array_equal(pairs_file("good"), oracle.relabel(lp, 0)[2])
+    at = np.argsort(lookup7)  # the vertex at each position of the shuffle
+    assert r.stdout.split("\n")[1:at.size] == [str(x) for x in rt[at[:-1]]]
     r = subprocess.run([os.path.join(bindir, "kcl"), str(e), "-k=4"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "total_num_cliques = %d" % oracle.kclique(g, 4) in r.stdout
@@ -547,6 +598,28 @@ def test_batch_counts_match_per_graph():
     extra = atc.rmat_graph(11, 16, 9)
     b.add(atc.pretc(extra, atc.Dir.DEGREE))
     assert b.run()[0].tolist() == want + [oracle.tc_count(extra)]
+
+
+def _hub_path(k, step):
+    """Vertex 0 joined to k vertices step, 2*step, ..., which form a path: k - 1 triangles."""
+    leaves = [step * i for i in range(1, k + 1)]
+    e = [(0, x) for x in leaves] + list(zip(leaves[:-1], leaves[1:]))
+    return np.array(e, dtype=np.int32)
+
+
+def test_batch_long_lists():
+    """Oriented lists longer than the batch's 32 KB tables: hashed (3000), bitmap (5000) and
+    searched in global memory (4200 over a span of 546 000), in the grouped and the rows items."""
+    gs = [_hub_path(3000, 1), _hub_path(5000, 1), _hub_path(4200, 130), atc.rmat_graph(10, 16, 1)]
+    want = [oracle.tc_count(g) for g in gs]
+    assert want[:3] == [2999, 4999, 4199]
+    b = atc.Batch()
+    for g in gs:
+        b.add(atc.pretc(g, atc.Dir.ID))
+    for t in (None, {"group_by_source": 1}, {"group_by_source": 2}, {"bisson_block_chunk": 64},
+              {"group_by_source": 1, "bisson_block_chunk": 64}):
+        assert b.run(tuning=t)[0].tolist() == want, t
+    b.free()
 
 
 def test_batch_reserve_and_empty():

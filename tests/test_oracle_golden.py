@@ -72,9 +72,11 @@ def test_aorder(golden, name, which):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("which,kind", [("aorder_v2", 1), ("relabel_good", 0), ("relabel4lp", 2)])
+@pytest.mark.parametrize("which,kind", [("aorder_v2", 1), ("relabel_good", 0), ("relabel4lp", 2), ("relabel_naive", 5),
+                                        ("relabel4lp_bad", 6), ("relabel_random", 7)])
 def test_relabel(golden, name, which, kind):
-    """A-order-v2 "naive", relabel-naive "degreeOrder", relabel4lpOut "good" on lpBasedGraph."""
+    """A-order-v2 "naive", relabel-naive "degreeOrder" and "naive", relabel4lpOut "good" and
+    "bad", relabel-random "bad" on lpBasedGraph."""
     c = golden["cases"][name]
     lookup, normal, rel = oracle.relabel(oracle.adirection(golden_input(c)), kind)
     check_pairs(rel, c[which])
@@ -285,3 +287,22 @@ def test_reference_gpu_programs_count_what_the_oracle_counts(golden):
             assert p["rc"] == 0 and p["count"] == want[gname], (gname, pname, p)
             seen += 1
     assert seen >= 4
+
+
+def test_c_library_rand_is_the_published_generator():
+    """The shuffled relabellings replay the C library's rand() on the device from its published
+    description (an additive lagged-Fibonacci generator of degree 31 and separation 3 seeded
+    through 16807 x mod 2^31-1; P. Selinger, "The GLIBC pseudo-random number generator").  The
+    host's rand() after srand(1), the state of a program that never seeds it, is that stream."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srand(1)
+    want = [libc.rand() for _ in range(2000)]
+    r = [1]
+    for i in range(1, 31):
+        r.append(16807 * r[-1] % 2147483647)
+    r += r[0:3]
+    while len(r) < 344 + 2000:
+        r.append((r[-3] + r[-31]) & 0xFFFFFFFF)
+    assert [x >> 1 for x in r[344:]] == want
+    libc.srand(1)
