@@ -211,7 +211,7 @@ ItemShape shape_from(const atc_tuning* t, const ItemShape& base) {
   ItemShape sh = base;
   if (!t) return sh;
   if (t->bisson_cutover > 0) sh.cutover = std::min(t->bisson_cutover, kWarpMax);
-  if (t->bisson_warp_max > 0) sh.warp_max = std::min(t->bisson_warp_max, kWarpMax);
+  if (t->bisson_warp_max > 0) sh.warp_max = std::min(t->bisson_warp_max, kWarpHashMax);
   if (t->bisson_warp_chunk > 0) sh.warp_chunk = t->bisson_warp_chunk;
   if (t->bisson_block_chunk > 0) sh.block_chunk = t->bisson_block_chunk;
   if (t->group_by_source > 0) sh.by_source = t->group_by_source >= 2 ? 2 : 1;

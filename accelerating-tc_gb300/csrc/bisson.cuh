@@ -47,8 +47,9 @@ int blocks_per_sm(const void* kernel, int block, size_t smem) {
 //     (lists too long for both) binary search in global memory.
 // Chunks come from device work counters (one atomicAdd per chunk; nothing waits on them).
 constexpr int kBgWarps = 8;
-constexpr int kWarpMax = 256;       // longest N+(h) handled by one warp
+constexpr int kWarpMax = 256;       // longest N+(h) handled by one warp unless tuned
 constexpr int kWarpSlots = 1024;    // warp-private hash slots (4 KB)
+constexpr int kWarpHashMax = kWarpSlots / 2;  // longest N+(h) a warp item can hash (load 1/2)
 constexpr int kWarpChunk = 512;     // partners per warp item
 constexpr int kBlockChunk = 2048;   // partners per block item
 constexpr int kTabWords = 16384;    // block table limit: 64 KB of slots or bitmap words
@@ -116,7 +117,7 @@ __global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* 
 
 // Pass 3: cut every group into work items; counters[0] = warp items, [1] = block items,
 // [3] = longest N+(h) among block items.
-// Runtime shape of the work items: lists up to warp_max (<= kWarpMax) go to warp
+// Runtime shape of the work items: lists up to warp_max (<= kWarpHashMax) go to warp
 // items of warp_chunk partners, longer ones to block items of block_chunk partners.
 struct ItemShape {
   int cutover;      // warp items: sorted copy up to this length, hash above
@@ -665,8 +666,8 @@ __global__ void __launch_bounds__(kBgWarps * 32, Items::kMinBlocks) bisson_warp_
       __syncwarp();
       for (int j = lane; j < dh; j += 32) T[j] = -1;
     } else {
-      uint32_t cap = 64;
-      while (cap < 4u * (uint32_t)dh) cap <<= 1;
+      uint32_t cap = 64;  // load 1/4, or up to 1/2 for lists longer than kWarpSlots / 4
+      while (cap < 4u * (uint32_t)dh && cap < (uint32_t)kWarpSlots) cap <<= 1;
       const uint32_t mask = cap - 1;
       for (int j = lane; j < dh; j += 32) hash_insert<S>(T, mask, __ldg(g.cols + hb + j));
       __syncwarp();

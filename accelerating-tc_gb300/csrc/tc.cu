@@ -641,7 +641,7 @@ static atc_status item_shape(const atc_tuning* t, ItemShape* sh, int* slots) {
   ATC_CHECK_ARG(t->bisson_slots == 0 || t->bisson_slots == 1 || t->bisson_slots == 2 || t->bisson_slots == 4,
                 "bisson_slots must be 0, 1, 2 or 4");
   if (t->bisson_cutover > 0) sh->cutover = std::min(t->bisson_cutover, kWarpMax);
-  if (t->bisson_warp_max > 0) sh->warp_max = std::min(t->bisson_warp_max, kWarpMax);
+  if (t->bisson_warp_max > 0) sh->warp_max = std::min(t->bisson_warp_max, kWarpHashMax);
   if (t->bisson_warp_chunk > 0) sh->warp_chunk = std::max(t->bisson_warp_chunk, 32);
   if (t->bisson_block_chunk > 0) sh->block_chunk = std::max(t->bisson_block_chunk, 32);
   if (t->bisson_slots > 0) *slots = t->bisson_slots;

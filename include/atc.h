@@ -140,7 +140,7 @@ typedef struct atc_tuning {
   int32_t fox_rearrange;     /* interleave each bin's edges (Fox/tc.cu:127-183) */
   int32_t fox_work_per_thread; /* bin base of the threads-per-edge bins (8) */
   int32_t tricore_blocks;    /* CTAs of the TriCore-style kernel (0: auto) */
-  int32_t bisson_warp_max;   /* longest list a warp item handles, <= 256 (256) */
+  int32_t bisson_warp_max;   /* longest list a warp item handles, <= 512 (256) */
   int32_t bisson_warp_chunk; /* partners per warp item (512) */
   int32_t bisson_block_chunk; /* partners per block item (2048) */
   int32_t bisson_slots;      /* hash slots per bucket of the tables: 1, 2 or 4 (0: default) */

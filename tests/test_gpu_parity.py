@@ -229,7 +229,9 @@ def test_tuning_knobs_do_not_change_counts():
     for t in ({"bisson_cutover": 8}, {"bisson_cutover": 64}, {"fox_rearrange": 1, "edge_kernels": 1},
               {"fox_work_per_thread": 4, "edge_kernels": 1}, {"edge_kernels": 1},
               {"hu_blocks": 7}, {"tricore_blocks": 3, "edge_kernels": 1}, {"hu_blocks": 2000}, {"bisson_slots": 1},
-              {"bisson_slots": 2}, {"bisson_slots": 4}, {"bisson_slots": 2, "bisson_warp_max": 64, "bisson_cutover": 4}):
+              {"bisson_slots": 2}, {"bisson_slots": 4}, {"bisson_slots": 2, "bisson_warp_max": 64, "bisson_cutover": 4},
+              {"bisson_warp_max": 512}, {"bisson_warp_max": 384, "bisson_slots": 2},
+              {"bisson_warp_max": 512, "bisson_slots": 1, "bisson_warp_chunk": 64}):
         for k in KERNELS:
             assert atc.tc(csr, k, tuning=t)[0] == want, (t, k.name)
 
@@ -587,7 +589,8 @@ def test_batch_counts_match_per_graph():
     counts2, _ = b.run()  # a second replay of the same captured graph
     assert counts2.tolist() == want
     for t in ({"bisson_cutover": 8, "bisson_warp_max": 64}, {"bisson_warp_chunk": 32, "bisson_block_chunk": 64},
-              {"bisson_warp_max": 256, "bisson_cutover": 256}, {"group_by_source": 1},
+              {"bisson_warp_max": 256, "bisson_cutover": 256}, {"bisson_warp_max": 512}, {"group_by_source": 1},
+              {"group_by_source": 1, "bisson_warp_max": 512},
               {"group_by_source": 1, "bisson_warp_max": 64, "bisson_warp_chunk": 32}, {"group_by_source": 2},
               {"group_by_source": 2, "bisson_warp_max": 64, "bisson_warp_chunk": 32}):
         assert b.run(tuning=t)[0].tolist() == want, t
