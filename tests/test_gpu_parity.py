@@ -236,6 +236,26 @@ def test_tuning_knobs_do_not_change_counts():
             assert atc.tc(csr, k, tuning=t)[0] == want, (t, k.name)
 
 
+def test_warp_tables_at_their_limits():
+    """Hubs whose oriented lists are 255, 256 and 257 long (the compact 16-bit warp tables
+    hold up to 256 keys; 257 takes the 32-bit table), each joined to a path of its leaves, plus
+    a dense core: Bisson- and Hu-style counts with the default and the tuned item shapes."""
+    e = []
+    base = 0
+    for k in (255, 256, 257):
+        leaves = list(range(base + 1, base + 1 + k))
+        e += [(base, x) for x in leaves] + list(zip(leaves[:-1], leaves[1:]))
+        base += k + 1
+    e += [(base + a, base + b) for a in range(40) for b in range(a + 1, 40)]
+    g = np.array(e, dtype=np.int32)
+    want = oracle.tc_count(g)
+    assert want == 254 + 255 + 256 + 40 * 39 * 38 // 6
+    csr = atc.pretc(g, atc.Dir.ID)
+    for t in (None, {"bisson_cutover": 4}, {"bisson_warp_max": 512}, {"bisson_slots": 2}):
+        for k in (atc.Kernel.BISSON, atc.Kernel.HU):
+            assert atc.tc(csr, k, tuning=t)[0] == want, (t, k.name)
+
+
 def test_bad_slot_count_rejected():
     csr = atc.pretc(atc.rmat_graph(8, 8, 1), atc.Dir.DEGREE)
     for k in (atc.Kernel.BISSON, atc.Kernel.HU):
