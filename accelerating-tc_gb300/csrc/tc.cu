@@ -262,11 +262,16 @@ __global__ void fox_deal_kernel(const uint64_t* keys, const int64_t* list, int64
 //   KIND 0, TriCore-style (tricount_gpu.cu:215-290): 32 samples of the longer list (the
 //     reference's per-warp pivot cache) sit contiguous in shared memory, so the first five
 //     levels of every search touch 32 distinct banks; the sample bracket holding the
-//     element is then binary-searched.
+//     element is then binary-searched.  Every bracket of a list holds at most ceil(d/32)
+//     elements, so the bracket search is a fixed run of halving steps, the same number on
+//     every lane, without a loop test or a bound test per step (a read past the list is
+//     clamped to its last element, which is not below the element searched).
 //   KIND 1, Fox-style (Fox/tc.cu:64-125): a lane's successive elements of a list ascend, so
 //     each search gallops forward from where the lane's previous one ended (restarting
 //     when the element is smaller than the previous one), then binary-searches the last
 //     step.
+constexpr int kLiftMax = 11;  // the unrolled bracket search covers brackets of up to 4095
+
 template <int KIND>
 struct SortedProber {
   const int32_t* T;    // sorted N+(h) (shared memory, or global for lists beyond it)
@@ -276,6 +281,8 @@ struct SortedProber {
   int prev;      // Fox: lower bound of the lane's previous element
   int32_t last;  // Fox: the lane's previous element
   int gap;       // Fox: how far the lane's previous forward search moved
+  int lg = -1;   // TriCore: floor(log2(ceil(d/32))), the first halving step of the bracket search
+                 // (the same for the whole list); -1: the bracket is searched by a loop
   __device__ __forceinline__ unsigned probe(int32_t x, bool valid) {
     if (!valid) return 0u;
     if (x > hi) return 0u;  // above the longer list: no search
@@ -289,6 +296,32 @@ struct SortedProber {
       if (piv[k - 1] == x) return 1u;
       int b = (int)(((int64_t)(k - 1) * d) >> 5) + 1;  // strictly inside the bracket
       int e = k == 32 ? d : (int)(((int64_t)k * d) >> 5);
+      if (lg >= 0 && lg <= kLiftMax) {
+        // the last index below x: T[b-1] (the sample) is below x, and 2^(lg+1) - 1 steps cover
+        // the bracket; T[e] (the next sample, or past the list) is not below x
+        int lo = b - 1;
+#define ATC_LIFT(t) \
+  case t: {        \
+    const int c = lo + (1 << t); \
+    if (T[min(c, d - 1)] < x) lo = c; \
+  }
+        switch (lg) {  // enters at the first step and falls through the rest
+          ATC_LIFT(11) [[fallthrough]];
+          ATC_LIFT(10) [[fallthrough]];
+          ATC_LIFT(9) [[fallthrough]];
+          ATC_LIFT(8) [[fallthrough]];
+          ATC_LIFT(7) [[fallthrough]];
+          ATC_LIFT(6) [[fallthrough]];
+          ATC_LIFT(5) [[fallthrough]];
+          ATC_LIFT(4) [[fallthrough]];
+          ATC_LIFT(3) [[fallthrough]];
+          ATC_LIFT(2) [[fallthrough]];
+          ATC_LIFT(1) [[fallthrough]];
+          ATC_LIFT(0)
+        }
+#undef ATC_LIFT
+        return lo + 1 < d && T[lo + 1] == x;
+      }
       while (b < e) {
         const int mid = (b + e) >> 1;
         if (T[mid] < x) b = mid + 1; else e = mid;
@@ -423,7 +456,7 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_warp_kernel(CsrView g, c
     __syncwarp();
     int64_t cur = gi.b;
     auto nb = [&]() { int64_t r = cur; cur += 32; return r; };
-    SortedProber<KIND> pr{L, piv[w], dh, L[dh - 1], 0, INT32_MIN, 16};
+    SortedProber<KIND> pr{L, piv[w], dh, L[dh - 1], 0, INT32_MIN, 16, 31 - __clz((dh + 31) >> 5)};
     total += stream_partners(g, plist, gi.e, lane, nb, pr);
     __syncwarp();  // the next item overwrites the copy
   }
@@ -482,7 +515,8 @@ __global__ void __launch_bounds__(kBgWarps * 32) sorted_block_kernel(CsrView g, 
       if (lane == 0) r = atomicAdd(&bnext, 32ull);
       return gi.b + (int64_t)__shfl_sync(0xffffffffu, r, 0);
     };
-    SortedProber<KIND> pr{L, piv, (int)dh, __ldg(g.cols + hb + dh - 1), 0, INT32_MIN, 16};
+    SortedProber<KIND> pr{L, piv, (int)dh, __ldg(g.cols + hb + dh - 1), 0, INT32_MIN, 16,
+                          31 - __clz((int)((dh + 31) >> 5))};
     total += stream_partners(g, plist, gi.e, lane, nb, pr);
     __syncthreads();  // the next item overwrites the copy
   }
