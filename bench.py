@@ -216,23 +216,24 @@ def cpu_baseline(g_lower_off, g_lower_cols, m_total, target_s):
     t0 = time.perf_counter()
     cnt, e = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride, 0, nthreads)
     dt = time.perf_counter() - t0
-    # the same count on one host thread, on a sample of the same kind of about a third of the
-    # wall time (vertex 0, the top hub, is in phase 0 of every stride and is left out by
-    # starting at 1; the stride is calibrated, since a sample's edges are not proportional to
-    # its vertices on a skewed graph)
-    stride1 = max(1, n // 64)
-    for _ in range(4):
+    # the same count on one host thread: successive phases of a fine stride (each call a few
+    # thousand vertices) until about a third of the all-core time has passed, so the sample's
+    # length is bounded by the clock and not by how its edges fall on a skewed graph
+    stride1 = max(2, n // 4096)
+    e1, dt1, calls = 0, 0.0, 0
+    for phase in range(1, stride1):
         t0 = time.perf_counter()
-        _, e1 = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride1, 1, 1)
-        dt1 = time.perf_counter() - t0
-        if dt1 > target_s / 6 or stride1 == 1:
+        _, e_p = oracle.tc_count_lower_sample(g_lower_off, g_lower_cols, stride1, phase, 1)
+        dt1 += time.perf_counter() - t0
+        e1 += e_p
+        calls += 1
+        if dt1 >= target_s / 3:
             break
-        stride1 = max(1, int(stride1 * dt1 / (target_s / 3))) if dt1 > 0 else max(1, stride1 // 16)
     return {"value": e / dt if dt > 0 else None, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": "every %d-th vertex u (%d of %d) with all its smaller-neighbour edges (%d of %d edges); %.1f s"
             % (stride, (n + stride - 1) // stride, n, e, m_total, dt),
             "one_thread": {"value": e1 / dt1 if dt1 > 0 else None, "unit": UNIT, "cores": 1,
-                           "sample": "every %d-th vertex u from vertex 1 (%d edges), %.1f s" % (stride1, e1, dt1)},
+                           "sample": "phases 1..%d of every %d-th vertex u (%d edges), %.1f s" % (calls, stride1, e1, dt1)},
             "machine": os.uname().machine}
 
 
