@@ -359,6 +359,14 @@ atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uin
   if (n_v <= 0) return ATC_OK;
   const bool as_given = kind == ATC_RELABEL_OUTDEG_DESC || kind == ATC_RELABEL_OUTDEG_SHUFFLED;
   ATC_CHECK_ARG(!as_given || pairs != nullptr, "OUTDEG_DESC / OUTDEG_SHUFFLED need pairs");
+  if (kind == ATC_RELABEL_RANDOM) {  // the degree list plays no part (relabel-random.cpp:77-89)
+    DevBuf<int32_t> perm;
+    ATC_TRY(perm.alloc(n_v, s));
+    ATC_TRY(shuffle_ids(perm.p, n_v, s));
+    inverse_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(perm.p, n_v, lookup);
+    ATC_CK(cudaGetLastError());
+    if (!oriented || ne == 0) return ATC_OK;  // else the degree-oriented pairs below
+  }
   DevBuf<int32_t> deg, rt;
   DevBuf<int> mx;
   ATC_TRY(rt.alloc(n_v, s));
@@ -376,14 +384,7 @@ atc_status relabel_lookup(const int2* pairs, const uint64_t* keys, int bits, uin
     rt_kernel<<<grid_for(ne, 256), 256, 0, s>>>(pairs, keys, bits, ne, deg.p, rt.p, oriented);
   }
   ATC_CK(cudaGetLastError());
-  if (kind == ATC_RELABEL_RANDOM) {  // the degree list plays no part (relabel-random.cpp:77-89)
-    DevBuf<int32_t> perm;
-    ATC_TRY(perm.alloc(n_v, s));
-    ATC_TRY(shuffle_ids(perm.p, n_v, s));
-    inverse_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(perm.p, n_v, lookup);
-    ATC_CK(cudaGetLastError());
-    return ATC_OK;
-  }
+  if (kind == ATC_RELABEL_RANDOM) return ATC_OK;
   rt_hist_kernel<<<grid_for(n_v, 256), 256, 0, s>>>(rt.p, n_v, nullptr, mx.p);
   ATC_CK(cudaGetLastError());
   int maxrt = 0;
