@@ -42,3 +42,22 @@ def test_kcl_cpu_sample_is_calibrated():
     assert time.perf_counter() - t0 < 30
     assert set(s) == {"stride", "edges", "seconds", "edges_per_s", "cores", "kind"}
     assert 1 <= s["stride"] < n // 16 and s["edges"] > 0 and s["kind"] == "port"
+
+
+def test_cpu_baseline_samples_are_bounded_by_the_clock():
+    # the GPU line's CPU baseline: an all-core sample calibrated to the target and a one-thread
+    # sample that stops after about a third of it, both labelled
+    import time
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bench
+    import oracle
+    raw = oracle.gen_rmat(16, 16, 1)
+    loff, lcols = oracle.lower_csr(raw)
+    t0 = time.perf_counter()
+    r = bench.cpu_baseline(loff, lcols, int(loff[-1]), 1.5)
+    assert time.perf_counter() - t0 < 30
+    assert r["kind"] == "port" and r["cores"] >= 1 and r["value"] > 0
+    one = r["one_thread"]
+    assert one["cores"] == 1 and one["value"] > 0 and one["unit"] == r["unit"]
+    assert "phases 1.." in one["sample"]
