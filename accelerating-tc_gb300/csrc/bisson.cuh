@@ -70,9 +70,20 @@ __device__ __forceinline__ bool longer_is_u(int32_t u, int32_t v, int64_t du, in
   return du > dv || (du == dv && u < v);
 }
 
+// Out-degrees as int32: the grouping passes read a random vertex's degree with one 4-byte
+// load from an array half the size of the offsets (it stays in L2 at R-MAT scale 24).
+__global__ void csr_outdeg_kernel(CsrView g, int32_t* deg) {
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < g.n; u += (int64_t)gridDim.x * blockDim.x)
+    deg[u] = (int32_t)(g.off[u + 1] - g.off[u]);
+}
+
+__device__ __forceinline__ int64_t degree_of(const CsrView& g, const int32_t* deg, int32_t v) {
+  return deg ? (int64_t)__ldg(deg + v) : g.off[v + 1] - g.off[v];
+}
+
 // Pass 1: partners per group, with warp-aggregated atomics (edges of one source are
-// contiguous, so runs of one h are common).
-__global__ void group_count_kernel(CsrView g, int32_t* cnt) {
+// contiguous, so runs of one h are common).  deg (nullable): the out-degrees.
+__global__ void group_count_kernel(CsrView g, int32_t* cnt, const int32_t* deg) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t w_pad = (g.e1 - g.e0 + 31) & ~31ll;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < w_pad; i += stride) {
@@ -80,7 +91,7 @@ __global__ void group_count_kernel(CsrView g, int32_t* cnt) {
     int32_t h = -1;
     if (e < g.e1) {
       int32_t u = g.esrc[e], v = g.cols[e];
-      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      int64_t du = degree_of(g, deg, u), dv = degree_of(g, deg, v);
       if (du > 0 && dv > 0) h = longer_is_u(u, v, du, dv) ? u : v;
     }
     unsigned same = __match_any_sync(0xffffffffu, h);
@@ -90,7 +101,8 @@ __global__ void group_count_kernel(CsrView g, int32_t* cnt) {
 }
 
 // Pass 2: scatter partners into their group (order inside a group is irrelevant).
-__global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist) {
+__global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* cur, int32_t* plist,
+                                     const int32_t* deg) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t w_pad = (g.e1 - g.e0 + 31) & ~31ll;
   const int lane = threadIdx.x & 31;
@@ -99,7 +111,7 @@ __global__ void group_scatter_kernel(CsrView g, const int64_t* gstart, int32_t* 
     int32_t h = -1, p = 0;
     if (e < g.e1) {
       int32_t u = g.esrc[e], v = g.cols[e];
-      int64_t du = g.off[u + 1] - g.off[u], dv = g.off[v + 1] - g.off[v];
+      int64_t du = degree_of(g, deg, u), dv = degree_of(g, deg, v);
       if (du > 0 && dv > 0) {
         bool hu = longer_is_u(u, v, du, dv);
         h = hu ? u : v;

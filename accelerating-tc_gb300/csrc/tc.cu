@@ -722,7 +722,7 @@ static atc_status run_hu(const CsrView& g, const atc_tuning* t, unsigned long lo
 // with the longer list, the partners of each h contiguous in plist, cut into warp and block
 // items.  hc = {warp items, block items, -, longest hashed block list}.
 struct Grouping {
-  DevBuf<int32_t> cnt, cur, plist;
+  DevBuf<int32_t> cnt, cur, plist, deg;
   DevBuf<int64_t> gstart;
   DevBuf<int> counters;  // warp items, block items, (unused), longest block list, warp next, block next
   DevBuf<GroupItem> witems, bitems;
@@ -737,14 +737,18 @@ static atc_status group_edges(const CsrView& g, const ItemShape& sh, Grouping* g
   ATC_CK(cudaMemsetAsync(gr->cnt.p, 0, sizeof(int32_t) * (g.n + 1), s));
   ATC_CK(cudaMemsetAsync(gr->cur.p, 0, sizeof(int32_t) * g.n, s));
   ATC_CK(cudaMemsetAsync(gr->counters.p, 0, sizeof(int) * 8, s));
-  group_count_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gr->cnt.p);
+  ATC_TRY(gr->deg.alloc(g.n + 1, s));
+  csr_outdeg_kernel<<<grid_for(g.n, 256), 256, 0, s>>>(g, gr->deg.p);
+  ATC_CK(cudaGetLastError());
+  group_count_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gr->cnt.p, gr->deg.p);
   ATC_CK(cudaGetLastError());
   ATC_TRY(exclusive_scan_i32_to_i64(gr->cnt.p, gr->gstart.p, g.n + 1, s));
   int64_t total = 0;
   ATC_CK(cudaMemcpyAsync(&total, gr->gstart.p + g.n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
   ATC_TRY(gr->plist.alloc(total + 32, s));
-  group_scatter_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gr->gstart.p, gr->cur.p, gr->plist.p);
+  group_scatter_kernel<<<grid_for(g.e1 - g.e0, 256), 256, 0, s>>>(g, gr->gstart.p, gr->cur.p, gr->plist.p,
+                                                                   gr->deg.p);
   ATC_CK(cudaGetLastError());
   // items: at most one per group plus one per chunk boundary
   int64_t max_items = g.n + total / std::min(sh.warp_chunk, sh.block_chunk) + 1;
@@ -755,7 +759,7 @@ static atc_status group_edges(const CsrView& g, const ItemShape& sh, Grouping* g
   ATC_CK(cudaGetLastError());
   ATC_CK(cudaMemcpyAsync(gr->hc, gr->counters.p, sizeof(gr->hc), cudaMemcpyDeviceToHost, s));
   ATC_CK(cudaStreamSynchronize(s));
-  *launches += 4;
+  *launches += 5;
   return ATC_OK;
 }
 
@@ -959,9 +963,9 @@ static atc_status tc_noalloc_impl(const int64_t* off, const int32_t* cols, int64
   esrc_fill_kernel<<<grid_for(n * 32, 256), 256, 0, s>>>(off, n, esrc);
   ATC_CK(cudaGetLastError());
   CsrView g = csr_view(off, cols, esrc, n, m);
-  group_count_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, cnt);
+  group_count_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, cnt, nullptr);
   scan_one_block_kernel<<<1, 1024, 0, s>>>(cnt, n + 1, gstart);
-  group_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, gstart, cur, plist);
+  group_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(g, gstart, cur, plist, nullptr);
   group_items_kernel<<<grid_for(n, 256), 256, 0, s>>>(g, gstart, witems, bitems, counters, default_shape(32), 0,
                                                        INT64_MAX);
   ATC_CK(cudaGetLastError());
