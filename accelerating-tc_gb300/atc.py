@@ -153,6 +153,7 @@ _SIGS = {
     "atc_set_alloc_budget": (C.c_int, [C.c_int64]),
     "atc_phase_timing": (C.c_int, [C.c_int32]),
     "atc_phase_times": (C.c_int, [C.POINTER(PhaseTimeStruct), C.c_int32, C.POINTER(C.c_int32)]),
+    "atc_check_wait_timeout": (C.c_int, [_P]),
     "atc_gen_rmat_host": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, C.c_int]),
     "atc_gen_rmat_device": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, _P, _P]),
     "atc_gen_rgg_host": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, _P, C.c_uint64, C.POINTER(C.c_uint64), C.c_int]),
@@ -265,6 +266,12 @@ def phase_times(cap=256):
     n = C.c_int32(0)
     _check(lib().atc_phase_times(buf, cap, C.byref(n)))
     return [(buf[i].name.decode(), buf[i].depth, buf[i].ms) for i in range(min(n.value, cap))]
+
+
+def check_wait_timeout(stream=None):
+    """Runs the library's bounded-wait check: returns the status of a wait that cannot
+    complete (Status.ERR_TIMEOUT when it gave up within its limit, as it must)."""
+    return Status(lib().atc_check_wait_timeout(stream))
 
 
 GRAPH500 = (570000, 190000, 190000)

@@ -368,9 +368,15 @@ struct SortedProber {
 // 16-byte boundaries and the size is a multiple of 16 bytes: a list is copied from the
 // 16-byte boundary at or below its first element to the one at or above its end (the CSR's
 // cols carry 16 ints of padding, so the rounded end stays inside the allocation), and read
-// from the offset of its first element.  Every wait is bounded: a wait that runs out records
-// an error for the host (ATC_ERR_TIMEOUT) and the kernel stops counting.
-constexpr uint32_t kBulkWaitPolls = 1u << 22;
+// from the offset of its first element.  Every wait is bounded in time: a wait that runs out
+// records an error for the host (ATC_ERR_TIMEOUT) and the kernel stops counting.
+constexpr uint64_t kBulkWaitNs = 1000000000ull;  // one second without the copy landing
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -391,9 +397,10 @@ __device__ __forceinline__ void bulk_list_to_smem(int32_t* dst, const int32_t* s
                : "memory");
 }
 
-// Waits for phase `parity` of the barrier to complete; false if kBulkWaitPolls polls did not see it.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kBulkWaitPolls; ++i) {
+// Waits for phase `parity` of the barrier to complete; false if it did not within limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kBulkWaitNs) {
+  const uint64_t t0 = global_ns();
+  for (;;) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -401,8 +408,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     if (done) return true;
+    if (global_ns() - t0 > limit_ns) return false;
   }
-  return false;
+}
+
+// The bounded wait's failure path, for tests: a barrier whose phase announces 16 bytes that
+// no copy delivers (one arrival, its transaction count never reached), waited on with
+// limit_ns.  err = 1 when the wait gave up, as it must; nothing is in flight at exit.
+__global__ void wait_timeout_check_kernel(uint64_t limit_ns, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(&bar)), "r"(16u)
+                 : "memory");
+  }
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0, limit_ns);
+  if (!ok && threadIdx.x == 0) *err = 1;
 }
 
 // The 16-byte-aligned window [a0, a1) of cols holding the list [hb, hb + dh).
@@ -1107,4 +1129,21 @@ extern "C" atc_status atc_tc_noalloc(const int64_t* offsets, const int32_t* cols
   if (m == 0 || n == 0) return ATC_OK;
   ATC_CHECK_ARG(offsets != nullptr && cols != nullptr, "NULL CSR array");
   return tc_noalloc_impl(offsets, cols, n, m, count, as_stream(st));
+} ATC_CATCH
+
+extern "C" atc_status atc_check_wait_timeout(atc_stream st) try {
+  cudaStream_t s = as_stream(st);
+  DevBuf<int> err;
+  ATC_TRY(err.alloc(1, s));
+  ATC_CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  atc::wait_timeout_check_kernel<<<1, 32, 0, s>>>(1000000ull, err.p);  // a 1 ms limit
+  ATC_CK(cudaGetLastError());
+  int h = 0;
+  ATC_CK(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  ATC_CK(cudaStreamSynchronize(s));
+  if (h) {
+    atc::set_error("a bulk-copy wait gave up after its time limit (the check's barrier never completes)");
+    return ATC_ERR_TIMEOUT;
+  }
+  return ATC_OK;
 } ATC_CATCH

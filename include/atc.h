@@ -209,6 +209,12 @@ typedef struct atc_phase_time {
 } atc_phase_time;
 atc_status atc_phase_timing(int32_t enable);
 atc_status atc_phase_times(atc_phase_time* out, int32_t cap, int32_t* n);
+/* The bounded-wait failure path, for tests: the counting kernels that stage lists with bulk
+   copies wait on an mbarrier for at most one second, then stop and report ATC_ERR_TIMEOUT.
+   This runs a one-CTA kernel whose barrier can never complete (bytes announced, no copy
+   issued) with a 1 ms limit: it returns ATC_ERR_TIMEOUT when the wait gave up, as it must,
+   ATC_OK if it did not, and leaves the device usable.  No counterpart in the reference. */
+atc_status atc_check_wait_timeout(atc_stream s);
 /* Makes `device` current on the calling thread and initialises its context.  device = -1
    initialises the calling thread's current device and leaves the current device as it is. */
 atc_status atc_init(int device);

@@ -130,3 +130,20 @@ def test_batch_replay_stages(tuning):
     assert all(ms >= 0 for _, _, ms in stages)
     assert sum(ms for _, _, ms in stages) <= ph[0][2] * 1.05 + 0.05
     assert st.launches >= 3
+
+
+def test_bounded_wait_gives_up_and_leaves_the_device_usable():
+    """The staged kernels' bulk-copy waits are bounded in time: a wait on a barrier that can
+    never complete gives up within its limit and is reported as ERR_TIMEOUT; the context stays
+    usable and the next counts are exact."""
+    import time
+    g, want = _small()
+    for _ in range(3):
+        t0 = time.perf_counter()
+        assert atc.check_wait_timeout() == atc.Status.ERR_TIMEOUT
+        assert time.perf_counter() - t0 < 5.0
+        assert "time limit" in atc.lib().atc_last_error().decode()
+        csr = atc.pretc(g, atc.Dir.ADIRECTION)
+        for k in (atc.Kernel.TRICORE, atc.Kernel.FOX):
+            assert atc.tc(csr, k)[0] == want
+        csr.free()
