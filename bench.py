@@ -76,6 +76,7 @@ def parse():
                     help="tc mode: graphs of the reduced batch leg (every (4096 / N)-th graph of the 4096-graph "
                          "batch; 0 = no batch leg)")
     ap.add_argument("--no-select-leg", action="store_true", help="tc mode: skip the selector leg")
+    ap.add_argument("--no-kcl-leg", action="store_true", help="tc mode: skip the k-clique leg")
     ap.add_argument("--prep-scale", type=int, default=20,
                     help="R-MAT scale of the reference preprocessing programs' timed run (0 = skip)")
     return ap.parse_args()
@@ -484,6 +485,8 @@ def run_ours(a):
         line["batch_leg"] = batch_leg(a, idx, ["bisson", "hu"], sp, stream)
     if rank == 0 and world == 1 and not a.no_select_leg:
         line["select_leg"] = select_leg()
+    if rank == 0 and world == 1 and not a.no_kcl_leg:
+        line["kcl_leg"] = kcl_leg(sp)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         import oracle
         off, cols = oracle.lower_csr(host_raw.numpy())
@@ -719,6 +722,35 @@ def run_batch(a):
         list(range(0, 4096, max(1, 4096 // a.batch_graphs)))[: a.batch_graphs]
     line = {"mode": "batch", **batch_leg(a, idx, [x.strip() for x in a.batch_plain_kernels.split(",")], sp)}
     print(json.dumps(line), flush=True)
+
+
+def kcl_leg(sp):
+    """The k-clique configuration's RGG (n = 2^20, mean degree 32, seed 1, A-direction) at
+    k = 4..7: device time of one atc_kcl call per k (after a warm-up call), each count checked
+    against the oracle's count pinned in tests/golden/config_pins.json."""
+    import ctypes as C
+    import torch
+    import atc
+    with open(os.path.join(ROOT, "tests", "golden", "config_pins.json")) as f:
+        pins = json.load(f)["kcl"]["rgg20"]
+    src = pins["source"]
+    n = int(src["n"])
+    cnt = C.c_uint64(0)
+    cap = n * 20
+    dev = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    assert atc.lib().atc_gen_rgg_device(n, float(src["mean_degree"]), int(src["seed"]), dev.data_ptr(), cap,
+                                        C.byref(cnt), sp) == 0
+    csr = atc.pretc_device(dev.data_ptr(), int(cnt.value), atc.Dir.ADIRECTION, stream=sp)
+    del dev
+    out = {"graph": "RGG n=2^20 mean degree 32 seed 1, A-direction", "n": csr.n, "m": csr.m, "k": {}}
+    for k in range(4, 8):
+        atc.kcl(csr, k, stream=sp)
+        c, st = atc.kcl(csr, k, stream=sp)
+        out["k"][str(k)] = {"cliques": c, "ms": st.kernel_ms, "cliques_per_s": c / (st.kernel_ms * 1e-3),
+                            "matches_oracle": c == int(pins["cliques"][str(k)])}
+    csr.free()
+    torch.cuda.empty_cache()
+    return out
 
 
 def select_leg():
