@@ -9,7 +9,11 @@ A step counts the triangles of the resident oriented CSR once with the headline 
 the 1+ GB CSR exceeds the 129 MB L2, so no flush is needed between steps).  `e2e` is the
 same metric through the public C ABI with host buffers: every step copies the raw
 int32 pairs from pinned host memory, builds the CSR (dedup, A-order, A-direction),
-counts and reads the count back.  Every kernel family is also timed ("kernels").
+counts and reads the count back.  Every kernel family is also timed ("kernels").  The
+single-GPU line also carries a reduced batch leg (256 of the 4096 Chung-Lu graphs, batched
+against per-graph loops), the learned selector on its committed timing fixture, a k-clique
+leg (the RGG configuration at k = 4..7), and the CPU baseline (all cores and one thread, and
+the reference's own preprocessing programs).
 
 With N > 1 ranks (torchrun, NCCL) every rank builds the same CSR, each step counts the rank's
 work-balanced part of the edges (atc_tc_part) and sums the parts with one all_reduce: the
